@@ -1,0 +1,234 @@
+/*
+ * vmp.h -- C ABI of libvmp.so, the GB300 (sm_103a) odometry hot path of a
+ * FAST-LIO2 + VoxelMapPlus LiDAR-inertial odometry node.
+ *
+ * One vmp_stream_t owns the complete device-resident state of one sensor
+ * stream: the voxel plane map (hash, voxel records, point slabs, LRU queue),
+ * the iterated error-state Kalman filter (state x, covariance P) and the
+ * per-point residual records.  Every call enqueues CUDA kernels on the
+ * stream's own CUDA stream; there is no CPU fallback: a library that cannot
+ * reach a GPU fails vmp_create with VMP_ERR_CUDA.
+ *
+ * Reference call surface each entry point replaces (paths are relative to the
+ * voxel_plus package of liangheming/VoxelMapPlus_FASTLIO2):
+ *   vmp_create / vmp_destroy     lio::LIOBuilder::loadConfig   src/map_builder/lio_builder.cpp:5-26
+ *   vmp_process                  lio::LIOBuilder::process      src/map_builder/lio_builder.cpp:175-248
+ *   vmp_undistort                lio::LIOBuilder::undistortCloud src/map_builder/lio_builder.cpp:65-153
+ *   vmp_downsample               pcl::VoxelGrid filter call    src/map_builder/lio_builder.cpp:215-223
+ *   vmp_map_index                lio::VoxelMap::index          src/map_builder/voxel_map.cpp:194-198
+ *   vmp_map_build                lio::VoxelMap::build          src/map_builder/voxel_map.cpp:200-230
+ *   vmp_map_update               lio::VoxelMap::update         src/map_builder/voxel_map.cpp:232-256
+ *   vmp_residual_reduce          lio::LIOBuilder::sharedUpdateFunc src/map_builder/lio_builder.cpp:250-311
+ *   vmp_ieskf_predict            kf::IESKF::predict            src/map_builder/ieskf.cpp:101-123
+ *   vmp_ieskf_update             kf::IESKF::update             src/map_builder/ieskf.cpp:125-156
+ *   vmp_get_state / vmp_set_state kf::IESKF::x(), P(), change_x, change_P  src/map_builder/ieskf.h:86-94
+ *   vmp_map_export / vmp_map_import  direct featmap access by the node  src/utils.cpp:154-208
+ *
+ * Conventions: all matrices are row-major double.  Points are float as in
+ * pcl::PointXYZINormal; the per-point time is the field the reference keeps in
+ * `curvature` (milliseconds since the scan start, src/utils.cpp:20).
+ * No exception crosses the ABI; every entry point returns a vmp_status and
+ * vmp_last_error() gives a human-readable reason.  A handle is not
+ * re-entrant: one caller thread per handle.
+ */
+#ifndef VMP_H_
+#define VMP_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VMP_ABI_VERSION 1
+
+typedef enum vmp_status {
+    VMP_OK = 0,
+    VMP_ERR_INVALID_ARG = 1,      /* bad pointer, size or configuration */
+    VMP_ERR_OUT_OF_MEMORY = 2,    /* device allocation failed */
+    VMP_ERR_ADMISSION_DENIED = 3, /* server HBM budget would be exceeded */
+    VMP_ERR_HASH_FULL = 4,        /* voxel hash table has no free slot */
+    VMP_ERR_TIMEOUT = 5,          /* a bounded device wait gave up */
+    VMP_ERR_CUDA = 6,             /* CUDA runtime error (no GPU, launch failure) */
+    VMP_ERR_KEY_RANGE = 7,        /* a voxel index left the packed 21-bit range */
+    VMP_ERR_STATE = 8,            /* call not valid in the current stream state */
+    VMP_ERR_CAPACITY = 9          /* a per-call size exceeds the configured maximum */
+} vmp_status;
+
+/* lio::LIOStatus (lio_builder.h:10-16) */
+typedef enum vmp_lio_status {
+    VMP_IMU_INIT = 0,
+    VMP_MAP_INIT = 1,
+    VMP_LIO_MAPPING = 2
+} vmp_lio_status;
+
+/* Mirrors lio::LIOConfig (lio_builder.h:17-42): same field names, same
+ * defaults (vmp_config_default).  The trailing members size the device
+ * buffers and expose the two private kf::IESKF constants (ieskf.h:101-102). */
+typedef struct vmp_config {
+    int opti_max_iter;            /* 5: read by the node, never applied by the reference */
+    double na, ng, nba, nbg;      /* 0.01, 0.01, 1e-4, 1e-4 */
+    int imu_init_num;             /* 20 */
+    double r_il[9];               /* identity */
+    double p_il[3];               /* zero */
+    int gravity_align;            /* 1 */
+    int estimate_ext;             /* 0 */
+    double scan_resolution;       /* 0.1 */
+    double voxel_size;            /* 0.5 */
+    int update_size_thresh;       /* 10 (must be >= 2) */
+    int max_point_thresh;         /* 100 */
+    double plane_thresh;          /* 0.01 */
+    double ranging_cov;           /* 0.04 */
+    double angle_cov;             /* 0.1 (degrees) */
+    double merge_thresh_for_angle;    /* 0.1 */
+    double merge_thresh_for_distance; /* 0.04 */
+    int map_capacity;             /* 100000 */
+    /* kf::IESKF private members */
+    int ieskf_max_iter;           /* 5 (ieskf.h:101) */
+    double ieskf_eps;             /* 0.001 (ieskf.h:102) */
+    /* device sizing; no reference counterpart */
+    int max_scan_points;          /* raw points accepted per scan (default 262144) */
+    int max_imu_per_scan;         /* IMU samples accepted per scan (default 4096) */
+    int reserved[6];
+} vmp_config;
+
+/* One LiDAR point: xyz in the LiDAR frame and the time offset in ms. */
+typedef struct vmp_point {
+    float x, y, z, t_ms;
+} vmp_point;
+
+/* lio::IMUData (commons.h:12-20) */
+typedef struct vmp_imu {
+    double t;
+    double acc[3];
+    double gyro[3];
+} vmp_imu;
+
+/* lio::SyncPackage (commons.h:22-28): cloud + its start/end time. */
+typedef struct vmp_scan {
+    const vmp_point* points;
+    int n;
+    double t_start;
+    double t_end;
+} vmp_scan;
+
+/* kf::State (ieskf.h:31-62); rotations row-major. */
+typedef struct vmp_state {
+    double pos[3];
+    double rot[9];
+    double rot_ext[9];
+    double pos_ext[3];
+    double vel[3];
+    double bg[3];
+    double ba[3];
+    double g[3];
+} vmp_state;
+
+typedef struct vmp_result {
+    int lio_status;       /* vmp_lio_status after the call */
+    int iters;            /* IEKF iterations run this scan */
+    int effect_num;       /* valid residuals in the last iteration */
+    int n_raw;            /* points in the scan */
+    int n_down;           /* points after the scan downsample */
+    int flags;            /* bit0: no effective point in an iteration */
+    long long map_size;   /* live voxels after the scan */
+    long long evicted;    /* voxels evicted by this scan */
+    vmp_state x;
+    double P[23 * 23];
+} vmp_result;
+
+/* Sizes of the voxel map (for vmp_map_export buffers). */
+typedef struct vmp_map_info {
+    long long size;          /* live voxels */
+    long long capacity;      /* LRU capacity */
+    long long group_counter; /* VoxelGrid::count */
+    long long slab_points;   /* buffered points over all voxels */
+} vmp_map_info;
+
+/* One voxel of lio::VoxelGrid + its lio::Plane (voxel_map.h:43-103). */
+typedef struct vmp_voxel {
+    int64_t key[3];
+    int32_t n;               /* plane->n */
+    int32_t newly_add_point;
+    int32_t is_init, is_plane, update_enable, merged;
+    uint64_t group_id;
+    uint64_t lru_stamp;      /* larger = more recently touched */
+    int32_t n_temp;          /* temp_points.size() */
+    int32_t pad;
+    double mean[3];
+    double ppt[9];
+    double norm[3];
+    double center[3];
+    double cov[36];
+} vmp_voxel;
+
+typedef struct vmp_stream_s* vmp_stream_t;
+
+void vmp_config_default(vmp_config* cfg);
+int vmp_abi_version(void);
+
+vmp_status vmp_create(const vmp_config* cfg, vmp_stream_t* out);
+vmp_status vmp_destroy(vmp_stream_t s);
+const char* vmp_last_error(vmp_stream_t s);
+
+/* Full per-scan step (LIOBuilder::process).  Host buffers in, result out. */
+vmp_status vmp_process(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* imus, int n_imu,
+                       vmp_result* out);
+
+/* Same step with the scan and IMU samples already in device memory
+ * (device pointers; the call does no host<->device copy of inputs; the
+ * result is still written to the host struct). */
+vmp_status vmp_process_device(vmp_stream_t s, const vmp_point* d_points, int n, double t_start,
+                              double t_end, const vmp_imu* d_imus, int n_imu, vmp_result* out);
+
+/* ---- component entry points (the voxel_plus VoxelMap / IESKF surface) ---- */
+
+/* VoxelMap::index: keys[i*3+0..2] = floor(pts[i]/voxel_size). */
+vmp_status vmp_map_index(vmp_stream_t s, const double* pts, int n, int64_t* keys);
+/* VoxelMap::build on an empty map: pts n x 3, cov n x 9. */
+vmp_status vmp_map_build(vmp_stream_t s, const double* pts, const double* cov, int n);
+/* VoxelMap::update: pts n x 3, cov n x 9, applied in order. */
+vmp_status vmp_map_update(vmp_stream_t s, const double* pts, const double* cov, int n);
+vmp_status vmp_map_info_get(vmp_stream_t s, vmp_map_info* info);
+/* Copies up to max voxels, most recently used first (LRU order). */
+vmp_status vmp_map_export(vmp_stream_t s, vmp_voxel* out, long long max, long long* n_out);
+/* Replaces the map by the given voxels (LRU order as listed, first = most
+ * recent) and their buffered points (pts/cov of all voxels concatenated in
+ * voxel order, vox[i].n_temp each). */
+vmp_status vmp_map_import(vmp_stream_t s, const vmp_voxel* vox, long long n, const double* pts,
+                          const double* cov, long long group_counter);
+/* Buffered points of the exported voxels, in export order (n_temp each). */
+vmp_status vmp_map_export_points(vmp_stream_t s, double* pts, double* cov, long long max_points,
+                                 long long* n_out);
+
+/* LIOBuilder::sharedUpdateFunc with an explicit state: pts_l n x 3 (LiDAR
+ * frame, after the calcBodyCov z-fix), cov_l n x 9, P 23x23.  Writes the
+ * 12x12 H and 12 b of kf::SharedState and the valid-point count.  The
+ * per-point residual records persist across calls like residual_info. */
+vmp_status vmp_residual_reduce(vmp_stream_t s, const vmp_state* x, const double* P,
+                               const double* pts_l, const double* cov_l, int n, double* H,
+                               double* b, int* effect_num);
+
+/* IESKF on the stream's device state. */
+vmp_status vmp_get_state(vmp_stream_t s, vmp_state* x, double* P);
+vmp_status vmp_set_state(vmp_stream_t s, const vmp_state* x, const double* P);
+vmp_status vmp_ieskf_predict(vmp_stream_t s, const double acc[3], const double gyro[3], double dt,
+                             const double* Q /* 12x12 */);
+/* Iterated update with the measurement model of sharedUpdateFunc over the
+ * given LiDAR points (after downsample): iters/effect_num reported. */
+vmp_status vmp_ieskf_update(vmp_stream_t s, const float* pts_l /* n x 3 */, int n, int* iters,
+                            int* effect_num);
+
+/* LIOBuilder::undistortCloud on the stream's filter state: points are sorted
+ * by time and compensated in place into out (n points). */
+vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* imus, int n_imu,
+                         vmp_point* out);
+/* pcl::VoxelGrid leaf-centroid downsample at the given leaf size. */
+vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double leaf,
+                          vmp_point* out, int* n_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VMP_H_ */

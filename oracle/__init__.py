@@ -1,0 +1,93 @@
+"""ORACLE / TEST INFRASTRUCTURE ONLY.
+
+ctypes loader for the CPU restatement of the reference hot path
+(oracle/oracle.cpp, built by oracle/Makefile into oracle/_build/liboracle.so).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package; the product library never does.
+
+Parity unpinned: the reference has no tests or golden vectors for this path
+and cannot be built here (no Eigen3 / Sophus / PCL / ROS).
+"""
+import ctypes as C
+import os
+import subprocess
+
+from voxelmapplus_fastlio2_gb300 import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(_HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(ORACLE_SO):
+        build()
+    lib = C.CDLL(ORACLE_SO)
+    vp = C.c_void_p
+    P = C.POINTER
+    d = C.c_double
+    lib.orc_create.argtypes = [P(abi.vmp_config)]
+    lib.orc_create.restype = vp
+    lib.orc_destroy.argtypes = [vp]
+    lib.orc_set_threads.argtypes = [vp, C.c_int]
+    lib.orc_process.argtypes = [vp, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, P(abi.vmp_result)]
+    lib.orc_get_state.argtypes = [vp, P(abi.vmp_state), P(d)]
+    lib.orc_set_state.argtypes = [vp, P(abi.vmp_state), P(d)]
+    lib.orc_get_aux.argtypes = [vp, P(d)]
+    lib.orc_set_aux.argtypes = [vp, P(d)]
+    lib.orc_map_info.argtypes = [vp, P(abi.vmp_map_info)]
+    lib.orc_map_export.argtypes = [vp, P(abi.vmp_voxel), C.c_longlong]
+    lib.orc_map_export.restype = C.c_longlong
+    lib.orc_map_export_points.argtypes = [vp, P(d), P(d), C.c_longlong]
+    lib.orc_map_export_points.restype = C.c_longlong
+    lib.orc_map_import.argtypes = [vp, P(abi.vmp_voxel), C.c_longlong, P(d), P(d), C.c_longlong]
+    lib.orc_map_build.argtypes = [vp, P(d), P(d), C.c_int]
+    lib.orc_map_update.argtypes = [vp, P(d), P(d), C.c_int]
+    lib.orc_map_index.argtypes = [vp, P(d), C.c_int, P(C.c_int64)]
+    lib.orc_residual_reduce.argtypes = [vp, P(abi.vmp_state), P(d), P(d), P(d), C.c_int, P(d), P(d),
+                                        P(C.c_int), P(C.c_ubyte)]
+    lib.orc_ieskf_predict.argtypes = [vp, P(d), P(d), d, P(d)]
+    lib.orc_ieskf_update.argtypes = [vp, P(C.c_float), C.c_int, P(C.c_int), P(C.c_int)]
+    lib.orc_undistort.argtypes = [vp, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, P(abi.vmp_point)]
+    lib.orc_downsample.argtypes = [P(abi.vmp_point), C.c_int, d, P(abi.vmp_point)]
+    lib.orc_downsample.restype = C.c_int
+    lib.orc_calc_body_cov.argtypes = [P(d), C.c_int, d, d, P(d), P(d)]
+    lib.orc_last_cloud.argtypes = [vp, C.c_int, P(abi.vmp_point), C.c_int]
+    lib.orc_last_cloud.restype = C.c_int
+    lib.orc_so3_exp.argtypes = [P(d), P(d)]
+    lib.orc_so3_log.argtypes = [P(d), P(d)]
+    lib.orc_eig_sym3.argtypes = [P(d), P(d), P(d)]
+    _lib = lib
+    return lib
+
+
+class Oracle:
+    """lio::LIOBuilder restated on the CPU (one sensor stream)."""
+
+    def __init__(self, cfg=None, threads=1):
+        self.lib = load()
+        self.cfg = cfg if cfg is not None else abi.default_config()
+        self.h = self.lib.orc_create(C.byref(self.cfg))
+        self.lib.orc_set_threads(self.h, threads)
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.orc_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def process(self, pkg):
+        res = abi.vmp_result()
+        scan = pkg.scan()
+        self.lib.orc_process(self.h, C.byref(scan), pkg.imus, pkg.n_imu, C.byref(res))
+        return res
