@@ -1,0 +1,93 @@
+"""Shared helpers of the parity tests: seeded inputs and oracle/GPU pairs."""
+import ctypes as C
+
+import numpy as np
+
+from voxelmapplus_fastlio2_gb300 import abi
+
+
+def rot_angle(Ra, Rb):
+    R = np.asarray(Ra).reshape(3, 3).T @ np.asarray(Rb).reshape(3, 3)
+    c = np.clip((np.trace(R) - 1.0) / 2.0, -1.0, 1.0)
+    return float(np.arccos(c))
+
+
+def plane_points(rng, n_planes=40, pts_per=(5, 160), extent=20.0, noise=0.01, iso_frac=0.1):
+    """Points on random planes (with normal noise) plus isotropic clusters, and
+    per-point covariances like the map receives them (3x3, row-major)."""
+    P, Cv = [], []
+    for k in range(n_planes):
+        c = rng.uniform(-extent, extent, 3)
+        m = int(rng.integers(pts_per[0], pts_per[1]))
+        if rng.random() < iso_frac:
+            p = c + rng.normal(0, 0.15, (m, 3))
+        else:
+            nrm = rng.normal(size=3)
+            nrm /= np.linalg.norm(nrm)
+            u = np.cross(nrm, [1.0, 0.0, 0.0])
+            if np.linalg.norm(u) < 1e-3:
+                u = np.cross(nrm, [0.0, 1.0, 0.0])
+            u /= np.linalg.norm(u)
+            v = np.cross(nrm, u)
+            a = rng.uniform(-0.6, 0.6, (m, 2))
+            p = c + a[:, :1] * u + a[:, 1:] * v + rng.normal(0, noise, (m, 1)) * nrm
+        # float world points, as the reference's float transform produces
+        p = p.astype(np.float32).astype(np.float64)
+        for q in p:
+            A = rng.normal(0, 0.02, (3, 3))
+            cov = A @ A.T + np.eye(3) * 1e-4
+            P.append(q)
+            Cv.append(cov.reshape(9))
+    P = np.array(P)
+    Cv = np.array(Cv)
+    perm = rng.permutation(len(P))
+    return P[perm], Cv[perm]
+
+
+def export_oracle_map(olib, h):
+    info = abi.vmp_map_info()
+    olib.orc_map_info(h, C.byref(info))
+    arr = (abi.vmp_voxel * max(1, info.size))()
+    n = olib.orc_map_export(h, arr, info.size)
+    pts = np.zeros((max(1, info.slab_points), 3))
+    cov = np.zeros((max(1, info.slab_points), 9))
+    m = olib.orc_map_export_points(h, pts.ctypes.data_as(C.POINTER(C.c_double)),
+                                   cov.ctypes.data_as(C.POINTER(C.c_double)), info.slab_points)
+    return arr, n, info, pts[:m], cov[:m]
+
+
+def voxels_by_key(arr, n):
+    return {tuple(arr[i].key): arr[i] for i in range(n)}
+
+
+def compare_maps(vo, no, vg, ng, exact=True, tol=1e-9):
+    """Compares two exported maps voxel by voxel; returns a list of problems."""
+    problems = []
+    A = voxels_by_key(vo, no)
+    B = voxels_by_key(vg, ng)
+    if set(A) != set(B):
+        problems.append(f"key sets differ: oracle-only {len(set(A) - set(B))}, gpu-only {len(set(B) - set(A))}")
+        return problems
+    for k, a in A.items():
+        b = B[k]
+        for f in ("n", "newly_add_point", "is_init", "is_plane", "update_enable", "merged", "group_id", "n_temp"):
+            if getattr(a, f) != getattr(b, f):
+                problems.append(f"{k}: {f} oracle={getattr(a, f)} gpu={getattr(b, f)}")
+        for f, size in (("mean", 3), ("ppt", 9), ("norm", 3), ("center", 3), ("cov", 36)):
+            x = np.array(getattr(a, f)[:size])
+            y = np.array(getattr(b, f)[:size])
+            if exact:
+                if not np.array_equal(x, y):
+                    problems.append(f"{k}: {f} differs by {np.max(np.abs(x - y)):.3e}")
+            else:
+                scale = max(1.0, float(np.max(np.abs(x))))
+                if np.max(np.abs(x - y)) > tol * scale:
+                    problems.append(f"{k}: {f} differs by {np.max(np.abs(x - y)):.3e}")
+        if len(problems) > 20:
+            break
+    # LRU order
+    ko = [tuple(vo[i].key) for i in range(no)]
+    kg = [tuple(vg[i].key) for i in range(ng)]
+    if ko != kg:
+        problems.append("LRU order differs")
+    return problems

@@ -1,0 +1,202 @@
+"""GPU parity against the CPU oracle (restated reference), through the C ABI.
+
+Tolerances: integer / index work (voxel keys, match sets, group ids, flags,
+point counts, downsampled float clouds) must be identical.  FP64 results:
+the map's per-voxel arithmetic runs in the reference's order on both sides
+and must be bit-identical; H / b of the residual reduction differ only by the
+summation order of a parallel reduction (relative 1e-9); the pose after a
+scan must agree within 1e-6 m and 1e-6 rad (the target the odometry hot path
+is specified to).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from voxelmapplus_fastlio2_gb300 import abi, synth
+from tests.helpers import compare_maps, export_oracle_map, plane_points, rot_angle
+
+pytestmark = pytest.mark.gpu
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+@pytest.fixture(scope="module")
+def lio_mod():
+    from voxelmapplus_fastlio2_gb300 import lio
+    return lio
+
+
+def test_downsample_matches_oracle(lio_mod, oracle_lib):
+    rng = np.random.default_rng(7)
+    g = lio_mod.LIOBuilder(abi.default_config(max_scan_points=70000))
+    for trial in range(3):
+        n = [1, 5000, 65000][trial]
+        pts = np.zeros((n, 4), dtype=np.float32)
+        pts[:, :3] = rng.uniform(-30, 30, (n, 3)).astype(np.float32)
+        pts[:, 3] = np.sort(rng.uniform(0, 100, n)).astype(np.float32)
+        for leaf in (0.1, 0.5):
+            out_g = g.downsample(pts, leaf)
+            out_o = (abi.vmp_point * n)()
+            m = oracle_lib.orc_downsample(pts.ctypes.data_as(C.POINTER(abi.vmp_point)), n, leaf, out_o)
+            o = np.ctypeslib.as_array(C.cast(out_o, C.POINTER(C.c_float)), shape=(n, 4))[:m]
+            assert out_g.shape[0] == m
+            assert np.array_equal(out_g.view(np.uint32), o.view(np.uint32))
+
+
+@pytest.mark.parametrize("merge_mode", [0, 1])
+def test_map_build_update_bit_exact(lio_mod, oracle_lib, merge_mode):
+    rng = np.random.default_rng(11 + merge_mode)
+    cfg = abi.default_config(map_capacity=200000, max_scan_points=60000)
+    g = lio_mod.LIOBuilder(cfg)
+    g.set_merge_mode(merge_mode)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        P, Cv = plane_points(rng, n_planes=120)
+        oracle_lib.orc_map_build(o, _dp(P), _dp(Cv), len(P))
+        g.map.build(P, Cv)
+        for step in range(6):
+            P2, C2 = plane_points(rng, n_planes=150, pts_per=(2, 90))
+            oracle_lib.orc_map_update(o, _dp(P2), _dp(C2), len(P2))
+            g.map.update(P2, C2)
+            vo, no, info, _, _ = export_oracle_map(oracle_lib, o)
+            vg, ng = g.map.export()
+            problems = compare_maps(vo, no, vg, ng, exact=True)
+            assert not problems, f"step {step}: " + "; ".join(problems[:8])
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
+def test_map_index_matches_oracle(lio_mod, oracle_lib):
+    rng = np.random.default_rng(3)
+    cfg = abi.default_config()
+    g = lio_mod.LIOBuilder(cfg)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        P = rng.uniform(-500, 500, (20000, 3))
+        P[:100] = np.round(P[:100] * 2) / 2  # exact voxel boundaries
+        kg = g.map.index(P)
+        ko = np.zeros_like(kg)
+        oracle_lib.orc_map_index(o, _dp(P), len(P), ko.ctypes.data_as(C.POINTER(C.c_int64)))
+        assert np.array_equal(kg, ko)
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
+def _seeded_state(rng):
+    x = abi.vmp_state()
+    ang = rng.normal(0, 0.3, 3)
+    th = np.linalg.norm(ang)
+    k = ang / th
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    R = np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+    for i in range(9):
+        x.rot[i] = R.reshape(9)[i]
+        x.rot_ext[i] = 1.0 if i in (0, 4, 8) else 0.0
+    for i in range(3):
+        x.pos[i] = rng.normal(0, 0.5)
+        x.vel[i] = rng.normal(0, 0.3)
+        x.bg[i] = rng.normal(0, 0.01)
+        x.ba[i] = rng.normal(0, 0.05)
+    x.g[0], x.g[1], x.g[2] = 0.0, 0.0, -9.81
+    A = rng.normal(0, 0.01, (23, 23))
+    P = A @ A.T + np.eye(23) * 1e-4
+    return x, P
+
+
+def test_residual_reduce_matches_oracle(lio_mod, oracle_lib):
+    rng = np.random.default_rng(5)
+    cfg = abi.default_config(map_capacity=200000, max_scan_points=60000)
+    g = lio_mod.LIOBuilder(cfg)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        P, Cv = plane_points(rng, n_planes=200, noise=0.005, iso_frac=0.0)
+        oracle_lib.orc_map_build(o, _dp(P), _dp(Cv), len(P))
+        g.map.build(P, Cv)
+        x, Pc = _seeded_state(rng)
+        # LiDAR points near the map: world points pulled back through the pose
+        R = np.array(x.rot[:]).reshape(3, 3)
+        t = np.array(x.pos[:])
+        for rep in range(3):
+            sel = rng.choice(len(P), 20000)
+            pw = P[sel] + rng.normal(0, 0.02, (20000, 3))
+            pl = (pw - t) @ R
+            pl = pl.astype(np.float32).astype(np.float64)
+            cov_l = np.zeros((20000, 9))
+            pl_fix = np.zeros_like(pl)
+            oracle_lib.orc_calc_body_cov(_dp(pl), 20000, 0.04, 0.1, _dp(pl_fix), _dp(cov_l))
+            Hg, bg, eg = g.residual_reduce(x, Pc, pl_fix, cov_l)
+            Ho = np.zeros(144)
+            bo = np.zeros(12)
+            eo = C.c_int()
+            vo = np.zeros(20000, dtype=np.uint8)
+            oracle_lib.orc_residual_reduce(o, C.byref(x), _dp(Pc), _dp(pl_fix), _dp(cov_l), 20000, _dp(Ho), _dp(bo),
+                                           C.byref(eo), vo.ctypes.data_as(C.POINTER(C.c_ubyte)))
+            vg = g.residual_valid(20000)
+            assert eg == eo.value
+            assert np.array_equal(vg, vo), f"match sets differ at {np.flatnonzero(vg != vo)[:10]}"
+            scale = np.max(np.abs(Ho))
+            assert np.max(np.abs(Hg.reshape(144) - Ho)) <= 1e-9 * scale
+            assert np.max(np.abs(bg - bo)) <= 1e-9 * max(1.0, np.max(np.abs(bo)))
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
+def test_ieskf_predict_bit_exact(lio_mod, oracle_lib):
+    rng = np.random.default_rng(9)
+    cfg = abi.default_config()
+    g = lio_mod.LIOBuilder(cfg)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        x, P = _seeded_state(rng)
+        P = np.ascontiguousarray(P)
+        g.kf.set(x, P)
+        oracle_lib.orc_set_state(o, C.byref(x), _dp(P))
+        Q = np.diag([0.01] * 6 + [1e-4] * 6)
+        for k in range(20):
+            acc = rng.normal(0, 0.3, 3) + np.array([0, 0, 9.81])
+            gyro = rng.normal(0, 0.2, 3)
+            dt = 0.005
+            g.kf.predict(acc, gyro, dt, Q)
+            oracle_lib.orc_ieskf_predict(o, _dp(acc), _dp(gyro), dt, _dp(np.ascontiguousarray(Q.reshape(144))))
+        xg, Pg = g.kf.get()
+        xo = abi.vmp_state()
+        Po = np.zeros(529)
+        oracle_lib.orc_get_state(o, C.byref(xo), _dp(Po))
+        dx = max(abs(a - b) for a, b in zip(bytes(xg), bytes(xo))) if False else None
+        for f in ("pos", "rot", "vel", "bg", "ba", "g"):
+            a = np.array(getattr(xg, f)[:])
+            b = np.array(getattr(xo, f)[:])
+            assert np.allclose(a, b, rtol=0, atol=1e-13), f
+        assert np.max(np.abs(Pg.reshape(529) - Po)) <= 1e-13 * np.max(np.abs(Po))
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
+def test_process_sequence_room(lio_mod, oracle_lib):
+    """LIOBuilder::process over a seeded room sequence: per-scan pose within
+    1e-6 m / 1e-6 rad, identical downsample sizes, valid-residual counts and
+    map sizes."""
+    import oracle as orc
+    seq_g = synth.Sequence(synth.KIND_ROOM, points_per_scan=8000)
+    seq_o = synth.Sequence(synth.KIND_ROOM, points_per_scan=8000)
+    cfg = abi.default_config(scan_resolution=0.2, max_scan_points=16384)
+    g = lio_mod.LIOBuilder(cfg)
+    o = orc.Oracle(cfg)
+    for k in range(25):
+        pg = seq_g.next()
+        po = seq_o.next()
+        rg = g.process(pg)
+        ro = o.process(po)
+        assert rg.lio_status == ro.lio_status
+        if ro.lio_status != abi.LIO_MAPPING or k < 2:
+            continue
+        assert rg.n_down == ro.n_down, k
+        assert rg.effect_num == ro.effect_num, k
+        assert rg.iters == ro.iters, k
+        assert rg.map_size == ro.map_size, k
+        dp = np.max(np.abs(np.array(rg.x.pos[:]) - np.array(ro.x.pos[:])))
+        da = rot_angle(rg.x.rot[:], ro.x.rot[:])
+        assert dp < 1e-6 and da < 1e-6, (k, dp, da)

@@ -1,0 +1,77 @@
+"""Loader of the in-tree CUDA library (_build/libvmp.so).
+
+There is no CPU fallback: if the library is missing or no GPU is visible the
+calls fail with an exception.
+"""
+import ctypes as C
+import os
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libvmp.so")
+
+_lib = None
+
+
+class VmpError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _declare(lib):
+    P = C.POINTER
+    vp = C.c_void_p
+    d = C.c_double
+    st = C.c_int
+    sig = {
+        "vmp_abi_version": ([], C.c_int),
+        "vmp_config_default": ([P(abi.vmp_config)], None),
+        "vmp_create": ([P(abi.vmp_config), P(vp)], st),
+        "vmp_destroy": ([vp], st),
+        "vmp_last_error": ([vp], C.c_char_p),
+        "vmp_process": ([vp, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, P(abi.vmp_result)], st),
+        "vmp_process_device": ([vp, vp, C.c_int, d, d, vp, C.c_int, P(abi.vmp_result)], st),
+        "vmp_map_index": ([vp, P(d), C.c_int, P(C.c_int64)], st),
+        "vmp_map_build": ([vp, P(d), P(d), C.c_int], st),
+        "vmp_map_update": ([vp, P(d), P(d), C.c_int], st),
+        "vmp_map_info_get": ([vp, P(abi.vmp_map_info)], st),
+        "vmp_map_export": ([vp, P(abi.vmp_voxel), C.c_longlong, P(C.c_longlong)], st),
+        "vmp_map_import": ([vp, P(abi.vmp_voxel), C.c_longlong, P(d), P(d), C.c_longlong], st),
+        "vmp_map_export_points": ([vp, P(d), P(d), C.c_longlong, P(C.c_longlong)], st),
+        "vmp_residual_reduce": ([vp, P(abi.vmp_state), P(d), P(d), P(d), C.c_int, P(d), P(d), P(C.c_int)], st),
+        "vmp_get_state": ([vp, P(abi.vmp_state), P(d)], st),
+        "vmp_set_state": ([vp, P(abi.vmp_state), P(d)], st),
+        "vmp_ieskf_predict": ([vp, P(d), P(d), d, P(d)], st),
+        "vmp_ieskf_update": ([vp, P(C.c_float), C.c_int, P(C.c_int), P(C.c_int)], st),
+        "vmp_undistort": ([vp, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, P(abi.vmp_point)], st),
+        "vmp_downsample": ([vp, P(abi.vmp_point), C.c_int, d, P(abi.vmp_point), P(C.c_int)], st),
+        "vmp_residual_valid": ([vp, P(C.c_ubyte), C.c_int], st),
+        "vmp_last_cloud": ([vp, C.c_int, P(abi.vmp_point), C.c_int, P(C.c_int)], st),
+        "vmp_set_merge_mode": ([vp, C.c_int], st),
+        "vmp_last_merge_rounds": ([vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+def load():
+    """Returns the ctypes handle of libvmp.so (raises if it is not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+        _lib = _declare(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def check(handle, code):
+    if code != abi.VMP_OK:
+        lib = load()
+        msg = lib.vmp_last_error(handle) if handle else b""
+        raise VmpError(code, (msg or b"").decode(errors="replace"))

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
 CU_SOURCES = [
     "vmp_api.cu",
     "k_sort.cu",
-    "k_scan.cu",
+    "k_points.cu",
     "k_filter.cu",
     "k_map.cu",
     "k_merge.cu",

@@ -1,0 +1,826 @@
+// Device-resident voxel plane map: VoxelMap::build / update with LRU
+// (voxel_map.cpp:200-256), VoxelGrid::pushPoint / addPoint / updatePlane
+// (voxel_map.cpp:29-136).
+//
+// One batch of N world points (in order) is applied as:
+//   1. key + hash lookup / CAS insert per point; a new key's slot records the
+//      smallest point index that reached it (atomicMin) = its creating point;
+//   2. creating points are ranked by a prefix sum: rank = creation order, so
+//      VoxelGrid::count (group_id) is assigned exactly as the sequential
+//      loop would;
+//   3. points are stably sorted by record -> one segment per touched voxel,
+//      each in point order;
+//   4. a warp per segment runs the pushPoint state machine in point order
+//      (lane 0 carries the incremental mean / ppt; refits use all lanes: the
+//      per-point J * cov * J^T terms are computed 32 at a time and each of the
+//      36 plane-cov entries is summed by one lane in point order, so the sum
+//      is the reference's sequential sum);
+//   5. points that reach a frozen plane voxel become merge events, resolved in
+//      point order in k_merge.cu (merges only read and write frozen voxels,
+//      which no other step changes);
+//   6. LRU: each touched voxel's stamp = global index of its last touching
+//      point; evictions take the least recent untouched voxels in creation
+//      order.
+#include "kernels.cuh"
+
+namespace vmp {
+
+constexpr int kMapThreads = 256;
+constexpr int kSegThreads = 128;  // 4 warps: 4 x 32 x 36 doubles of refit staging
+
+static int grid_for_map(int n) {
+    int b = (n + kMapThreads - 1) / kMapThreads;
+    if (b > 152 * 8) b = 152 * 8;
+    return b < 1 ? 1 : b;
+}
+
+// ---------------------------------------------------------------- lookup / insert
+__global__ void k_lookup_insert(DMap m, const double* __restrict__ bpts, const int* d_n, uint32_t* slot_out,
+                                unsigned long long* keys_out) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double p[3] = {bpts[i * 3], bpts[i * 3 + 1], bpts[i * 3 + 2]};
+        int64_t k[3];
+        if (!voxel_index(p, m.voxel_size, k)) {
+            set_error(m.cnt, E_KEY_RANGE);
+            slot_out[i] = kNoRec;
+            continue;
+        }
+        uint64_t key = pack_key(k[0], k[1], k[2]);
+        if (keys_out) keys_out[i] = key;
+        uint64_t h = hash_key(key) & m.table_mask;
+        bool placed = false;
+        for (uint64_t probe = 0; probe <= m.table_mask; ++probe) {
+            uint64_t cur = *((volatile unsigned long long*)&m.keys[h]);
+            if (cur == key) { placed = true; break; }
+            if (cur == kEmptyKey) {
+                unsigned long long prev = atomicCAS((unsigned long long*)&m.keys[h], (unsigned long long)kEmptyKey,
+                                                    (unsigned long long)key);
+                if (prev == kEmptyKey || prev == key) { placed = true; break; }
+            }
+            h = (h + 1) & m.table_mask;
+        }
+        if (!placed) {
+            set_error(m.cnt, E_HASH_FULL);
+            slot_out[i] = kNoRec;
+            continue;
+        }
+        uint32_t v = *((volatile uint32_t*)&m.vals[h]);
+        if (v >= kPending) atomicMin(&m.vals[h], kPending | (uint32_t)i);
+        slot_out[i] = (uint32_t)h;
+    }
+}
+
+__global__ void k_creator_flags(DMap m, const uint32_t* __restrict__ slot, const int* d_n, uint32_t* flag) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s = slot[i];
+        flag[i] = (s != kNoRec && m.vals[s] == (kPending | (uint32_t)i)) ? 1u : 0u;
+    }
+}
+
+__global__ void k_assign(DMap m, const uint32_t* __restrict__ slot, const uint32_t* __restrict__ flag,
+                         const uint32_t* __restrict__ rank, const int* d_n, uint32_t* new_pos) {
+    const int n = *d_n;
+    const int top = m.cnt->rec_free_top;
+    const long long gbase = m.cnt->group_counter;
+    const unsigned long long base = m.cnt->batch_base;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        uint32_t r = rank[i];
+        uint32_t s = slot[i];
+        if ((int)r >= top) {
+            set_error(m.cnt, E_RECORDS);
+            m.vals[s] = kNoRec;
+            continue;
+        }
+        uint32_t rec = m.rec_free[top - 1 - (int)r];
+        RecHot& h = m.hot[rec];
+        for (int a = 0; a < 3; ++a) { h.mean[a] = 0.0; h.norm[a] = 0.0; }
+        h.flags = F_UPDATE | F_ALIVE;
+        h.n = 0;
+        h.group = (uint64_t)(gbase + (long long)r);
+        RecCold& c = m.cold[rec];
+        for (int a = 0; a < 9; ++a) c.ppt[a] = 0.0;
+        for (int a = 0; a < 36; ++a) c.cov[a] = 0.0;
+        for (int a = 0; a < 3; ++a) c.center[a] = 0.0;
+        c.key = m.keys[s];
+        c.stamp = base + (unsigned long long)i;
+        c.create_g = base + (unsigned long long)i;
+        c.freeze_g = kNever;
+        c.evict_g = kNever;
+        c.touch_first_g = kNever;
+        c.newly = 0;
+        c.nslab = 0;
+        for (int a = 0; a < kMaxChunks; ++a) c.chunks[a] = -1;
+        new_pos[r] = (uint32_t)i;
+        __threadfence();
+        m.vals[s] = rec;
+    }
+}
+
+__global__ void k_assign_counters(DMap m, const int* d_n_new) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int nn = *d_n_new;
+        Counters* c = m.cnt;
+        int take = nn <= c->rec_free_top ? nn : c->rec_free_top;
+        c->rec_free_top -= take;
+        c->group_counter += nn;
+        c->size += take;
+        c->n_new = nn;
+        c->n_evict = 0;
+        c->split_at = -1;
+    }
+}
+
+__global__ void k_resolve(DMap m, const uint32_t* __restrict__ slot, const int* d_n, uint32_t* rec,
+                          uint32_t* sk, uint32_t* sv) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s = slot[i];
+        uint32_t r = (s == kNoRec) ? kNoRec : m.vals[s];
+        if (r >= kPending) r = kNoRec;
+        rec[i] = r;
+        sk[i] = r;
+        sv[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_seg_heads(const uint32_t* __restrict__ sk, const int* d_n, uint32_t* flag) {
+    const int n = *d_n;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        flag[j] = (sk[j] != kNoRec && (j == 0 || sk[j] != sk[j - 1])) ? 1u : 0u;
+}
+
+// Segment bounds + LRU bookkeeping of the touched records.
+__global__ void k_seg_bounds(DMap m, const uint32_t* __restrict__ sk, const uint32_t* __restrict__ sv,
+                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ rank, const int* d_n,
+                             uint32_t* seg_start, uint32_t* seg_end, uint32_t* seg_rec, uint32_t* last_touch) {
+    const int n = *d_n;
+    const unsigned long long base = m.cnt->batch_base;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        uint32_t r = sk[j];
+        if (r == kNoRec) continue;
+        uint32_t s = rank[j];  // segment index (exclusive scan of heads; valid for non-head too: rank of next head)
+        if (flag[j]) {
+            seg_start[s] = (uint32_t)j;
+            seg_rec[s] = r;
+            m.cold[r].touch_first_g = base + sv[j];
+        }
+        bool tail = (j == n - 1) || sk[j + 1] != r;
+        if (tail) {
+            uint32_t seg = flag[j] ? s : s - 1;
+            seg_end[seg] = (uint32_t)(j + 1);
+            last_touch[sv[j]] = 1u;
+        }
+    }
+}
+
+__global__ void k_fill_u32(uint32_t* p, const int* d_n, uint32_t v) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
+
+// ---------------------------------------------------------------- eviction
+// Sequential walk over the creations of this batch that overflow the
+// capacity (exact LRU semantics): the victim of a creation at point c is the
+// least recently used voxel that no point before c touched in this batch.
+// A victim that a later point of the batch touches would be re-created by the
+// reference; the walk then reports the first such point (split_at) and the
+// host applies the batch in two parts.
+__global__ void k_evict_walk(DMap m, const uint32_t* __restrict__ new_pos, uint32_t* victims) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Counters* c = m.cnt;
+    const int n_new = c->n_new;
+    const long long size_before = c->size - n_new;
+    const unsigned long long base = c->batch_base;
+    c->n_evict = 0;
+    c->split_at = -1;
+    long long j0 = m.capacity - size_before;  // creations j >= j0 evict
+    if (j0 < 0) j0 = 0;
+    if (j0 >= n_new) return;
+    unsigned long long q = c->q_head;
+    int ne = 0;
+    long long split = -1;
+    for (long long j = j0; j < n_new; ++j) {
+        const unsigned long long cg = base + new_pos[j];
+        uint32_t victim = kNoRec;
+        while (q < c->q_tail) {
+            uint32_t r = m.q_rec[q % m.q_cap];
+            uint64_t st = m.q_stamp[q % m.q_cap];
+            ++q;
+            if (!(m.hot[r].flags & F_ALIVE) || m.cold[r].stamp != st) continue;
+            uint64_t tf = m.cold[r].touch_first_g;
+            bool touched_here = (tf != kNever) && tf >= base;
+            if (touched_here && tf < cg) continue;  // moved to the front before this creation
+            victim = r;
+            if (touched_here) split = (long long)(tf - base);  // re-created later by the reference
+            break;
+        }
+        if (split >= 0) break;
+        if (victim == kNoRec) { set_error(c, E_CAPACITY); break; }
+        victims[ne++] = victim;
+    }
+    if (split >= 0) {
+        c->split_at = (int)split;
+        return;
+    }
+    for (int v = 0; v < ne; ++v) m.cold[victims[v]].evict_g = base + new_pos[j0 + v];
+    c->q_head = q;
+    c->n_evict = ne;
+}
+
+// Undoes the creations of an aborted batch (the batch is split and re-applied).
+__global__ void k_rollback(DMap m, const uint32_t* __restrict__ slot, const uint32_t* __restrict__ flag,
+                           const int* d_n) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        uint32_t s = slot[i];
+        uint32_t r = m.vals[s];
+        m.keys[s] = kTombKey;
+        m.vals[s] = 0xFFFFFFFFu;
+        if (r < kPending) m.hot[r].flags = 0;
+    }
+}
+__global__ void k_rollback_counters(DMap m) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Counters* c = m.cnt;
+    c->rec_free_top += c->n_new;
+    c->group_counter -= c->n_new;
+    c->size -= c->n_new;
+    c->n_tomb += c->n_new;
+    c->n_new = 0;
+}
+
+// ---------------------------------------------------------------- segments
+struct SegShared {
+    double stage[kSegThreads / 32][32][36];
+};
+
+__device__ inline double* slab_pt(const DMap& m, const int* chunks, int j) {
+    return m.slab + ((size_t)chunks[j / kChunkPts] * kChunkPts + (j % kChunkPts)) * kSlabStride;
+}
+
+// Symmetric 3x3 eigen decomposition (cyclic Jacobi), the same operation
+// sequence as the oracle's restatement of Eigen's SelfAdjointEigenSolver.
+__device__ void eig_sym3(const double* A, double* evals, double* evecs) {
+    double a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) a[i][j] = A[i * 3 + j];
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+        double scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+        if (off == 0.0 || off <= 1e-300 || off < 1e-18 * scale) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                double apq = a[p][q];
+                if (apq == 0.0) continue;
+                double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; ++k) {
+                    double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int idx[3] = {0, 1, 2};
+    double d[3] = {a[0][0], a[1][1], a[2][2]};
+    for (int i = 0; i < 3; ++i)
+        for (int j = i + 1; j < 3; ++j)
+            if (d[idx[j]] < d[idx[i]]) { int t = idx[i]; idx[i] = idx[j]; idx[j] = t; }
+    for (int c = 0; c < 3; ++c) {
+        evals[c] = d[idx[c]];
+        for (int r = 0; r < 3; ++r) evecs[r * 3 + c] = v[r][idx[c]];
+    }
+}
+
+// Per-point term J * cov * J^T of VoxelGrid::updatePlane (voxel_map.cpp:115-130).
+__device__ void plane_cov_term(const double* p, const double* cov, const double* mean, int n, const double* ev,
+                               const double* evecs, double* out36) {
+    double pn[3] = {evecs[0], evecs[3], evecs[6]};
+    double F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double d[3] = {p[0] - mean[0], p[1] - mean[1], p[2] - mean[2]};
+    for (int mm_ = 1; mm_ < 3; ++mm_) {
+        double vm[3] = {evecs[mm_], evecs[3 + mm_], evecs[6 + mm_]};
+        double den = (double)n * (ev[0] - ev[mm_]);
+        double dd[3] = {d[0] / den, d[1] / den, d[2] / den};
+        double M1[9], M2[9], M[9], Fm[3];
+        mm<3, 1, 3>(vm, pn, M1);
+        mm<3, 1, 3>(pn, vm, M2);
+        for (int k = 0; k < 9; ++k) M[k] = M1[k] + M2[k];
+        mm<1, 3, 3>(dd, M, Fm);
+        F[mm_ * 3] = Fm[0]; F[mm_ * 3 + 1] = Fm[1]; F[mm_ * 3 + 2] = Fm[2];
+    }
+    double J[18], top[9];
+    mm<3, 3, 3>(evecs, F, top);
+    const double inv_n = 1.0 / (double)n, zero_n = 0.0 / (double)n;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            J[i * 3 + j] = top[i * 3 + j];
+            J[(3 + i) * 3 + j] = (i == j) ? inv_n : zero_n;
+        }
+    double T1[18], JT[18];
+    mm<6, 3, 3>(J, cov, T1);
+    tr<6, 3>(J, JT);
+    mm<6, 3, 6>(T1, JT, out36);
+}
+
+// Warp-cooperative updatePlane.  State lives in lane 0's registers (passed by
+// reference; only lane 0's copies are authoritative); cov lives in `cov`
+// (shared memory of the warp).  Points: from the slab (chunks) or from the
+// batch segment (sv/bpts/bcov) when from_batch.
+__device__ void warp_update_plane(const DMap& m, uint32_t& flags, int n, const double* mean, const double* ppt,
+                                  double* norm, double* center, double* cov, const int* chunks, int npts,
+                                  bool from_batch, const uint32_t* sv, int seg_b, const double* bpts,
+                                  const double* bcov, double (*stage)[36]) {
+    const int lane = threadIdx.x & 31;
+    int go = 0;
+    double ev[3], evecs[9], mn[3];
+    if (lane == 0) {
+        if (n >= m.update_thresh) {
+            flags |= F_INIT;
+            double C[9];
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) C[k * 3 + l] = ppt[k * 3 + l] / (double)n - mean[k] * mean[l];
+            eig_sym3(C, ev, evecs);
+            if (ev[0] > m.plane_thresh) {
+                flags &= ~F_PLANE;
+            } else {
+                flags |= F_PLANE;
+                go = 1;
+            }
+        }
+        for (int k = 0; k < 3; ++k) mn[k] = mean[k];
+    }
+    go = __shfl_sync(0xffffffffu, go, 0);
+    if (!go) return;
+    for (int k = 0; k < 3; ++k) {
+        ev[k] = __shfl_sync(0xffffffffu, ev[k], 0);
+        mn[k] = __shfl_sync(0xffffffffu, mn[k], 0);
+    }
+    for (int k = 0; k < 9; ++k) evecs[k] = __shfl_sync(0xffffffffu, evecs[k], 0);
+    n = __shfl_sync(0xffffffffu, n, 0);
+    for (int base = 0; base < npts; base += 32) {
+        int j = base + lane;
+        if (j < npts) {
+            const double* src;
+            double pc[12];
+            if (from_batch) {
+                uint32_t i = sv[seg_b + j];
+                for (int k = 0; k < 3; ++k) pc[k] = bpts[i * 3 + k];
+                for (int k = 0; k < 9; ++k) pc[3 + k] = bcov[i * 9 + k];
+                src = pc;
+            } else {
+                src = slab_pt(m, chunks, j);
+            }
+            plane_cov_term(src, src + 3, mn, n, ev, evecs, stage[lane]);
+        }
+        __syncwarp();
+        const int cnt = min(32, npts - base);
+        for (int e = lane; e < 36; e += 32) {
+            double s = cov[e];
+            for (int q = 0; q < cnt; ++q) s = s + stage[q][e];
+            cov[e] = s;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        double pn[3] = {evecs[0], evecs[3], evecs[6]};
+        double axis_distance = -dot3(mean, pn);
+        if (axis_distance < 0.0) { pn[0] = -pn[0]; pn[1] = -pn[1]; pn[2] = -pn[2]; }
+        for (int k = 0; k < 3; ++k) { norm[k] = pn[k]; center[k] = mean[k]; }
+    }
+    __syncwarp();
+}
+
+__device__ inline void add_to_plane(double* mean, double* ppt, int& n, const double* p) {
+    for (int k = 0; k < 3; ++k) mean[k] = mean[k] + (p[k] - mean[k]) / ((double)n + 1.0);
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) ppt[k * 3 + l] = ppt[k * 3 + l] + p[k] * p[l];
+    n += 1;
+}
+
+__device__ inline bool slab_append(const DMap& m, int* chunks, int& nslab, const double* p, const double* c) {
+    int ci = nslab / kChunkPts;
+    if (ci >= kMaxChunks) return false;
+    if (nslab % kChunkPts == 0) {
+        int top = atomicSub(&m.cnt->chunk_free_top, 1);
+        if (top <= 0) {
+            atomicAdd(&m.cnt->chunk_free_top, 1);
+            set_error(m.cnt, E_CHUNKS);
+            return false;
+        }
+        chunks[ci] = m.chunk_free[top - 1];
+    }
+    double* d = slab_pt(m, chunks, nslab);
+    for (int k = 0; k < 3; ++k) d[k] = p[k];
+    for (int k = 0; k < 9; ++k) d[3 + k] = c[k];
+    nslab++;
+    return true;
+}
+
+__device__ inline void slab_release(const DMap& m, int* chunks, int& nslab) {
+    int used = (nslab + kChunkPts - 1) / kChunkPts;
+    for (int k = 0; k < used && k < kMaxChunks; ++k) {
+        if (chunks[k] >= 0) {
+            int pos = atomicAdd(&m.cnt->chunk_freed_top, 1);
+            if (pos < m.chunk_pool) m.chunk_freed[pos] = chunks[k];
+        }
+        chunks[k] = -1;
+    }
+    nslab = 0;
+}
+
+__global__ void __launch_bounds__(kSegThreads) k_segments(DMap m, const uint32_t* __restrict__ seg_start,
+                                                          const uint32_t* __restrict__ seg_end,
+                                                          const uint32_t* __restrict__ seg_rec, const int* d_n_seg,
+                                                          const uint32_t* __restrict__ sv,
+                                                          const double* __restrict__ bpts,
+                                                          const double* __restrict__ bcov, uint32_t* ev_rec,
+                                                          int build) {
+    __shared__ SegShared sh;
+    __shared__ double s_cov[kSegThreads / 32][36];
+    __shared__ int s_chunks[kSegThreads / 32][kMaxChunks];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int nseg = *d_n_seg;
+    const unsigned long long base = m.cnt->batch_base;
+    double* cov = s_cov[wib];
+    int* chunks = s_chunks[wib];
+    for (int sidx = gw; sidx < nseg; sidx += nw) {
+        const uint32_t rec = seg_rec[sidx];
+        const int b = (int)seg_start[sidx], e = (int)seg_end[sidx];
+        RecHot& H = m.hot[rec];
+        RecCold& Cc = m.cold[rec];
+        // lane 0 state
+        uint32_t flags = 0;
+        int n = 0, newly = 0, nslab = 0;
+        double mean[3] = {0, 0, 0}, ppt[9], norm[3] = {0, 0, 0}, center[3] = {0, 0, 0};
+        for (int k = 0; k < 9; ++k) ppt[k] = 0.0;
+        if (lane == 0) {
+            flags = H.flags; n = H.n; newly = Cc.newly; nslab = Cc.nslab;
+            for (int k = 0; k < 3; ++k) { mean[k] = H.mean[k]; norm[k] = H.norm[k]; center[k] = Cc.center[k]; }
+            for (int k = 0; k < 9; ++k) ppt[k] = Cc.ppt[k];
+        }
+        for (int k = lane; k < 36; k += 32) cov[k] = Cc.cov[k];
+        if (lane < kMaxChunks) chunks[lane] = Cc.chunks[lane];
+        __syncwarp();
+        if (build) {
+            // VoxelMap::build: addPoint for every point, one updatePlane at the end.
+            const int cnt = e - b;
+            bool store = false;
+            if (lane == 0) {
+                store = (nslab + cnt) < m.max_thresh && !(flags & F_DROPPED);
+                for (int j = b; j < e; ++j) {
+                    uint32_t i = sv[j];
+                    const double* p = bpts + (size_t)i * 3;
+                    add_to_plane(mean, ppt, n, p);
+                    if (store) slab_append(m, chunks, nslab, p, bcov + (size_t)i * 9);
+                }
+                if (!store) flags |= F_DROPPED;
+            }
+            __syncwarp();
+            const int n_b = __shfl_sync(0xffffffffu, n, 0);
+            warp_update_plane(m, flags, n_b, mean, ppt, norm, center, cov, chunks, cnt, true, sv, b, bpts, bcov,
+                              sh.stage[wib]);
+            if (lane == 0 && (flags & F_DROPPED)) slab_release(m, chunks, nslab);
+        } else {
+            for (int j = b; j < e; ++j) {
+                const uint32_t i = sv[j];
+                const double* p = bpts + (size_t)i * 3;
+                const double* c = bcov + (size_t)i * 9;
+                int act = 0;  // bit0 refit, bit1 freeze, bit2 reset newly_add_point after the refit
+                if (lane == 0) {
+                    if (!(flags & F_INIT)) {
+                        add_to_plane(mean, ppt, n, p);
+                        if (!(flags & F_DROPPED)) slab_append(m, chunks, nslab, p, c);
+                        act = 1;
+                    } else if (flags & F_UPDATE) {
+                        add_to_plane(mean, ppt, n, p);
+                        if (!(flags & F_DROPPED)) slab_append(m, chunks, nslab, p, c);
+                        newly++;
+                        if (newly >= m.update_thresh) act |= 1 | 4;
+                        int size_after = (flags & F_DROPPED) ? n : nslab;
+                        if (size_after >= m.max_thresh) act |= 2;
+                    } else if (flags & F_PLANE) {
+                        ev_rec[i] = rec;  // merge() call at this point
+                    }
+                }
+                act = __shfl_sync(0xffffffffu, act, 0);
+                if (act & 1) {
+                    const int n_b = __shfl_sync(0xffffffffu, n, 0);
+                    const int np_b = __shfl_sync(0xffffffffu, nslab, 0);
+                    __syncwarp();
+                    warp_update_plane(m, flags, n_b, mean, ppt, norm, center, cov, chunks, np_b, false, sv, b, bpts,
+                                      bcov, sh.stage[wib]);
+                    if (lane == 0 && (act & 4)) newly = 0;
+                }
+                if ((act & 2) && lane == 0) {
+                    flags &= ~F_UPDATE;
+                    flags &= ~F_DROPPED;
+                    slab_release(m, chunks, nslab);
+                    Cc.freeze_g = base + i;
+                }
+                __syncwarp();
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            H.flags = flags; H.n = n;
+            for (int k = 0; k < 3; ++k) { H.mean[k] = mean[k]; H.norm[k] = norm[k]; Cc.center[k] = center[k]; }
+            for (int k = 0; k < 9; ++k) Cc.ppt[k] = ppt[k];
+            Cc.newly = newly;
+            Cc.nslab = nslab;
+            Cc.stamp = base + sv[e - 1];
+        }
+        for (int k = lane; k < 36; k += 32) Cc.cov[k] = cov[k];
+        if (lane < kMaxChunks) Cc.chunks[lane] = chunks[lane];
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- finalize
+__global__ void k_ev_flags(const uint32_t* __restrict__ ev_rec, const int* d_n, uint32_t* flag) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flag[i] = ev_rec[i] != kNoRec ? 1u : 0u;
+}
+__global__ void k_compact_idx(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ rank, const int* d_n,
+                              uint32_t* out) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (flag[i]) out[rank[i]] = (uint32_t)i;
+}
+
+// Appends the touched records to the LRU queue in last-touch order.
+__global__ void k_queue_append(DMap m, const uint32_t* __restrict__ last_touch, const uint32_t* __restrict__ rank,
+                               const uint32_t* __restrict__ rec, const int* d_n, const int* d_n_touch) {
+    const int n = *d_n;
+    const unsigned long long tail = m.cnt->q_tail;
+    const unsigned long long base = m.cnt->batch_base;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!last_touch[i]) continue;
+        unsigned long long q = tail + rank[i];
+        m.q_rec[q % m.q_cap] = rec[i];
+        m.q_stamp[q % m.q_cap] = base + (unsigned long long)i;
+    }
+    (void)d_n_touch;
+}
+
+// Evictions: remove the victims' keys (tombstones), return records and slab
+// chunks to their free stacks.
+__global__ void k_finalize(DMap m, const uint32_t* __restrict__ victims) {
+    Counters* c = m.cnt;
+    const int ne = c->n_evict;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < ne; v += gridDim.x * blockDim.x) {
+        uint32_t r = victims[v];
+        uint64_t key = m.cold[r].key;
+        uint64_t h = hash_key(key) & m.table_mask;
+        for (uint64_t probe = 0; probe <= m.table_mask; ++probe) {
+            uint64_t k = m.keys[h];
+            if (k == key && m.vals[h] == r) { m.keys[h] = kTombKey; m.vals[h] = 0xFFFFFFFFu; break; }
+            if (k == kEmptyKey) break;
+            h = (h + 1) & m.table_mask;
+        }
+        m.hot[r].flags = 0;
+        int nsl = m.cold[r].nslab;
+        slab_release(m, m.cold[r].chunks, nsl);
+        m.cold[r].nslab = 0;
+        m.rec_free[c->rec_free_top + v] = r;
+    }
+}
+__global__ void k_finalize_chunks(DMap m) {
+    Counters* c = m.cnt;
+    int nf = c->chunk_freed_top;
+    if (nf > m.chunk_pool) nf = m.chunk_pool;
+    const int top = c->chunk_free_top;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nf; k += gridDim.x * blockDim.x)
+        m.chunk_free[top + k] = m.chunk_freed[k];
+}
+__global__ void k_finalize_counters(DMap m, const int* d_n, const int* d_n_touch) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Counters* c = m.cnt;
+    const int ne = c->n_evict;
+    c->rec_free_top += ne;
+    c->size -= ne;
+    c->evicted_total += ne;
+    c->n_tomb += ne;
+    int nf = c->chunk_freed_top;
+    if (nf > m.chunk_pool) nf = m.chunk_pool;
+    c->chunk_free_top += nf;
+    c->chunk_freed_top = 0;
+    c->q_tail += (unsigned long long)(*d_n_touch);
+    c->batch_base += (unsigned long long)(*d_n);
+    c->n_evict = 0;
+}
+
+// ---------------------------------------------------------------- driver
+// Phase A: keys, hash insert, creation ranking, records, segments.
+void launch_map_phase_a(DMap& m, MapScratch& ms, const double* bpts, int n_max, cudaStream_t st) {
+    const int g = grid_for_map(n_max);
+    k_lookup_insert<<<g, kMapThreads, 0, st>>>(m, bpts, ms.d_n, ms.slot, nullptr);
+    k_creator_flags<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.flag);
+    exclusive_scan_u32(ms.flag, ms.rank, ms.d_n, ms.d_n_new, ms.scan, st);
+    k_assign<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.rank, ms.d_n, ms.new_pos);
+    k_assign_counters<<<1, 32, 0, st>>>(m, ms.d_n_new);
+}
+// Eviction walk (only when the batch can overflow the capacity).
+void launch_map_walk(DMap& m, MapScratch& ms, cudaStream_t st) {
+    k_evict_walk<<<1, 32, 0, st>>>(m, ms.new_pos, ms.victims);
+}
+void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
+    k_rollback<<<grid_for_map(n_max), kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.d_n);
+    k_rollback_counters<<<1, 32, 0, st>>>(m);
+}
+// Segments are formed before the walk (the walk needs each touched record's
+// first touch).
+void launch_map_segments(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
+    const int g = grid_for_map(n_max);
+    k_resolve<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.rec, ms.sk, ms.sv);
+    radix_sort_pairs(ms.sk, ms.sv, ms.d_n, 32, ms.sort, st);
+    k_seg_heads<<<g, kMapThreads, 0, st>>>(ms.sk, ms.d_n, ms.flag2);
+    exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_seg, ms.scan, st);
+    k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.last_touch, ms.d_n, 0u);
+    k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, kNoRec);
+    k_seg_bounds<<<g, kMapThreads, 0, st>>>(m, ms.sk, ms.sv, ms.flag2, ms.rank2, ms.d_n, ms.seg_start, ms.seg_end,
+                                            ms.seg_rec, ms.last_touch);
+}
+// Phase B: state machine, merges, LRU queue, evictions, counters.
+void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
+                        cudaStream_t st) {
+    const int g = grid_for_map(n_max);
+    int sg = (n_max + (kSegThreads / 32) - 1) / (kSegThreads / 32);
+    if (sg > 152 * 16) sg = 152 * 16;
+    if (sg < 1) sg = 1;
+    k_segments<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg, ms.sv, bpts, bcov,
+                                           ms.ev_rec, build ? 1 : 0);
+    if (!build) {
+        k_ev_flags<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, ms.flag2);
+        exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_ev, ms.scan, st);
+        k_compact_idx<<<g, kMapThreads, 0, st>>>(ms.flag2, ms.rank2, ms.d_n, ms.ev_list);
+        run_merge_events(m, ms, ms.merge, n_max, ms.merge_mode, &ms.merge_rounds, st);
+    }
+    exclusive_scan_u32(ms.last_touch, ms.rank2, ms.d_n, ms.d_n_touch, ms.scan, st);
+    k_queue_append<<<g, kMapThreads, 0, st>>>(m, ms.last_touch, ms.rank2, ms.rec, ms.d_n, ms.d_n_touch);
+    k_finalize<<<g, kMapThreads, 0, st>>>(m, ms.victims);
+    k_finalize_chunks<<<g, kMapThreads, 0, st>>>(m);
+    k_finalize_counters<<<1, 32, 0, st>>>(m, ms.d_n, ms.d_n_touch);
+}
+
+// Rebuilds the hash table from the live records (drops tombstones).
+__global__ void k_clear_table(DMap m) {
+    const size_t ts = (size_t)m.table_mask + 1;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ts; i += (size_t)gridDim.x * blockDim.x) {
+        m.keys[i] = kEmptyKey;
+        m.vals[i] = 0xFFFFFFFFu;
+    }
+}
+__global__ void k_reinsert(DMap m) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m.rec_pool; r += gridDim.x * blockDim.x) {
+        if (!(m.hot[r].flags & F_ALIVE)) continue;
+        uint64_t key = m.cold[r].key;
+        uint64_t h = hash_key(key) & m.table_mask;
+        for (uint64_t probe = 0; probe <= m.table_mask; ++probe) {
+            unsigned long long prev = atomicCAS((unsigned long long*)&m.keys[h], (unsigned long long)kEmptyKey,
+                                                (unsigned long long)key);
+            if (prev == kEmptyKey) { m.vals[h] = (uint32_t)r; break; }
+            h = (h + 1) & m.table_mask;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) m.cnt->n_tomb = 0;
+}
+void launch_rehash(DMap& m, cudaStream_t st) {
+    k_clear_table<<<1216, 256, 0, st>>>(m);
+    k_reinsert<<<1216, 256, 0, st>>>(m);
+}
+
+// LRU queue compaction: keeps the live entries, in order, from q_head.
+__global__ void k_q_live(DMap m, uint32_t* flag, const int* d_len) {
+    const int len = *d_len;
+    const unsigned long long h = m.cnt->q_head;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        unsigned long long q = (h + i) % m.q_cap;
+        uint32_t r = m.q_rec[q];
+        flag[i] = ((m.hot[r].flags & F_ALIVE) && m.cold[r].stamp == m.q_stamp[q]) ? 1u : 0u;
+    }
+}
+__global__ void k_q_gather(DMap m, const uint32_t* flag, const uint32_t* rank, const int* d_len, uint32_t* tr,
+                           uint64_t* ts) {
+    const int len = *d_len;
+    const unsigned long long h = m.cnt->q_head;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        unsigned long long q = (h + i) % m.q_cap;
+        tr[rank[i]] = m.q_rec[q];
+        ts[rank[i]] = m.q_stamp[q];
+    }
+}
+__global__ void k_q_scatter(DMap m, const uint32_t* tr, const uint64_t* ts, const int* d_live) {
+    const int live = *d_live;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < live; i += gridDim.x * blockDim.x) {
+        m.q_rec[i] = tr[i];
+        m.q_stamp[i] = ts[i];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        m.cnt->q_head = 0;
+        m.cnt->q_tail = (unsigned long long)live;
+    }
+}
+void launch_queue_compact(DMap& m, uint32_t* flag, uint32_t* rank, uint32_t* tr, uint64_t* ts, int* d_len,
+                          int* d_live, int len_max, ScanScratch& sc, cudaStream_t st) {
+    const int g = grid_for_map(len_max);
+    k_q_live<<<g, kMapThreads, 0, st>>>(m, flag, d_len);
+    exclusive_scan_u32(flag, rank, d_len, d_live, sc, st);
+    k_q_gather<<<g, kMapThreads, 0, st>>>(m, flag, rank, d_len, tr, ts);
+    k_q_scatter<<<g, kMapThreads, 0, st>>>(m, tr, ts, d_live);
+}
+
+__global__ void k_map_index(DMap m, const double* pts, int n, int64_t* keys) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double p[3] = {pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]};
+        // VoxelMap::index, unbounded int64 (no packing here)
+        for (int a = 0; a < 3; ++a) keys[i * 3 + a] = (int64_t)floor(__ddiv_rn(p[a], m.voxel_size));
+    }
+}
+void launch_map_index(const DMap& m, const double* pts, int n, int64_t* keys, cudaStream_t st) {
+    k_map_index<<<grid_for_map(n), kMapThreads, 0, st>>>(m, pts, n, keys);
+}
+
+__global__ void k_map_reset(DMap m) {
+    const size_t ts = (size_t)m.table_mask + 1;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ts; i += (size_t)gridDim.x * blockDim.x) {
+        m.keys[i] = kEmptyKey;
+        m.vals[i] = 0xFFFFFFFFu;
+    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)m.rec_pool;
+         i += (size_t)gridDim.x * blockDim.x) {
+        m.rec_free[i] = (uint32_t)(m.rec_pool - 1 - i);
+        m.hot[i].flags = 0;
+    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)m.chunk_pool;
+         i += (size_t)gridDim.x * blockDim.x)
+        m.chunk_free[i] = (int32_t)(m.chunk_pool - 1 - i);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Counters* c = m.cnt;
+        c->size = 0;
+        c->group_counter = 0;
+        c->batch_base = 1;
+        c->q_head = c->q_tail = 0;
+        c->rec_free_top = m.rec_pool;
+        c->chunk_free_top = m.chunk_pool;
+        c->chunk_freed_top = 0;
+        c->n_new = c->n_seg = c->n_events = c->n_evict = 0;
+        c->error = 0;
+        c->evicted_total = 0;
+        c->split_at = -1;
+        c->n_tomb = 0;
+    }
+}
+void launch_map_reset(DMap& m, cudaStream_t st) { k_map_reset<<<1216, 256, 0, st>>>(m); }
+
+cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
+    ms.max_batch = max_batch;
+    size_t nb = (size_t)max_batch + 16;
+    cudaError_t e;
+    uint32_t** u32s[] = {&ms.slot, &ms.rec, &ms.flag, &ms.rank, &ms.flag2, &ms.rank2, &ms.sk, &ms.sv, &ms.seg_start, &ms.seg_end,
+                         &ms.seg_rec, &ms.ev_rec, &ms.ev_list, &ms.last_touch, &ms.victims, &ms.new_pos};
+    for (auto pp : u32s)
+        if ((e = cudaMalloc(pp, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
+    if ((e = merge_scratch_alloc(&ms.merge, max_batch, rec_pool)) != cudaSuccess) return e;
+    ms.merge_mode = 0;
+    ms.merge_rounds = 0;
+    if ((e = cudaMalloc(&ms.d_scratch_int, sizeof(int) * 32)) != cudaSuccess) return e;
+    ms.d_n = ms.d_scratch_int;
+    ms.d_n_new = ms.d_scratch_int + 1;
+    ms.d_n_seg = ms.d_scratch_int + 2;
+    ms.d_n_ev = ms.d_scratch_int + 3;
+    ms.d_n_touch = ms.d_scratch_int + 4;
+    if ((e = sort_scratch_alloc(ms.sort, max_batch)) != cudaSuccess) return e;
+    if ((e = scan_scratch_alloc(ms.scan, max_batch)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+void map_scratch_free(MapScratch& ms) {
+    uint32_t* u32s[] = {ms.slot, ms.rec, ms.flag, ms.rank, ms.flag2, ms.rank2, ms.sk, ms.sv, ms.seg_start, ms.seg_end, ms.seg_rec,
+                        ms.ev_rec, ms.ev_list, ms.last_touch, ms.victims, ms.new_pos};
+    for (auto p : u32s) cudaFree(p);
+    merge_scratch_free(ms.merge);
+    cudaFree(ms.d_scratch_int);
+    sort_scratch_free(ms.sort);
+    scan_scratch_free(ms.scan);
+}
+
+}  // namespace vmp

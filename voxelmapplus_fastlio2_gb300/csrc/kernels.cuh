@@ -1,0 +1,124 @@
+// Kernel-side interfaces shared between the kernel translation units and the
+// host orchestration (vmp_api.cu).
+#pragma once
+#include "common.cuh"
+#include "prims.cuh"
+
+namespace vmp {
+
+// Per-scan device buffers of one stream.
+struct DScan {
+    // raw scan (input) and its time-sorted, undistorted copy
+    float4* raw;           // [max_pts] x, y, z, t_ms
+    float4* cloud;         // [max_pts] sorted by time, compensated in place
+    uint32_t* sort_k;      // [max_pts]
+    uint32_t* sort_v;      // [max_pts]
+    uint32_t* flags;       // [max_pts]
+    uint32_t* scan_out;    // [max_pts]
+    int* d_n_raw;          // device copy of the raw point count
+    // downsample
+    float4* down;          // [max_pts]
+    int* d_n_down;
+    float* minmax;         // [6] + per-block partials
+    float* blk_minmax;     // [blocks * 6]
+    int* ds_params;        // [16] leaf grid parameters / overflow flag
+    uint32_t* run_start;   // [max_pts + 1]
+    // per downsampled point
+    double* pl;            // [max_pts * 3] LiDAR-frame point (after the z == 0 fix)
+    double* covl;          // [max_pts * 9] calcBodyCov
+    // persistent residual records (residual_info): valid, normal, residual
+    uint8_t* rvalid;       // [max_pts]
+    double* rnorm;         // [max_pts * 3]
+    double* rres;          // [max_pts]
+    // map batch (world points + covariances handed to VoxelMap::build/update)
+    double* bpts;          // [max_pts * 3]
+    double* bcov;          // [max_pts * 9]
+    int* d_n_batch;
+    // IMU package
+    vmp_imu* imus;         // [max_imu]
+    DPose* poses;          // [max_imu + 2]
+    // reduction partials
+    double* partials;      // [res_blocks * 80]
+    unsigned int* done_ctr;
+    int max_pts;
+    int max_imu;
+    int res_blocks;
+};
+
+// ---- k_filter.cu
+void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& cfg, double t_end,
+                     cudaStream_t st);
+void launch_predict_chain(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st);
+void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st);
+void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st);
+void launch_update_begin(DFilter* f, cudaStream_t st);
+void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
+                          cudaStream_t st, int do_step = 1);
+void launch_update_end(DFilter* f, cudaStream_t st);
+
+// ---- k_points.cu
+void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st);
+void launch_downsample(DScan& s, int n_max, double leaf, SortScratch& ss, ScanScratch& sc, cudaStream_t st);
+void launch_copy_down(DScan& s, int n_max, cudaStream_t st);
+void launch_body_cov(DScan& s, int n_max, double range_inc, double sin_deg, cudaStream_t st);
+// world points + covariances for the map: from the downsampled cloud (after
+// update) or from the full undistorted cloud (map init)
+void launch_map_batch(DFilter* f, DScan& s, int n_max, bool from_full_cloud, double range_inc, double sin_deg,
+                      cudaStream_t st);
+
+// ---- k_map.cu
+struct MapScratch {
+    uint32_t* slot;       // [max_batch] hash slot per point
+    uint32_t* rec;        // [max_batch] record per point
+    uint32_t* flag;       // [max_batch] creation flags (kept until the batch commits)
+    uint32_t* rank;       // [max_batch] creation ranks
+    uint32_t* flag2;      // [max_batch] general flags
+    uint32_t* rank2;      // [max_batch] general scans
+    uint32_t* sk;         // [max_batch] sort keys (record id)
+    uint32_t* sv;         // [max_batch] sort values (point index)
+    uint32_t* seg_start;  // [max_batch + 1]
+    uint32_t* seg_end;    // [max_batch + 1]
+    uint32_t* seg_rec;    // [max_batch]
+    uint32_t* ev_rec;     // [max_batch] merge event record per point (kNoRec: none)
+    uint32_t* ev_list;    // [max_batch] compacted event point indices (ascending)
+    uint32_t* last_touch; // [max_batch] 1 if the point is its record's last touch
+    uint32_t* victims;    // [max_batch]
+    uint32_t* new_pos;    // [max_batch] point index of the j-th creation
+    void* merge;          // MergeScratch (k_merge.cu)
+    int merge_mode;
+    int merge_rounds;
+    int* d_n;             // batch size
+    int* d_n_new;
+    int* d_n_seg;
+    int* d_n_ev;
+    int* d_n_touch;
+    int* d_scratch_int;   // [16]
+    int max_batch;
+    SortScratch sort;
+    ScanScratch scan;
+};
+cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool);
+void map_scratch_free(MapScratch& ms);
+
+// Applies VoxelMap::update (build = false) or VoxelMap::build (build = true)
+// to batch points [0, *d_n) of bpts/bcov.
+void launch_map_phase_a(DMap& m, MapScratch& ms, const double* bpts, int n_max, cudaStream_t st);
+void launch_map_segments(DMap& m, MapScratch& ms, int n_max, cudaStream_t st);
+void launch_map_walk(DMap& m, MapScratch& ms, cudaStream_t st);
+void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st);
+void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
+                        cudaStream_t st);
+void launch_rehash(DMap& m, cudaStream_t st);
+void launch_queue_compact(DMap& m, uint32_t* flag, uint32_t* rank, uint32_t* tr, uint64_t* ts, int* d_len,
+                          int* d_live, int len_max, ScanScratch& sc, cudaStream_t st);
+void launch_map_index(const DMap& m, const double* pts, int n, int64_t* keys, cudaStream_t st);
+void launch_map_reset(DMap& m, cudaStream_t st);
+
+// ---- k_merge.cu
+cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool);
+void merge_scratch_free(void* p);
+// mode 0: parallel fixed point (sequential replay as fallback); 1: replay only
+cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, int mode, int* rounds_out,
+                             cudaStream_t st);
+
+}  // namespace vmp

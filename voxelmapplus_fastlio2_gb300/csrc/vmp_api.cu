@@ -1,0 +1,1023 @@
+// Host orchestration and the C ABI of libvmp (include/vmp.h).
+//
+// One vmp_stream owns a CUDA stream and every device buffer of one sensor
+// stream.  vmp_process follows LIOBuilder::process (lio_builder.cpp:175-248):
+//   IMU_INIT     accumulate IMU samples on the host until imu_init_num, then
+//                k_imu_init on the device;
+//   MAP_INIT     upload -> time sort -> IMU predict chain -> undistort ->
+//                float world transform + covariances of the full cloud ->
+//                VoxelMap::build;
+//   LIO_MAPPING  upload -> time sort -> predict chain -> undistort ->
+//                downsample -> calcBodyCov -> IESKF::update (ieskf_max_iter
+//                residual launches; the last CTA of each runs the FP64 step,
+//                later launches return at once after convergence) ->
+//                covariance update -> world points -> VoxelMap::update.
+// The scan's kernels are enqueued without host synchronisation; the call
+// ends with one device->host copy of the result.  Two conditions add a host
+// round trip: an IEKF-independent merge fixed point (one small read per
+// round, k_merge.cu) and a batch that can overflow the LRU capacity (the
+// eviction walk is read back to decide a split).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+using namespace vmp;
+
+namespace {
+
+struct DResult {
+    DState x;
+    double P[529];
+    int iters;
+    int effect_num;
+    int no_effect;
+    int n_down;
+    Counters cnt;
+};
+
+__global__ void k_gather_result(const DFilter* f, const int* d_n_down, const Counters* c, DResult* r) {
+    for (int e = threadIdx.x; e < 529; e += blockDim.x) r->P[e] = f->P[e];
+    if (threadIdx.x == 0) {
+        r->x = f->x;
+        r->iters = f->iters;
+        r->effect_num = f->effect_num;
+        r->no_effect = f->no_effect;
+        r->n_down = d_n_down ? *d_n_down : 0;
+        r->cnt = *c;
+    }
+}
+__global__ void k_clear_error(Counters* c) {
+    if (threadIdx.x == 0) c->error = 0;
+}
+__global__ void k_set_int(int* p, int v) {
+    if (threadIdx.x == 0) *p = v;
+}
+__global__ void k_copy_int(int* dst, const int* src) {
+    if (threadIdx.x == 0) *dst = *src;
+}
+__global__ void k_floats_to_points(const float* pts, int n, float4* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = make_float4(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2], 0.0f);
+}
+__global__ void k_reset_filter_iter(DFilter* f) {
+    if (threadIdx.x == 0) { f->converged = 0; f->iters = 0; f->effect_num = 0; f->no_effect = 0; }
+}
+__global__ void k_read_hm(const DFilter* f, double* H, double* b, int* eff) {
+    for (int e = threadIdx.x; e < 144; e += blockDim.x) H[e] = f->Hm[e];
+    if (threadIdx.x < 12) b[threadIdx.x] = f->bm[threadIdx.x];
+    if (threadIdx.x == 0) *eff = f->effect_num;
+}
+__global__ void k_valid_bytes(const uint8_t* v, int n, uint8_t* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v[i];
+}
+
+// Export of live records (device -> vmp_voxel).
+__global__ void k_export(DMap m, vmp_voxel* out, int* d_count, int max) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m.rec_pool; r += gridDim.x * blockDim.x) {
+        const RecHot& h = m.hot[r];
+        if (!(h.flags & F_ALIVE)) continue;
+        int pos = atomicAdd(d_count, 1);
+        if (pos >= max) continue;
+        const RecCold& c = m.cold[r];
+        vmp_voxel& v = out[pos];
+        int64_t x, y, z;
+        unpack_key(c.key, x, y, z);
+        v.key[0] = x; v.key[1] = y; v.key[2] = z;
+        v.n = h.n;
+        v.newly_add_point = c.newly;
+        v.is_init = (h.flags & F_INIT) ? 1 : 0;
+        v.is_plane = (h.flags & F_PLANE) ? 1 : 0;
+        v.update_enable = (h.flags & F_UPDATE) ? 1 : 0;
+        v.merged = (h.flags & F_MERGED) ? 1 : 0;
+        v.group_id = h.group;
+        v.lru_stamp = c.stamp;
+        v.n_temp = (h.flags & F_DROPPED) ? h.n : c.nslab;
+        v.pad = (int32_t)(r | ((h.flags & F_DROPPED) ? 0x40000000u : 0u));  // record id + "points not kept"
+        for (int k = 0; k < 3; ++k) { v.mean[k] = h.mean[k]; v.norm[k] = h.norm[k]; v.center[k] = c.center[k]; }
+        for (int k = 0; k < 9; ++k) v.ppt[k] = c.ppt[k];
+        for (int k = 0; k < 36; ++k) v.cov[k] = c.cov[k];
+    }
+}
+// Buffered points of the given records (offsets = prefix of their counts).
+__global__ void k_export_points(DMap m, const int* recs, const long long* offs, int nrec, double* pts, double* cov) {
+    for (int q = blockIdx.x; q < nrec; q += gridDim.x) {
+        const int r = recs[q];
+        const RecCold& c = m.cold[r];
+        const long long o = offs[q];
+        for (int j = threadIdx.x; j < c.nslab; j += blockDim.x) {
+            const double* s = m.slab + ((size_t)c.chunks[j / kChunkPts] * kChunkPts + (j % kChunkPts)) * kSlabStride;
+            for (int k = 0; k < 3; ++k) pts[(o + j) * 3 + k] = s[k];
+            for (int k = 0; k < 9; ++k) cov[(o + j) * 9 + k] = s[3 + k];
+        }
+    }
+}
+// Import: record q takes id q; LRU order given by the list (q = 0 most recent).
+__global__ void k_import(DMap m, const vmp_voxel* vox, int n, const long long* offs, const double* pts,
+                         const double* cov, unsigned long long stamp_top) {
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const vmp_voxel& v = vox[q];
+        const int r = q;
+        RecHot& h = m.hot[r];
+        RecCold& c = m.cold[r];
+        int ncopy = v.n_temp;
+        // buffered points that no refit can use any more are not kept: an
+        // updating voxel at or over max_point_thresh freezes on its next point
+        // before newly_add_point reaches update_size_thresh
+        bool dropped = v.update_enable && v.is_init && v.n_temp >= m.max_thresh &&
+                       v.newly_add_point + 1 < m.update_thresh;
+        if (!dropped && ncopy > kMaxChunks * kChunkPts) {
+            if (threadIdx.x == 0) set_error(m.cnt, E_CAPACITY);
+            ncopy = kMaxChunks * kChunkPts;
+        }
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < 3; ++k) { h.mean[k] = v.mean[k]; h.norm[k] = v.norm[k]; c.center[k] = v.center[k]; }
+            for (int k = 0; k < 9; ++k) c.ppt[k] = v.ppt[k];
+            for (int k = 0; k < 36; ++k) c.cov[k] = v.cov[k];
+            uint32_t fl = F_ALIVE;
+            if (v.is_init) fl |= F_INIT;
+            if (v.is_plane) fl |= F_PLANE;
+            if (v.update_enable) fl |= F_UPDATE;
+            if (v.merged) fl |= F_MERGED;
+            if (dropped) fl |= F_DROPPED;
+            h.flags = fl;
+            h.n = v.n;
+            h.group = v.group_id;
+            c.key = pack_key(v.key[0], v.key[1], v.key[2]);
+            c.stamp = stamp_top - (unsigned long long)q;
+            c.create_g = 0;
+            c.freeze_g = v.update_enable ? kNever : 0ull;
+            c.evict_g = kNever;
+            c.touch_first_g = kNever;
+            c.newly = v.newly_add_point;
+            c.nslab = 0;
+            for (int k = 0; k < kMaxChunks; ++k) c.chunks[k] = -1;
+            // slab chunks: ids taken from the end of the pool, record q -> a fixed range
+            if (!dropped && ncopy > 0) {
+                int nch = (ncopy + kChunkPts - 1) / kChunkPts;
+                int base_chunk = atomicAdd(&m.cnt->chunk_freed_top, nch);  // bump counter (reset below)
+                if (base_chunk + nch <= m.chunk_pool) {
+                    for (int k = 0; k < nch; ++k) c.chunks[k] = m.chunk_pool - 1 - (base_chunk + k);
+                    c.nslab = ncopy;
+                } else {
+                    set_error(m.cnt, E_CHUNKS);
+                }
+            }
+            // hash insert
+            uint64_t key = c.key;
+            uint64_t hh = hash_key(key) & m.table_mask;
+            for (uint64_t probe = 0; probe <= m.table_mask; ++probe) {
+                unsigned long long prev = atomicCAS((unsigned long long*)&m.keys[hh], (unsigned long long)kEmptyKey,
+                                                    (unsigned long long)key);
+                if (prev == kEmptyKey) { m.vals[hh] = (uint32_t)r; break; }
+                hh = (hh + 1) & m.table_mask;
+            }
+            // LRU queue: oldest first
+            m.q_rec[n - 1 - q] = (uint32_t)r;
+            m.q_stamp[n - 1 - q] = c.stamp;
+        }
+        __syncthreads();
+        if (!dropped && c.nslab > 0) {
+            const long long o = offs[q];
+            for (int j = threadIdx.x; j < c.nslab; j += blockDim.x) {
+                double* s = m.slab + ((size_t)c.chunks[j / kChunkPts] * kChunkPts + (j % kChunkPts)) * kSlabStride;
+                for (int k = 0; k < 3; ++k) s[k] = pts[(o + j) * 3 + k];
+                for (int k = 0; k < 9; ++k) s[3 + k] = cov[(o + j) * 9 + k];
+            }
+        }
+    }
+}
+__global__ void k_import_counters(DMap m, int n, long long group_counter, unsigned long long stamp_top) {
+    if (threadIdx.x != 0) return;
+    Counters* c = m.cnt;
+    int used_chunks = c->chunk_freed_top;
+    if (used_chunks > m.chunk_pool) used_chunks = m.chunk_pool;
+    c->chunk_freed_top = 0;
+    c->chunk_free_top = m.chunk_pool - used_chunks;
+    // records 0..n-1 are taken; the free stack holds n..pool-1 (pops give n, n+1, ...)
+    for (int i = 0; i < m.rec_pool - n; ++i) m.rec_free[i] = (uint32_t)(m.rec_pool - 1 - i);
+    c->rec_free_top = m.rec_pool - n;
+    c->size = n;
+    c->group_counter = group_counter;
+    c->batch_base = stamp_top + 1;
+    c->q_head = 0;
+    c->q_tail = (unsigned long long)n;
+    c->n_tomb = 0;
+}
+
+inline size_t next_pow2(size_t v) {
+    size_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+struct vmp_stream_s {
+    vmp_config cfg{};
+    cudaStream_t st = nullptr;
+    std::string err;
+    int lio_status = VMP_IMU_INIT;
+    std::vector<vmp_imu> imu_cache;
+    DFilter* f = nullptr;
+    DScan s{};
+    DMap m{};
+    Counters* cnt = nullptr;
+    MapScratch ms{};
+    SortScratch ss{};
+    ScanScratch sc{};
+    vmp_point* h_pts = nullptr;
+    vmp_imu* h_imus = nullptr;
+    DResult* h_res = nullptr;
+    DResult* d_res = nullptr;
+    Counters* h_cnt = nullptr;
+    int* h_int = nullptr;
+    double sin_deg = 0.0;
+    long long h_size = 0;
+    unsigned long long h_qlen = 0;
+    int h_tomb = 0;
+    // LRU queue compaction scratch
+    uint32_t* qc_flag = nullptr;
+    uint32_t* qc_rank = nullptr;
+    uint32_t* qc_rec = nullptr;
+    uint64_t* qc_stamp = nullptr;
+    int* qc_ints = nullptr;
+    ScanScratch qsc{};
+    std::vector<void*> allocs;
+    bool broken = false;
+    long long last_evicted_total = 0;
+};
+
+static vmp_status fail(vmp_stream_t s, vmp_status code, const std::string& msg) {
+    if (s) s->err = msg;
+    return code;
+}
+static vmp_status cuda_fail(vmp_stream_t s, cudaError_t e, const char* where) {
+    if (s) {
+        s->err = std::string(where) + ": " + cudaGetErrorString(e);
+        s->broken = true;
+    }
+    return VMP_ERR_CUDA;
+}
+
+#define VMP_TRY(expr, where)                          \
+    do {                                              \
+        cudaError_t e_ = (expr);                      \
+        if (e_ != cudaSuccess) return cuda_fail(s, e_, where); \
+    } while (0)
+
+template <typename T>
+static cudaError_t dalloc(vmp_stream_t s, T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count < 1 ? 1 : count));
+    if (e == cudaSuccess) s->allocs.push_back(*p);
+    return e;
+}
+
+static vmp_status validate(const vmp_config* c, std::string& why) {
+    if (!(c->voxel_size > 0)) { why = "voxel_size must be > 0"; return VMP_ERR_INVALID_ARG; }
+    if (!(c->scan_resolution >= 0)) { why = "scan_resolution must be >= 0"; return VMP_ERR_INVALID_ARG; }
+    if (c->update_size_thresh < 2 || c->update_size_thresh > kMaxChunks * kChunkPts) {
+        why = "update_size_thresh must be in [2, 256]";
+        return VMP_ERR_INVALID_ARG;
+    }
+    if (c->max_point_thresh < 1 || c->max_point_thresh > kMaxChunks * kChunkPts) {
+        why = "max_point_thresh must be in [1, 256]";
+        return VMP_ERR_INVALID_ARG;
+    }
+    if (c->max_point_thresh < c->update_size_thresh) {
+        why = "max_point_thresh must be >= update_size_thresh";
+        return VMP_ERR_INVALID_ARG;
+    }
+    if (c->map_capacity < 1) { why = "map_capacity must be >= 1"; return VMP_ERR_INVALID_ARG; }
+    if (c->ieskf_max_iter < 1 || c->ieskf_max_iter > 64) { why = "ieskf_max_iter must be in [1, 64]"; return VMP_ERR_INVALID_ARG; }
+    if (c->max_scan_points < 1 || c->max_scan_points > (1 << 24)) { why = "max_scan_points must be in [1, 2^24]"; return VMP_ERR_INVALID_ARG; }
+    if (c->max_imu_per_scan < 1 || c->max_imu_per_scan > 1000) { why = "max_imu_per_scan must be in [1, 1000]"; return VMP_ERR_INVALID_ARG; }
+    if (c->imu_init_num < 1) { why = "imu_init_num must be >= 1"; return VMP_ERR_INVALID_ARG; }
+    return VMP_OK;
+}
+
+extern "C" {
+
+int vmp_abi_version(void) { return VMP_ABI_VERSION; }
+
+void vmp_config_default(vmp_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->opti_max_iter = 5;
+    c->na = 0.01; c->ng = 0.01; c->nba = 0.0001; c->nbg = 0.0001;
+    c->imu_init_num = 20;
+    c->r_il[0] = c->r_il[4] = c->r_il[8] = 1.0;
+    c->gravity_align = 1;
+    c->estimate_ext = 0;
+    c->scan_resolution = 0.1;
+    c->voxel_size = 0.5;
+    c->update_size_thresh = 10;
+    c->max_point_thresh = 100;
+    c->plane_thresh = 0.01;
+    c->ranging_cov = 0.04;
+    c->angle_cov = 0.1;
+    c->merge_thresh_for_angle = 0.1;
+    c->merge_thresh_for_distance = 0.04;
+    c->map_capacity = 100000;
+    c->ieskf_max_iter = 5;
+    c->ieskf_eps = 0.001;
+    c->max_scan_points = 262144;
+    c->max_imu_per_scan = 1000;
+}
+
+const char* vmp_last_error(vmp_stream_t s) { return s ? s->err.c_str() : "null handle"; }
+
+vmp_status vmp_destroy(vmp_stream_t s) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    if (s->st) cudaStreamSynchronize(s->st);
+    for (void* p : s->allocs) cudaFree(p);
+    map_scratch_free(s->ms);
+    sort_scratch_free(s->ss);
+    scan_scratch_free(s->sc);
+    scan_scratch_free(s->qsc);
+    cudaFreeHost(s->h_pts);
+    cudaFreeHost(s->h_imus);
+    cudaFreeHost(s->h_res);
+    cudaFreeHost(s->h_cnt);
+    cudaFreeHost(s->h_int);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return VMP_OK;
+}
+
+vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
+    if (!out) return VMP_ERR_INVALID_ARG;
+    *out = nullptr;
+    vmp_config cfg;
+    if (cfg_in) cfg = *cfg_in; else vmp_config_default(&cfg);
+    if (cfg.max_imu_per_scan <= 0) cfg.max_imu_per_scan = 1000;
+    if (cfg.max_scan_points <= 0) cfg.max_scan_points = 262144;
+    std::string why;
+    vmp_status v = validate(&cfg, why);
+    if (v != VMP_OK) return v;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return VMP_ERR_CUDA;
+    vmp_stream_t s = new (std::nothrow) vmp_stream_s();
+    if (!s) return VMP_ERR_OUT_OF_MEMORY;
+    s->cfg = cfg;
+    cudaError_t e;
+#define CREATE_TRY(expr)                         \
+    do {                                         \
+        e = (expr);                              \
+        if (e != cudaSuccess) {                  \
+            vmp_destroy(s);                      \
+            return e == cudaErrorMemoryAllocation ? VMP_ERR_OUT_OF_MEMORY : VMP_ERR_CUDA; \
+        }                                        \
+    } while (0)
+    CREATE_TRY(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    const int max_pts = cfg.max_scan_points;
+    const int max_imu = cfg.max_imu_per_scan;
+    s->sin_deg = std::sin(cfg.angle_cov * 0.017453293);  // pcl_macros.h DEG2RAD
+    // filter
+    CREATE_TRY(dalloc(s, &s->f, 1));
+    CREATE_TRY(cudaMemset(s->f, 0, sizeof(DFilter)));
+    {
+        DFilter hf;
+        std::memset(&hf, 0, sizeof(hf));
+        // kf::State defaults (ieskf.h:35-42)
+        hf.x.rot[0] = hf.x.rot[4] = hf.x.rot[8] = 1.0;
+        hf.x.rot_ext[0] = hf.x.rot_ext[4] = hf.x.rot_ext[8] = 1.0;
+        hf.x.g[2] = -kGravity;
+        // LIODataGroup::Q (lio_builder.cpp:9-12, lio_builder.h:52)
+        for (int i = 0; i < 12; ++i) hf.Q[i * 13] = 1.0;
+        for (int i = 0; i < 3; ++i) {
+            hf.Q[i * 13] = cfg.ng;
+            hf.Q[(3 + i) * 13] = cfg.na;
+            hf.Q[(6 + i) * 13] = cfg.nbg;
+            hf.Q[(9 + i) * 13] = cfg.nba;
+        }
+        CREATE_TRY(cudaMemcpy(s->f, &hf, sizeof(hf), cudaMemcpyHostToDevice));
+    }
+    // scan buffers
+    DScan& sc = s->s;
+    sc.max_pts = max_pts;
+    sc.max_imu = max_imu;
+    sc.res_blocks = 2 * 152;
+    CREATE_TRY(dalloc(s, &sc.raw, max_pts));
+    CREATE_TRY(dalloc(s, &sc.cloud, max_pts));
+    CREATE_TRY(dalloc(s, &sc.sort_k, max_pts + 16));
+    CREATE_TRY(dalloc(s, &sc.sort_v, max_pts + 16));
+    CREATE_TRY(dalloc(s, &sc.flags, max_pts + 16));
+    CREATE_TRY(dalloc(s, &sc.scan_out, max_pts + 16));
+    CREATE_TRY(dalloc(s, &sc.d_n_raw, 4));
+    CREATE_TRY(dalloc(s, &sc.down, max_pts));
+    CREATE_TRY(dalloc(s, &sc.d_n_down, 4));
+    CREATE_TRY(dalloc(s, &sc.minmax, 8));
+    CREATE_TRY(dalloc(s, &sc.blk_minmax, 152 * 6 + 8));
+    CREATE_TRY(dalloc(s, &sc.ds_params, 32));
+    CREATE_TRY(dalloc(s, &sc.run_start, max_pts + 16));
+    CREATE_TRY(dalloc(s, &sc.pl, (size_t)max_pts * 3));
+    CREATE_TRY(dalloc(s, &sc.covl, (size_t)max_pts * 9));
+    CREATE_TRY(dalloc(s, &sc.rvalid, max_pts));
+    CREATE_TRY(cudaMemset(sc.rvalid, 0, max_pts));
+    CREATE_TRY(dalloc(s, &sc.rnorm, (size_t)max_pts * 3));
+    CREATE_TRY(cudaMemset(sc.rnorm, 0, sizeof(double) * (size_t)max_pts * 3));
+    CREATE_TRY(dalloc(s, &sc.rres, max_pts));
+    CREATE_TRY(cudaMemset(sc.rres, 0, sizeof(double) * (size_t)max_pts));
+    CREATE_TRY(dalloc(s, &sc.bpts, (size_t)max_pts * 3));
+    CREATE_TRY(dalloc(s, &sc.bcov, (size_t)max_pts * 9));
+    CREATE_TRY(dalloc(s, &sc.d_n_batch, 4));
+    CREATE_TRY(dalloc(s, &sc.imus, max_imu + 8));
+    CREATE_TRY(dalloc(s, &sc.poses, max_imu + 8));
+    CREATE_TRY(dalloc(s, &sc.partials, (size_t)sc.res_blocks * 160));
+    CREATE_TRY(dalloc(s, &sc.done_ctr, 4));
+    CREATE_TRY(cudaMemset(sc.done_ctr, 0, sizeof(unsigned int) * 4));
+    CREATE_TRY(sort_scratch_alloc(s->ss, max_pts));
+    CREATE_TRY(scan_scratch_alloc(s->sc, max_pts));
+    // map
+    DMap& m = s->m;
+    const long long cap = cfg.map_capacity;
+    const long long pool = cap + max_pts + 16;
+    if (pool > 0x7FFFFFF0LL) { vmp_destroy(s); return VMP_ERR_INVALID_ARG; }
+    m.rec_pool = (int)pool;
+    const size_t tsize = next_pow2((size_t)(2 * pool) < 1024 ? 1024 : (size_t)(2 * pool));
+    m.table_mask = tsize - 1;
+    long long chunks = cfg.reserved[0] > 0 ? (long long)cfg.reserved[0] : 2 * pool + 1024;
+    if (chunks > 0x7FFFFFF0LL) chunks = 0x7FFFFFF0LL;
+    m.chunk_pool = (int)chunks;
+    m.q_cap = (uint64_t)(2 * pool + 2 * (long long)max_pts);
+    m.voxel_size = cfg.voxel_size;
+    m.update_thresh = cfg.update_size_thresh;
+    m.max_thresh = cfg.max_point_thresh;
+    m.plane_thresh = cfg.plane_thresh;
+    m.merge_angle = cfg.merge_thresh_for_angle;
+    m.merge_dist = cfg.merge_thresh_for_distance;
+    m.capacity = cap;
+    CREATE_TRY(dalloc(s, &m.keys, tsize));
+    CREATE_TRY(dalloc(s, &m.vals, tsize));
+    CREATE_TRY(dalloc(s, &m.hot, pool));
+    CREATE_TRY(dalloc(s, &m.cold, pool));
+    CREATE_TRY(dalloc(s, &m.rec_free, pool));
+    CREATE_TRY(dalloc(s, &m.slab, (size_t)chunks * kChunkPts * kSlabStride));
+    CREATE_TRY(dalloc(s, &m.chunk_free, chunks));
+    CREATE_TRY(dalloc(s, &m.chunk_freed, chunks));
+    CREATE_TRY(dalloc(s, &m.q_rec, m.q_cap));
+    CREATE_TRY(dalloc(s, &m.q_stamp, m.q_cap));
+    CREATE_TRY(dalloc(s, &s->cnt, 1));
+    m.cnt = s->cnt;
+    CREATE_TRY(cudaMemset(s->cnt, 0, sizeof(Counters)));
+    CREATE_TRY(map_scratch_alloc(s->ms, max_pts, m.rec_pool));
+    // queue compaction scratch
+    const int qmax = (int)std::min<uint64_t>(m.q_cap, 0x7FFFFFF0ull);
+    CREATE_TRY(dalloc(s, &s->qc_flag, qmax));
+    CREATE_TRY(dalloc(s, &s->qc_rank, qmax));
+    CREATE_TRY(dalloc(s, &s->qc_rec, qmax));
+    CREATE_TRY(dalloc(s, &s->qc_stamp, qmax));
+    CREATE_TRY(dalloc(s, &s->qc_ints, 8));
+    CREATE_TRY(scan_scratch_alloc(s->qsc, qmax));
+    // pinned host staging
+    CREATE_TRY(cudaMallocHost(&s->h_pts, sizeof(vmp_point) * (size_t)max_pts));
+    CREATE_TRY(cudaMallocHost(&s->h_imus, sizeof(vmp_imu) * (size_t)(max_imu + 8)));
+    CREATE_TRY(cudaMallocHost(&s->h_res, sizeof(DResult)));
+    CREATE_TRY(cudaMallocHost(&s->h_cnt, sizeof(Counters)));
+    CREATE_TRY(cudaMallocHost(&s->h_int, sizeof(int) * 16));
+    CREATE_TRY(dalloc(s, &s->d_res, 1));
+    launch_map_reset(m, s->st);
+    CREATE_TRY(cudaGetLastError());
+    CREATE_TRY(cudaStreamSynchronize(s->st));
+#undef CREATE_TRY
+    *out = s;
+    return VMP_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ internals
+static bool is_pinned_or_device(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static vmp_status read_counters(vmp_stream_t s) {
+    VMP_TRY(cudaMemcpyAsync(s->h_cnt, s->cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s->st), "read counters");
+    VMP_TRY(cudaStreamSynchronize(s->st), "sync");
+    s->h_size = s->h_cnt->size;
+    s->h_qlen = s->h_cnt->q_tail - s->h_cnt->q_head;
+    s->h_tomb = s->h_cnt->n_tomb;
+    return VMP_OK;
+}
+
+static void map_maintenance(vmp_stream_t s) {
+    DMap& m = s->m;
+    if ((size_t)s->h_tomb > (size_t)(m.table_mask + 1) / 8) {
+        launch_rehash(m, s->st);
+        s->h_tomb = 0;
+    }
+    if (s->h_qlen + 2ull * (unsigned long long)s->cfg.max_scan_points > m.q_cap) {
+        // queue length is read on the device
+        int* d_len = s->qc_ints;
+        int* d_live = s->qc_ints + 1;
+        k_set_int<<<1, 32, 0, s->st>>>(d_len, (int)s->h_qlen);
+        launch_queue_compact(m, s->qc_flag, s->qc_rank, s->qc_rec, s->qc_stamp, d_len, d_live,
+                             (int)std::min<uint64_t>(m.q_cap, 0x7FFFFFF0ull), s->qsc, s->st);
+        s->h_qlen = 0;  // refreshed at the next counter read
+    }
+}
+
+// Applies batch points [0, n) of (bpts, bcov) where n is on the device
+// (d_n_src) or on the host (n_host >= 0).  n_upper bounds n.
+static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bcov, const int* d_n_src, int n_host,
+                            int n_upper, bool build) {
+    DMap& m = s->m;
+    MapScratch& ms = s->ms;
+    map_maintenance(s);
+    const bool evict_possible = s->h_size + (long long)n_upper > m.capacity;
+    if (d_n_src) k_copy_int<<<1, 32, 0, s->st>>>(ms.d_n, d_n_src);
+    else k_set_int<<<1, 32, 0, s->st>>>(ms.d_n, n_host);
+    const int n_max = n_upper;
+    if (!evict_possible) {
+        launch_map_phase_a(m, ms, bpts, n_max, s->st);
+        launch_map_segments(m, ms, n_max, s->st);
+        launch_map_phase_b(m, ms, bpts, bcov, n_max, build, s->st);
+        VMP_TRY(cudaGetLastError(), "map update launch");
+        s->h_size += n_upper;  // upper bound until the next counter read
+        return VMP_OK;
+    }
+    // eviction possible: know n exactly, then walk
+    int n = n_host;
+    if (d_n_src) {
+        VMP_TRY(cudaMemcpyAsync(s->h_int, d_n_src, sizeof(int), cudaMemcpyDeviceToHost, s->st), "read n");
+        VMP_TRY(cudaStreamSynchronize(s->st), "sync");
+        n = s->h_int[0];
+        k_set_int<<<1, 32, 0, s->st>>>(ms.d_n, n);
+    }
+    if (n <= 0) return VMP_OK;
+    launch_map_phase_a(m, ms, bpts, n, s->st);
+    launch_map_segments(m, ms, n, s->st);
+    launch_map_walk(m, ms, s->st);
+    vmp_status st = read_counters(s);
+    if (st != VMP_OK) return st;
+    const int split = s->h_cnt->split_at;
+    if (split < 0) {
+        launch_map_phase_b(m, ms, bpts, bcov, n, build, s->st);
+        VMP_TRY(cudaGetLastError(), "map update launch");
+        return read_counters(s);
+    }
+    launch_map_rollback(m, ms, n, s->st);
+    st = read_counters(s);
+    if (st != VMP_OK) return st;
+    if (split <= 0 || split >= n) return fail(s, VMP_ERR_STATE, "eviction split outside the batch");
+    st = map_apply(s, bpts, bcov, nullptr, split, split, build);
+    if (st != VMP_OK) return st;
+    st = read_counters(s);
+    if (st != VMP_OK) return st;
+    return map_apply(s, bpts + (size_t)split * 3, bcov + (size_t)split * 9, nullptr, n - split, n - split, build);
+}
+
+static vmp_status upload_scan(vmp_stream_t s, const vmp_point* pts, int n, bool device_ptr) {
+    if (device_ptr) {
+        VMP_TRY(cudaMemcpyAsync(s->s.raw, pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyDeviceToDevice, s->st), "scan copy");
+    } else if (is_pinned_or_device(pts)) {
+        VMP_TRY(cudaMemcpyAsync(s->s.raw, pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyDefault, s->st), "scan upload");
+    } else {
+        VMP_TRY(cudaStreamSynchronize(s->st), "sync");
+        std::memcpy(s->h_pts, pts, sizeof(vmp_point) * (size_t)n);
+        VMP_TRY(cudaMemcpyAsync(s->s.raw, s->h_pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyHostToDevice, s->st), "scan upload");
+    }
+    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
+    return VMP_OK;
+}
+
+static vmp_status upload_imus(vmp_stream_t s, const vmp_imu* imus, int n, bool device_ptr) {
+    if (n <= 0) return VMP_OK;
+    if (device_ptr) {
+        VMP_TRY(cudaMemcpyAsync(s->s.imus, imus, sizeof(vmp_imu) * (size_t)n, cudaMemcpyDeviceToDevice, s->st), "imu copy");
+    } else {
+        VMP_TRY(cudaStreamSynchronize(s->st), "sync");
+        std::memcpy(s->h_imus, imus, sizeof(vmp_imu) * (size_t)n);
+        VMP_TRY(cudaMemcpyAsync(s->s.imus, s->h_imus, sizeof(vmp_imu) * (size_t)n, cudaMemcpyHostToDevice, s->st), "imu upload");
+    }
+    return VMP_OK;
+}
+
+static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
+    k_gather_result<<<1, 256, 0, s->st>>>(s->f, s->s.d_n_down, s->cnt, s->d_res);
+    VMP_TRY(cudaGetLastError(), "result launch");
+    VMP_TRY(cudaMemcpyAsync(s->h_res, s->d_res, sizeof(DResult), cudaMemcpyDeviceToHost, s->st), "result copy");
+    VMP_TRY(cudaStreamSynchronize(s->st), "scan");
+    const DResult& r = *s->h_res;
+    s->h_size = r.cnt.size;
+    s->h_qlen = r.cnt.q_tail - r.cnt.q_head;
+    s->h_tomb = r.cnt.n_tomb;
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        out->lio_status = s->lio_status;
+        out->iters = r.iters;
+        out->effect_num = r.effect_num;
+        out->n_raw = n_raw;
+        out->n_down = r.n_down;
+        out->flags = r.no_effect ? 1 : 0;
+        out->map_size = r.cnt.size;
+        out->evicted = r.cnt.evicted_total - s->last_evicted_total;
+        std::memcpy(&out->x, &r.x, sizeof(vmp_state));
+        std::memcpy(out->P, r.P, sizeof(r.P));
+    }
+    s->last_evicted_total = r.cnt.evicted_total;
+    if (r.cnt.error) {
+        unsigned int e = r.cnt.error;
+        k_clear_error<<<1, 32, 0, s->st>>>(s->cnt);
+        cudaStreamSynchronize(s->st);
+        if (e & E_KEY_RANGE) return fail(s, VMP_ERR_KEY_RANGE, "a voxel index left the packed range [-2^20, 2^20)");
+        if (e & E_HASH_FULL) return fail(s, VMP_ERR_HASH_FULL, "voxel hash table full");
+        if (e & (E_RECORDS | E_CHUNKS | E_CAPACITY))
+            return fail(s, VMP_ERR_CAPACITY, "voxel record / slab pool exhausted (error bits " + std::to_string(e) + ")");
+    }
+    return VMP_OK;
+}
+
+static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, double t_start, double t_end,
+                               const vmp_imu* imus, int n_imu, bool device_ptrs, vmp_result* out) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    if (!pts || n <= 0) return fail(s, VMP_ERR_INVALID_ARG, "empty scan");
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "scan larger than max_scan_points");
+    if (!imus || n_imu <= 0) return fail(s, VMP_ERR_INVALID_ARG, "package without IMU samples");
+    if (n_imu > s->cfg.max_imu_per_scan) return fail(s, VMP_ERR_CAPACITY, "more IMU samples than max_imu_per_scan");
+    const vmp_config& cfg = s->cfg;
+    cudaStream_t st = s->st;
+    if (s->lio_status == VMP_IMU_INIT) {
+        // LIOBuilder::initializeImu: accumulate on the host, initialise on the device
+        size_t old = s->imu_cache.size();
+        s->imu_cache.resize(old + n_imu);
+        if (device_ptrs) {
+            VMP_TRY(cudaMemcpy(s->imu_cache.data() + old, imus, sizeof(vmp_imu) * n_imu, cudaMemcpyDeviceToHost), "imu read");
+        } else {
+            std::memcpy(s->imu_cache.data() + old, imus, sizeof(vmp_imu) * n_imu);
+        }
+        if ((int)s->imu_cache.size() >= cfg.imu_init_num) {
+            vmp_imu* d_all = nullptr;
+            VMP_TRY(cudaMalloc(&d_all, sizeof(vmp_imu) * s->imu_cache.size()), "imu init alloc");
+            cudaMemcpyAsync(d_all, s->imu_cache.data(), sizeof(vmp_imu) * s->imu_cache.size(), cudaMemcpyHostToDevice, st);
+            launch_imu_init(s->f, d_all, (int)s->imu_cache.size(), cfg, t_end, st);
+            cudaError_t e = cudaStreamSynchronize(st);
+            cudaFree(d_all);
+            if (e != cudaSuccess) return cuda_fail(s, e, "imu init");
+            s->imu_cache.clear();
+            s->lio_status = VMP_MAP_INIT;
+        }
+        k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
+        return finish_result(s, n, out);
+    }
+    vmp_status v = upload_scan(s, pts, n, device_ptrs);
+    if (v != VMP_OK) return v;
+    v = upload_imus(s, imus, n_imu, device_ptrs);
+    if (v != VMP_OK) return v;
+    launch_time_sort(s->s, n, s->ss, st);
+    launch_predict_chain(s->f, s->s, n_imu, t_start, t_end, st);
+    launch_undistort(s->f, s->s, n, st);
+    if (s->lio_status == VMP_MAP_INIT) {
+        launch_map_batch(s->f, s->s, n, true, cfg.ranging_cov, s->sin_deg, st);
+        k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
+        VMP_TRY(cudaGetLastError(), "map init launch");
+        v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, n, true);
+        if (v != VMP_OK) return v;
+        s->lio_status = VMP_LIO_MAPPING;
+        return finish_result(s, n, out);
+    }
+    if (cfg.scan_resolution > 0.0) launch_downsample(s->s, n, cfg.scan_resolution, s->ss, s->sc, st);
+    else launch_copy_down(s->s, n, st);
+    launch_body_cov(s->s, n, cfg.ranging_cov, s->sin_deg, st);
+    launch_update_begin(s->f, st);
+    for (int it = 0; it < cfg.ieskf_max_iter; ++it)
+        launch_residual_iter(s->f, s->s, s->m, n, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+    launch_update_end(s->f, st);
+    launch_map_batch(s->f, s->s, n, false, cfg.ranging_cov, s->sin_deg, st);
+    VMP_TRY(cudaGetLastError(), "scan launch");
+    v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, n, false);
+    if (v != VMP_OK) return v;
+    return finish_result(s, n, out);
+}
+
+extern "C" {
+
+vmp_status vmp_process(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* imus, int n_imu, vmp_result* out) {
+    if (!s || !scan) return VMP_ERR_INVALID_ARG;
+    return process_impl(s, scan->points, scan->n, scan->t_start, scan->t_end, imus, n_imu, false, out);
+}
+
+vmp_status vmp_process_device(vmp_stream_t s, const vmp_point* d_points, int n, double t_start, double t_end,
+                              const vmp_imu* d_imus, int n_imu, vmp_result* out) {
+    return process_impl(s, d_points, n, t_start, t_end, d_imus, n_imu, true, out);
+}
+
+// ------------------------------------------------------------- component API
+static vmp_status stage_doubles(vmp_stream_t s, double* dst, const double* src, size_t count) {
+    VMP_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyHostToDevice, s->st), "upload");
+    return VMP_OK;
+}
+
+vmp_status vmp_map_index(vmp_stream_t s, const double* pts, int n, int64_t* keys) {
+    if (!s || (!pts && n > 0) || (!keys && n > 0) || n < 0) return VMP_ERR_INVALID_ARG;
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
+    if (n == 0) return VMP_OK;
+    vmp_status v = stage_doubles(s, s->s.bpts, pts, (size_t)n * 3);
+    if (v != VMP_OK) return v;
+    int64_t* d_keys = reinterpret_cast<int64_t*>(s->s.bcov);
+    launch_map_index(s->m, s->s.bpts, n, d_keys, s->st);
+    VMP_TRY(cudaMemcpyAsync(keys, d_keys, sizeof(int64_t) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->st), "keys");
+    VMP_TRY(cudaStreamSynchronize(s->st), "index");
+    return VMP_OK;
+}
+
+static vmp_status map_component(vmp_stream_t s, const double* pts, const double* cov, int n, bool build) {
+    if (!s || n < 0 || (n > 0 && (!pts || !cov))) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
+    if (build) {
+        vmp_status v = read_counters(s);
+        if (v != VMP_OK) return v;
+        if (s->h_cnt->size != 0) return fail(s, VMP_ERR_STATE, "VoxelMap::build on a non-empty map");
+    }
+    if (n == 0) return VMP_OK;
+    vmp_status v = stage_doubles(s, s->s.bpts, pts, (size_t)n * 3);
+    if (v != VMP_OK) return v;
+    v = stage_doubles(s, s->s.bcov, cov, (size_t)n * 9);
+    if (v != VMP_OK) return v;
+    v = map_apply(s, s->s.bpts, s->s.bcov, nullptr, n, n, build);
+    if (v != VMP_OK) return v;
+    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, 0);
+    return finish_result(s, n, nullptr);
+}
+
+vmp_status vmp_map_build(vmp_stream_t s, const double* pts, const double* cov, int n) {
+    return map_component(s, pts, cov, n, true);
+}
+vmp_status vmp_map_update(vmp_stream_t s, const double* pts, const double* cov, int n) {
+    return map_component(s, pts, cov, n, false);
+}
+
+vmp_status vmp_map_info_get(vmp_stream_t s, vmp_map_info* info) {
+    if (!s || !info) return VMP_ERR_INVALID_ARG;
+    vmp_status v = read_counters(s);
+    if (v != VMP_OK) return v;
+    info->size = s->h_cnt->size;
+    info->capacity = s->m.capacity;
+    info->group_counter = s->h_cnt->group_counter;
+    // buffered points: exported on demand
+    std::vector<vmp_voxel> tmp;
+    info->slab_points = -1;
+    return VMP_OK;
+}
+
+static vmp_status export_all(vmp_stream_t s, std::vector<vmp_voxel>& out) {
+    vmp_status v = read_counters(s);
+    if (v != VMP_OK) return v;
+    const long long n = s->h_cnt->size;
+    out.resize((size_t)n);
+    if (n == 0) return VMP_OK;
+    vmp_voxel* d = nullptr;
+    int* d_count = nullptr;
+    VMP_TRY(cudaMalloc(&d, sizeof(vmp_voxel) * (size_t)n), "export alloc");
+    VMP_TRY(cudaMalloc(&d_count, sizeof(int)), "export alloc");
+    cudaMemsetAsync(d_count, 0, sizeof(int), s->st);
+    k_export<<<1216, 256, 0, s->st>>>(s->m, d, d_count, (int)n);
+    cudaMemcpyAsync(out.data(), d, sizeof(vmp_voxel) * (size_t)n, cudaMemcpyDeviceToHost, s->st);
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    cudaFree(d);
+    cudaFree(d_count);
+    if (e != cudaSuccess) return cuda_fail(s, e, "export");
+    std::sort(out.begin(), out.end(), [](const vmp_voxel& a, const vmp_voxel& b) { return a.lru_stamp > b.lru_stamp; });
+    return VMP_OK;
+}
+
+vmp_status vmp_map_export(vmp_stream_t s, vmp_voxel* out, long long max, long long* n_out) {
+    if (!s || (!out && max > 0)) return VMP_ERR_INVALID_ARG;
+    std::vector<vmp_voxel> all;
+    vmp_status v = export_all(s, all);
+    if (v != VMP_OK) return v;
+    long long n = std::min<long long>(max, (long long)all.size());
+    if (n > 0) std::memcpy(out, all.data(), sizeof(vmp_voxel) * (size_t)n);
+    if (n_out) *n_out = (long long)all.size();
+    return VMP_OK;
+}
+
+vmp_status vmp_map_export_points(vmp_stream_t s, double* pts, double* cov, long long max_points, long long* n_out) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    std::vector<vmp_voxel> all;
+    vmp_status v = export_all(s, all);
+    if (v != VMP_OK) return v;
+    std::vector<int> recs;
+    std::vector<long long> offs;
+    long long total = 0;
+    for (const vmp_voxel& x : all) {
+        // voxels whose buffered points were not kept (no refit can use them)
+        // contribute none
+        const bool stored = !(x.pad & 0x40000000);
+        const int cnt = stored ? x.n_temp : 0;
+        recs.push_back(x.pad & 0x3FFFFFFF);
+        offs.push_back(total);
+        total += cnt;
+    }
+    if (n_out) *n_out = total;
+    if (!pts || !cov || total == 0) return VMP_OK;
+    if (total > max_points) return fail(s, VMP_ERR_CAPACITY, "max_points too small");
+    int* d_recs = nullptr;
+    long long* d_offs = nullptr;
+    double *d_p = nullptr, *d_c = nullptr;
+    VMP_TRY(cudaMalloc(&d_recs, sizeof(int) * recs.size()), "alloc");
+    VMP_TRY(cudaMalloc(&d_offs, sizeof(long long) * offs.size()), "alloc");
+    VMP_TRY(cudaMalloc(&d_p, sizeof(double) * 3 * (size_t)total), "alloc");
+    VMP_TRY(cudaMalloc(&d_c, sizeof(double) * 9 * (size_t)total), "alloc");
+    cudaMemcpyAsync(d_recs, recs.data(), sizeof(int) * recs.size(), cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(d_offs, offs.data(), sizeof(long long) * offs.size(), cudaMemcpyHostToDevice, s->st);
+    k_export_points<<<1216, 128, 0, s->st>>>(s->m, d_recs, d_offs, (int)recs.size(), d_p, d_c);
+    cudaMemcpyAsync(pts, d_p, sizeof(double) * 3 * (size_t)total, cudaMemcpyDeviceToHost, s->st);
+    cudaMemcpyAsync(cov, d_c, sizeof(double) * 9 * (size_t)total, cudaMemcpyDeviceToHost, s->st);
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    cudaFree(d_recs); cudaFree(d_offs); cudaFree(d_p); cudaFree(d_c);
+    if (e != cudaSuccess) return cuda_fail(s, e, "export points");
+    return VMP_OK;
+}
+
+vmp_status vmp_map_import(vmp_stream_t s, const vmp_voxel* vox, long long n, const double* pts, const double* cov,
+                          long long group_counter) {
+    if (!s || n < 0 || (n > 0 && !vox)) return VMP_ERR_INVALID_ARG;
+    if (n > s->m.capacity) return fail(s, VMP_ERR_CAPACITY, "more voxels than map_capacity");
+    std::vector<long long> offs((size_t)n + 1, 0);
+    long long total = 0;
+    for (long long i = 0; i < n; ++i) {
+        offs[(size_t)i] = total;
+        total += vox[i].n_temp;
+    }
+    if (total > 0 && (!pts || !cov)) return VMP_ERR_INVALID_ARG;
+    launch_map_reset(s->m, s->st);
+    if (n > 0) {
+        vmp_voxel* d_v = nullptr;
+        long long* d_o = nullptr;
+        double *d_p = nullptr, *d_c = nullptr;
+        VMP_TRY(cudaMalloc(&d_v, sizeof(vmp_voxel) * (size_t)n), "alloc");
+        VMP_TRY(cudaMalloc(&d_o, sizeof(long long) * (size_t)(n + 1)), "alloc");
+        VMP_TRY(cudaMalloc(&d_p, sizeof(double) * 3 * (size_t)(total + 1)), "alloc");
+        VMP_TRY(cudaMalloc(&d_c, sizeof(double) * 9 * (size_t)(total + 1)), "alloc");
+        cudaMemcpyAsync(d_v, vox, sizeof(vmp_voxel) * (size_t)n, cudaMemcpyHostToDevice, s->st);
+        cudaMemcpyAsync(d_o, offs.data(), sizeof(long long) * (size_t)(n + 1), cudaMemcpyHostToDevice, s->st);
+        if (total > 0) {
+            cudaMemcpyAsync(d_p, pts, sizeof(double) * 3 * (size_t)total, cudaMemcpyHostToDevice, s->st);
+            cudaMemcpyAsync(d_c, cov, sizeof(double) * 9 * (size_t)total, cudaMemcpyHostToDevice, s->st);
+        }
+        const unsigned long long stamp_top = (unsigned long long)n + 1;
+        k_set_int<<<1, 32, 0, s->st>>>(&s->cnt->chunk_freed_top, 0);
+        k_import<<<1216, 128, 0, s->st>>>(s->m, d_v, (int)n, d_o, d_p, d_c, stamp_top);
+        k_import_counters<<<1, 32, 0, s->st>>>(s->m, (int)n, group_counter, stamp_top);
+        cudaError_t e = cudaStreamSynchronize(s->st);
+        cudaFree(d_v); cudaFree(d_o); cudaFree(d_p); cudaFree(d_c);
+        if (e != cudaSuccess) return cuda_fail(s, e, "import");
+    } else {
+        k_import_counters<<<1, 32, 0, s->st>>>(s->m, 0, group_counter, 1ull);
+    }
+    return read_counters(s);
+}
+
+vmp_status vmp_get_state(vmp_stream_t s, vmp_state* x, double* P) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    if (x) VMP_TRY(cudaMemcpyAsync(x, &s->f->x, sizeof(vmp_state), cudaMemcpyDeviceToHost, s->st), "state");
+    if (P) VMP_TRY(cudaMemcpyAsync(P, s->f->P, sizeof(double) * 529, cudaMemcpyDeviceToHost, s->st), "P");
+    VMP_TRY(cudaStreamSynchronize(s->st), "get state");
+    return VMP_OK;
+}
+
+vmp_status vmp_set_state(vmp_stream_t s, const vmp_state* x, const double* P) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    if (x) VMP_TRY(cudaMemcpyAsync(&s->f->x, x, sizeof(vmp_state), cudaMemcpyHostToDevice, s->st), "state");
+    if (P) VMP_TRY(cudaMemcpyAsync(s->f->P, P, sizeof(double) * 529, cudaMemcpyHostToDevice, s->st), "P");
+    VMP_TRY(cudaStreamSynchronize(s->st), "set state");
+    return VMP_OK;
+}
+
+vmp_status vmp_ieskf_predict(vmp_stream_t s, const double acc[3], const double gyro[3], double dt, const double* Q) {
+    if (!s || !acc || !gyro) return VMP_ERR_INVALID_ARG;
+    if (Q) VMP_TRY(cudaMemcpyAsync(s->f->Q, Q, sizeof(double) * 144, cudaMemcpyHostToDevice, s->st), "Q");
+    launch_ieskf_predict_once(s->f, acc, gyro, dt, s->st);
+    VMP_TRY(cudaGetLastError(), "predict");
+    VMP_TRY(cudaStreamSynchronize(s->st), "predict");
+    return VMP_OK;
+}
+
+vmp_status vmp_ieskf_update(vmp_stream_t s, const float* pts_l, int n, int* iters, int* effect_num) {
+    if (!s || n < 0 || (n > 0 && !pts_l)) return VMP_ERR_INVALID_ARG;
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
+    float* d_f = reinterpret_cast<float*>(s->s.bcov);
+    VMP_TRY(cudaMemcpyAsync(d_f, pts_l, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->st), "upload");
+    k_floats_to_points<<<152, 256, 0, s->st>>>(d_f, n, s->s.down);
+    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
+    launch_body_cov(s->s, n, s->cfg.ranging_cov, s->sin_deg, s->st);
+    launch_update_begin(s->f, s->st);
+    for (int it = 0; it < s->cfg.ieskf_max_iter; ++it)
+        launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 1);
+    launch_update_end(s->f, s->st);
+    vmp_status v = finish_result(s, n, nullptr);
+    if (v != VMP_OK) return v;
+    if (iters) *iters = s->h_res->iters;
+    if (effect_num) *effect_num = s->h_res->effect_num;
+    return VMP_OK;
+}
+
+vmp_status vmp_residual_reduce(vmp_stream_t s, const vmp_state* x, const double* P, const double* pts_l,
+                               const double* cov_l, int n, double* H, double* b, int* effect_num) {
+    if (!s || !x || !P || n < 0 || (n > 0 && (!pts_l || !cov_l)) || !H || !b) return VMP_ERR_INVALID_ARG;
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
+    VMP_TRY(cudaMemcpyAsync(&s->f->x, x, sizeof(vmp_state), cudaMemcpyHostToDevice, s->st), "state");
+    VMP_TRY(cudaMemcpyAsync(s->f->P, P, sizeof(double) * 529, cudaMemcpyHostToDevice, s->st), "P");
+    vmp_status v = stage_doubles(s, s->s.pl, pts_l, (size_t)n * 3);
+    if (v != VMP_OK) return v;
+    v = stage_doubles(s, s->s.covl, cov_l, (size_t)n * 9);
+    if (v != VMP_OK) return v;
+    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
+    k_reset_filter_iter<<<1, 32, 0, s->st>>>(s->f);
+    launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 0);
+    double* d_h = s->s.bcov;  // scratch
+    int* d_e = reinterpret_cast<int*>(s->s.bcov + 160);
+    k_read_hm<<<1, 256, 0, s->st>>>(s->f, d_h, d_h + 144, d_e);
+    VMP_TRY(cudaMemcpyAsync(H, d_h, sizeof(double) * 144, cudaMemcpyDeviceToHost, s->st), "H");
+    VMP_TRY(cudaMemcpyAsync(b, d_h + 144, sizeof(double) * 12, cudaMemcpyDeviceToHost, s->st), "b");
+    VMP_TRY(cudaMemcpyAsync(s->h_int, d_e, sizeof(int), cudaMemcpyDeviceToHost, s->st), "eff");
+    VMP_TRY(cudaStreamSynchronize(s->st), "residual");
+    if (effect_num) *effect_num = s->h_int[0];
+    return VMP_OK;
+}
+
+vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* imus, int n_imu, vmp_point* out) {
+    if (!s || !scan || !out || !imus || n_imu <= 0 || scan->n <= 0) return VMP_ERR_INVALID_ARG;
+    const int n = scan->n;
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "scan larger than max_scan_points");
+    if (n_imu > s->cfg.max_imu_per_scan) return fail(s, VMP_ERR_CAPACITY, "too many IMU samples");
+    vmp_status v = upload_scan(s, scan->points, n, false);
+    if (v != VMP_OK) return v;
+    v = upload_imus(s, imus, n_imu, false);
+    if (v != VMP_OK) return v;
+    launch_time_sort(s->s, n, s->ss, s->st);
+    launch_predict_chain(s->f, s->s, n_imu, scan->t_start, scan->t_end, s->st);
+    launch_undistort(s->f, s->s, n, s->st);
+    VMP_TRY(cudaGetLastError(), "undistort");
+    VMP_TRY(cudaMemcpyAsync(out, s->s.cloud, sizeof(vmp_point) * (size_t)n, cudaMemcpyDeviceToHost, s->st), "cloud");
+    VMP_TRY(cudaStreamSynchronize(s->st), "undistort");
+    return VMP_OK;
+}
+
+vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double leaf, vmp_point* out, int* n_out) {
+    if (!s || n < 0 || (n > 0 && (!pts || !out)) || !n_out) return VMP_ERR_INVALID_ARG;
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
+    if (!(leaf > 0)) return fail(s, VMP_ERR_INVALID_ARG, "leaf must be > 0");
+    VMP_TRY(cudaMemcpyAsync(s->s.cloud, pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyHostToDevice, s->st), "upload");
+    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
+    launch_downsample(s->s, n > 0 ? n : 1, leaf, s->ss, s->sc, s->st);
+    VMP_TRY(cudaMemcpyAsync(s->h_int, s->s.d_n_down, sizeof(int), cudaMemcpyDeviceToHost, s->st), "n");
+    VMP_TRY(cudaStreamSynchronize(s->st), "downsample");
+    const int m = s->h_int[0];
+    *n_out = m;
+    if (m > 0) {
+        VMP_TRY(cudaMemcpyAsync(out, s->s.down, sizeof(vmp_point) * (size_t)m, cudaMemcpyDeviceToHost, s->st), "down");
+        VMP_TRY(cudaStreamSynchronize(s->st), "downsample");
+    }
+    return VMP_OK;
+}
+
+// Valid flags of the persistent residual records (test hook for the match set).
+vmp_status vmp_residual_valid(vmp_stream_t s, unsigned char* valid, int n) {
+    if (!s || !valid || n < 0 || n > s->cfg.max_scan_points) return VMP_ERR_INVALID_ARG;
+    VMP_TRY(cudaMemcpyAsync(valid, s->s.rvalid, (size_t)n, cudaMemcpyDeviceToHost, s->st), "valid");
+    VMP_TRY(cudaStreamSynchronize(s->st), "valid");
+    return VMP_OK;
+}
+
+// The clouds of the last scan: kind 0 = undistorted (time-sorted) raw cloud,
+// kind 1 = downsampled cloud.
+vmp_status vmp_last_cloud(vmp_stream_t s, int kind, vmp_point* out, int max, int* n_out) {
+    if (!s || !n_out) return VMP_ERR_INVALID_ARG;
+    const int* d_n = kind == 0 ? s->s.d_n_raw : s->s.d_n_down;
+    VMP_TRY(cudaMemcpyAsync(s->h_int, d_n, sizeof(int), cudaMemcpyDeviceToHost, s->st), "n");
+    VMP_TRY(cudaStreamSynchronize(s->st), "n");
+    const int n = s->h_int[0];
+    *n_out = n;
+    if (out && max > 0) {
+        VMP_TRY(cudaMemcpyAsync(out, kind == 0 ? s->s.cloud : s->s.down, sizeof(vmp_point) * (size_t)std::min(n, max),
+                                cudaMemcpyDeviceToHost, s->st), "cloud");
+        VMP_TRY(cudaStreamSynchronize(s->st), "cloud");
+    }
+    return VMP_OK;
+}
+
+// Selects the merge resolution: 0 = parallel fixed point (default),
+// 1 = single-thread replay in point order (both exact).
+vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode) {
+    if (!s || mode < 0 || mode > 1) return VMP_ERR_INVALID_ARG;
+    s->ms.merge_mode = mode;
+    return VMP_OK;
+}
+int vmp_last_merge_rounds(vmp_stream_t s) { return s ? s->ms.merge_rounds : -1; }
+
+}  // extern "C"
