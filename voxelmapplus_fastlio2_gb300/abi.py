@@ -106,7 +106,7 @@ def default_config(**kw):
     c.ieskf_max_iter = 5
     c.ieskf_eps = 0.001
     c.max_scan_points = 262144
-    c.max_imu_per_scan = 4096
+    c.max_imu_per_scan = 1000
     for k, v in kw.items():
         if k in ("r_il", "p_il"):
             arr = getattr(c, k)

@@ -253,6 +253,8 @@ struct vmp_stream_s {
     long long last_evicted_total = 0;
 };
 
+static thread_local std::string g_create_error;
+
 static vmp_status fail(vmp_stream_t s, vmp_status code, const std::string& msg) {
     if (s) s->err = msg;
     return code;
@@ -330,7 +332,8 @@ void vmp_config_default(vmp_config* c) {
     c->max_imu_per_scan = 1000;
 }
 
-const char* vmp_last_error(vmp_stream_t s) { return s ? s->err.c_str() : "null handle"; }
+// With a null handle: the reason the calling thread's last vmp_create failed.
+const char* vmp_last_error(vmp_stream_t s) { return s ? s->err.c_str() : g_create_error.c_str(); }
 
 vmp_status vmp_destroy(vmp_stream_t s) {
     if (!s) return VMP_ERR_INVALID_ARG;
@@ -359,9 +362,14 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     if (cfg.max_scan_points <= 0) cfg.max_scan_points = 262144;
     std::string why;
     vmp_status v = validate(&cfg, why);
+    g_create_error = why;
     if (v != VMP_OK) return v;
     int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return VMP_ERR_CUDA;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        g_create_error = "no CUDA device visible (libvmp has no CPU fallback)";
+        return VMP_ERR_CUDA;
+    }
     vmp_stream_t s = new (std::nothrow) vmp_stream_s();
     if (!s) return VMP_ERR_OUT_OF_MEMORY;
     s->cfg = cfg;
@@ -370,6 +378,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     do {                                         \
         e = (expr);                              \
         if (e != cudaSuccess) {                  \
+            g_create_error = std::string("device allocation / setup failed: ") + cudaGetErrorString(e); \
             vmp_destroy(s);                      \
             return e == cudaErrorMemoryAllocation ? VMP_ERR_OUT_OF_MEMORY : VMP_ERR_CUDA; \
         }                                        \

@@ -116,7 +116,7 @@ class LIOBuilder:
         code = self.lib.vmp_create(C.byref(self.cfg), C.byref(h))
         if code != abi.VMP_OK:
             from ._lib import VmpError
-            raise VmpError(code, "vmp_create failed (no GPU, bad config or out of memory)")
+            raise VmpError(code, "vmp_create: " + (self.lib.vmp_last_error(None) or b"").decode())
         self.h = h
         self.map = VoxelMapView(self)
         self.kf = IESKFView(self)
