@@ -88,7 +88,7 @@ typedef struct vmp_config {
     double ieskf_eps;             /* 0.001 (ieskf.h:102) */
     /* device sizing; no reference counterpart */
     int max_scan_points;          /* raw points accepted per scan (default 262144) */
-    int max_imu_per_scan;         /* IMU samples accepted per scan (default 4096) */
+    int max_imu_per_scan;         /* IMU samples accepted per scan (default 1000, at most 1000) */
     int reserved[6];
 } vmp_config;
 
@@ -226,6 +226,46 @@ vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* im
 /* pcl::VoxelGrid leaf-centroid downsample at the given leaf size. */
 vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double leaf,
                           vmp_point* out, int* n_out);
+
+/* ---- measurement hooks (no reference counterpart) ----
+ * Per-phase device time of vmp_process, from CUDA events recorded on the
+ * stream's own CUDA stream.  Slot order: */
+enum {
+    VMP_PROF_UPLOAD = 0,        /* host->device copy of the scan and IMU samples */
+    VMP_PROF_TIME_SORT = 1,     /* stable radix sort of the points by time */
+    VMP_PROF_PREDICT = 2,       /* IMU predict chain (IESKF::predict per sample) */
+    VMP_PROF_UNDISTORT = 3,     /* per-point motion compensation */
+    VMP_PROF_DOWNSAMPLE = 4,    /* leaf-centroid downsample */
+    VMP_PROF_BODY_COV = 5,      /* calcBodyCov per downsampled point */
+    VMP_PROF_RESIDUAL = 6,      /* residual + reduction + IEKF step launches that ran an iteration */
+    VMP_PROF_RESIDUAL_IDLE = 7, /* residual launches after convergence (return at once) */
+    VMP_PROF_UPDATE_OTHER = 8,  /* P^-1 before, covariance update after the iterations */
+    VMP_PROF_MAP_BATCH = 9,     /* float world transform + point covariances */
+    VMP_PROF_MAP_GROUP = 10,    /* keys, hash insert, creation order, sort into voxel segments */
+    VMP_PROF_MAP_STATE = 11,    /* per-voxel pushPoint state machine + plane refits */
+    VMP_PROF_MAP_FINISH = 12,   /* merges, LRU queue, evictions */
+    VMP_PROF_RESULT = 13,       /* result gather + device->host copy */
+    VMP_PROF_SLOTS = 16
+};
+/* Enables (1) or disables (0) the profiler; either resets the totals. */
+vmp_status vmp_profile_enable(vmp_stream_t s, int on);
+/* Totals since enable: device ms, launches and points processed per slot
+ * (arrays of VMP_PROF_SLOTS; any may be NULL). */
+vmp_status vmp_profile_read(vmp_stream_t s, double* ms, long long* launches, long long* items);
+/* The cudaStream_t the stream's kernels run on. */
+void* vmp_cuda_stream(vmp_stream_t s);
+/* Bytes the stream copied host->device and device->host so far. */
+vmp_status vmp_io_bytes(vmp_stream_t s, long long* h2d, long long* d2h);
+/* Kernel launches issued by the library so far (all streams). */
+long long vmp_launch_count(void);
+/* Merge resolution: 0 parallel fixed point (default), 1 single-thread replay
+ * in point order; both exact.  Rounds of the last parallel resolution. */
+vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode);
+int vmp_last_merge_rounds(vmp_stream_t s);
+/* Test hooks: valid flags of the persistent residual records; the clouds of
+ * the last scan (kind 0 undistorted time-sorted cloud, 1 downsampled). */
+vmp_status vmp_residual_valid(vmp_stream_t s, unsigned char* valid, int n);
+vmp_status vmp_last_cloud(vmp_stream_t s, int kind, vmp_point* out, int max, int* n_out);
 
 #ifdef __cplusplus
 }

@@ -50,6 +50,11 @@ def _declare(lib):
         "vmp_residual_valid": ([vp, P(C.c_ubyte), C.c_int], st),
         "vmp_last_cloud": ([vp, C.c_int, P(abi.vmp_point), C.c_int, P(C.c_int)], st),
         "vmp_set_merge_mode": ([vp, C.c_int], st),
+        "vmp_profile_enable": ([vp, C.c_int], st),
+        "vmp_profile_read": ([vp, P(d), P(C.c_longlong), P(C.c_longlong)], st),
+        "vmp_cuda_stream": ([vp], vp),
+        "vmp_launch_count": ([], C.c_longlong),
+        "vmp_io_bytes": ([vp, P(C.c_longlong), P(C.c_longlong)], st),
         "vmp_last_merge_rounds": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():

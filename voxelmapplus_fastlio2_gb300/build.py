@@ -48,7 +48,7 @@ def build_synth():
     src = os.path.join(CSRC, "synth.cpp")
     if os.path.exists(out) and os.path.getmtime(out) > os.path.getmtime(src):
         return out
-    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INC, "-o", out, src])
+    _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-I" + INC, "-o", out, src])
     return out
 
 

@@ -7,12 +7,17 @@
 // --fmad=false, so the device rounds exactly like the reference's x86-64
 // build, which has no fused multiply-add.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "vmp.h"
 
 namespace vmp {
+
+// Host-side count of kernel launches issued by the library (all streams).
+extern std::atomic<long long> g_launch_count;
+#define VMP_NOTE_LAUNCH() ::vmp::g_launch_count.fetch_add(1, std::memory_order_relaxed)
 
 constexpr double kGravity = 9.81;          // kf::GRAVITY (ieskf.h:6)
 constexpr double kSophusEps = 1e-10;       // Sophus::Constants<double>::epsilon()

@@ -723,29 +723,30 @@ void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& c
     DState ext{};
     for (int i = 0; i < 9; ++i) ext.rot_ext[i] = cfg.r_il[i];
     for (int i = 0; i < 3; ++i) ext.pos_ext[i] = cfg.p_il[i];
-    k_imu_init<<<1, 32, 0, st>>>(f, imus, n, cfg.gravity_align, ext, t_end);
+    VMP_NOTE_LAUNCH(); k_imu_init<<<1, 32, 0, st>>>(f, imus, n, cfg.gravity_align, ext, t_end);
 }
 void launch_predict_chain(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st) {
-    k_predict_chain<<<1, 256, 0, st>>>(f, s.imus, n_imu, t_start, t_end, s.poses);
+    VMP_NOTE_LAUNCH(); k_predict_chain<<<1, 256, 0, st>>>(f, s.imus, n_imu, t_start, t_end, s.poses);
 }
 void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st) {
     int blocks = (n_max + 255) / 256;
     if (blocks > 1216) blocks = 1216;
     if (blocks < 1) blocks = 1;
-    k_undistort<<<blocks, 256, 0, st>>>(f, s.poses, s.cloud, s.d_n_raw);
+    VMP_NOTE_LAUNCH(); k_undistort<<<blocks, 256, 0, st>>>(f, s.poses, s.cloud, s.d_n_raw);
 }
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st) {
-    k_predict_once<<<1, 256, 0, st>>>(f, acc[0], acc[1], acc[2], gyro[0], gyro[1], gyro[2], dt);
+    VMP_NOTE_LAUNCH(); k_predict_once<<<1, 256, 0, st>>>(f, acc[0], acc[1], acc[2], gyro[0], gyro[1], gyro[2], dt);
 }
-void launch_update_begin(DFilter* f, cudaStream_t st) { k_update_begin<<<1, 256, 0, st>>>(f); }
+void launch_update_begin(DFilter* f, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_update_begin<<<1, 256, 0, st>>>(f); }
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step) {
     (void)n_max;
+    VMP_NOTE_LAUNCH();
     if (estimate_ext)
         k_residual<12><<<s.res_blocks, kResThreads, 0, st>>>(f, s, m, eps, do_step);
     else
         k_residual<6><<<s.res_blocks, kResThreads, 0, st>>>(f, s, m, eps, do_step);
 }
-void launch_update_end(DFilter* f, cudaStream_t st) { k_update_end<<<1, 256, 0, st>>>(f); }
+void launch_update_end(DFilter* f, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_update_end<<<1, 256, 0, st>>>(f); }
 
 }  // namespace vmp

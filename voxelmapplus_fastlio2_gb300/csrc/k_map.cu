@@ -632,53 +632,61 @@ __global__ void k_finalize_counters(DMap m, const int* d_n, const int* d_n_touch
 // Phase A: keys, hash insert, creation ranking, records, segments.
 void launch_map_phase_a(DMap& m, MapScratch& ms, const double* bpts, int n_max, cudaStream_t st) {
     const int g = grid_for_map(n_max);
-    k_lookup_insert<<<g, kMapThreads, 0, st>>>(m, bpts, ms.d_n, ms.slot, nullptr);
-    k_creator_flags<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.flag);
+    VMP_NOTE_LAUNCH(); k_lookup_insert<<<g, kMapThreads, 0, st>>>(m, bpts, ms.d_n, ms.slot, nullptr);
+    VMP_NOTE_LAUNCH(); k_creator_flags<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.flag);
     exclusive_scan_u32(ms.flag, ms.rank, ms.d_n, ms.d_n_new, ms.scan, st);
-    k_assign<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.rank, ms.d_n, ms.new_pos);
-    k_assign_counters<<<1, 32, 0, st>>>(m, ms.d_n_new);
+    VMP_NOTE_LAUNCH(); k_assign<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.rank, ms.d_n, ms.new_pos);
+    VMP_NOTE_LAUNCH(); k_assign_counters<<<1, 32, 0, st>>>(m, ms.d_n_new);
 }
 // Eviction walk (only when the batch can overflow the capacity).
 void launch_map_walk(DMap& m, MapScratch& ms, cudaStream_t st) {
-    k_evict_walk<<<1, 32, 0, st>>>(m, ms.new_pos, ms.victims);
+    VMP_NOTE_LAUNCH(); k_evict_walk<<<1, 32, 0, st>>>(m, ms.new_pos, ms.victims);
 }
 void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
-    k_rollback<<<grid_for_map(n_max), kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.d_n);
-    k_rollback_counters<<<1, 32, 0, st>>>(m);
+    VMP_NOTE_LAUNCH(); k_rollback<<<grid_for_map(n_max), kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.d_n);
+    VMP_NOTE_LAUNCH(); k_rollback_counters<<<1, 32, 0, st>>>(m);
 }
 // Segments are formed before the walk (the walk needs each touched record's
 // first touch).
 void launch_map_segments(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
     const int g = grid_for_map(n_max);
-    k_resolve<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.rec, ms.sk, ms.sv);
+    VMP_NOTE_LAUNCH(); k_resolve<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.rec, ms.sk, ms.sv);
     radix_sort_pairs(ms.sk, ms.sv, ms.d_n, 32, ms.sort, st);
-    k_seg_heads<<<g, kMapThreads, 0, st>>>(ms.sk, ms.d_n, ms.flag2);
+    VMP_NOTE_LAUNCH(); k_seg_heads<<<g, kMapThreads, 0, st>>>(ms.sk, ms.d_n, ms.flag2);
     exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_seg, ms.scan, st);
-    k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.last_touch, ms.d_n, 0u);
-    k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, kNoRec);
-    k_seg_bounds<<<g, kMapThreads, 0, st>>>(m, ms.sk, ms.sv, ms.flag2, ms.rank2, ms.d_n, ms.seg_start, ms.seg_end,
+    VMP_NOTE_LAUNCH(); k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.last_touch, ms.d_n, 0u);
+    VMP_NOTE_LAUNCH(); k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, kNoRec);
+    VMP_NOTE_LAUNCH(); k_seg_bounds<<<g, kMapThreads, 0, st>>>(m, ms.sk, ms.sv, ms.flag2, ms.rank2, ms.d_n, ms.seg_start, ms.seg_end,
                                             ms.seg_rec, ms.last_touch);
 }
-// Phase B: state machine, merges, LRU queue, evictions, counters.
-void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
-                        cudaStream_t st) {
-    const int g = grid_for_map(n_max);
+// Phase B1: the per-voxel pushPoint / addPoint state machine.
+void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
+                      cudaStream_t st) {
     int sg = (n_max + (kSegThreads / 32) - 1) / (kSegThreads / 32);
     if (sg > 152 * 16) sg = 152 * 16;
     if (sg < 1) sg = 1;
-    k_segments<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg, ms.sv, bpts, bcov,
-                                           ms.ev_rec, build ? 1 : 0);
+    VMP_NOTE_LAUNCH(); k_segments<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg,
+                                                              ms.sv, bpts, bcov, ms.ev_rec, build ? 1 : 0);
+}
+// Phase B2: merges, LRU queue, evictions, counters.
+void launch_map_finish(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st) {
+    const int g = grid_for_map(n_max);
     if (!build) {
-        k_ev_flags<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, ms.flag2);
+        VMP_NOTE_LAUNCH(); k_ev_flags<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, ms.flag2);
         exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_ev, ms.scan, st);
-        k_compact_idx<<<g, kMapThreads, 0, st>>>(ms.flag2, ms.rank2, ms.d_n, ms.ev_list);
+        VMP_NOTE_LAUNCH(); k_compact_idx<<<g, kMapThreads, 0, st>>>(ms.flag2, ms.rank2, ms.d_n, ms.ev_list);
         run_merge_events(m, ms, ms.merge, n_max, ms.merge_mode, &ms.merge_rounds, st);
     }
     exclusive_scan_u32(ms.last_touch, ms.rank2, ms.d_n, ms.d_n_touch, ms.scan, st);
-    k_queue_append<<<g, kMapThreads, 0, st>>>(m, ms.last_touch, ms.rank2, ms.rec, ms.d_n, ms.d_n_touch);
-    k_finalize<<<g, kMapThreads, 0, st>>>(m, ms.victims);
-    k_finalize_chunks<<<g, kMapThreads, 0, st>>>(m);
-    k_finalize_counters<<<1, 32, 0, st>>>(m, ms.d_n, ms.d_n_touch);
+    VMP_NOTE_LAUNCH(); k_queue_append<<<g, kMapThreads, 0, st>>>(m, ms.last_touch, ms.rank2, ms.rec, ms.d_n, ms.d_n_touch);
+    VMP_NOTE_LAUNCH(); k_finalize<<<g, kMapThreads, 0, st>>>(m, ms.victims);
+    VMP_NOTE_LAUNCH(); k_finalize_chunks<<<g, kMapThreads, 0, st>>>(m);
+    VMP_NOTE_LAUNCH(); k_finalize_counters<<<1, 32, 0, st>>>(m, ms.d_n, ms.d_n_touch);
+}
+void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
+                        cudaStream_t st) {
+    launch_map_state(m, ms, bpts, bcov, n_max, build, st);
+    launch_map_finish(m, ms, n_max, build, st);
 }
 
 // Rebuilds the hash table from the live records (drops tombstones).
@@ -704,8 +712,8 @@ __global__ void k_reinsert(DMap m) {
     if (blockIdx.x == 0 && threadIdx.x == 0) m.cnt->n_tomb = 0;
 }
 void launch_rehash(DMap& m, cudaStream_t st) {
-    k_clear_table<<<1216, 256, 0, st>>>(m);
-    k_reinsert<<<1216, 256, 0, st>>>(m);
+    VMP_NOTE_LAUNCH(); k_clear_table<<<1216, 256, 0, st>>>(m);
+    VMP_NOTE_LAUNCH(); k_reinsert<<<1216, 256, 0, st>>>(m);
 }
 
 // LRU queue compaction: keeps the live entries, in order, from q_head.
@@ -743,10 +751,10 @@ __global__ void k_q_scatter(DMap m, const uint32_t* tr, const uint64_t* ts, cons
 void launch_queue_compact(DMap& m, uint32_t* flag, uint32_t* rank, uint32_t* tr, uint64_t* ts, int* d_len,
                           int* d_live, int len_max, ScanScratch& sc, cudaStream_t st) {
     const int g = grid_for_map(len_max);
-    k_q_live<<<g, kMapThreads, 0, st>>>(m, flag, d_len);
+    VMP_NOTE_LAUNCH(); k_q_live<<<g, kMapThreads, 0, st>>>(m, flag, d_len);
     exclusive_scan_u32(flag, rank, d_len, d_live, sc, st);
-    k_q_gather<<<g, kMapThreads, 0, st>>>(m, flag, rank, d_len, tr, ts);
-    k_q_scatter<<<g, kMapThreads, 0, st>>>(m, tr, ts, d_live);
+    VMP_NOTE_LAUNCH(); k_q_gather<<<g, kMapThreads, 0, st>>>(m, flag, rank, d_len, tr, ts);
+    VMP_NOTE_LAUNCH(); k_q_scatter<<<g, kMapThreads, 0, st>>>(m, tr, ts, d_live);
 }
 
 __global__ void k_map_index(DMap m, const double* pts, int n, int64_t* keys) {
@@ -757,7 +765,7 @@ __global__ void k_map_index(DMap m, const double* pts, int n, int64_t* keys) {
     }
 }
 void launch_map_index(const DMap& m, const double* pts, int n, int64_t* keys, cudaStream_t st) {
-    k_map_index<<<grid_for_map(n), kMapThreads, 0, st>>>(m, pts, n, keys);
+    VMP_NOTE_LAUNCH(); k_map_index<<<grid_for_map(n), kMapThreads, 0, st>>>(m, pts, n, keys);
 }
 
 __global__ void k_map_reset(DMap m) {
@@ -790,7 +798,7 @@ __global__ void k_map_reset(DMap m) {
         c->n_tomb = 0;
     }
 }
-void launch_map_reset(DMap& m, cudaStream_t st) { k_map_reset<<<1216, 256, 0, st>>>(m); }
+void launch_map_reset(DMap& m, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_map_reset<<<1216, 256, 0, st>>>(m); }
 
 cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
     ms.max_batch = max_batch;
@@ -803,6 +811,7 @@ cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
     if ((e = merge_scratch_alloc(&ms.merge, max_batch, rec_pool)) != cudaSuccess) return e;
     ms.merge_mode = 0;
     ms.merge_rounds = 0;
+    ms.merge_d2h = 0;
     if ((e = cudaMalloc(&ms.d_scratch_int, sizeof(int) * 32)) != cudaSuccess) return e;
     ms.d_n = ms.d_scratch_int;
     ms.d_n_new = ms.d_scratch_int + 1;

@@ -242,7 +242,7 @@ __global__ void k_merge_apply(DMap m, MergeScratch ms, int cur) {
 __global__ void k_flag_merge_fallback(DMap m) {
     if (threadIdx.x == 0 && blockIdx.x == 0) m.cnt->changed = 1;  // informational: the replay path ran
 }
-static void set_error_host_flag(DMap& m, cudaStream_t st) { k_flag_merge_fallback<<<1, 32, 0, st>>>(m); }
+static void set_error_host_flag(DMap& m, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_flag_merge_fallback<<<1, 32, 0, st>>>(m); }
 
 static MergeScratch* g_unused = nullptr;
 
@@ -285,23 +285,24 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     if (grid < 1) grid = 1;
     if (rounds_out) *rounds_out = 0;
     if (mode == 1) {  // sequential replay only
-        k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev);
+        VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev);
         return cudaGetLastError();
     }
     cudaError_t e;
-    k_merge_begin<<<1, 32, 0, st>>>(g);
+    VMP_NOTE_LAUNCH(); k_merge_begin<<<1, 32, 0, st>>>(g);
     // clear both logs (left over from the previous batch)
     for (int b = 0; b < 2; ++b) {
-        k_merge_clear<<<grid, kMergeThreads, 0, st>>>(g, b);
-        k_merge_reset_count<<<1, 32, 0, st>>>(g, b);
+        VMP_NOTE_LAUNCH(); k_merge_clear<<<grid, kMergeThreads, 0, st>>>(g, b);
+        VMP_NOTE_LAUNCH(); k_merge_reset_count<<<1, 32, 0, st>>>(g, b);
     }
     int cur = 0;
     bool converged = false;
     for (int r = 0; r < kMaxRounds; ++r) {
-        k_merge_clear<<<grid, kMergeThreads, 0, st>>>(g, cur);
-        k_merge_reset_count<<<1, 32, 0, st>>>(g, cur);
-        k_merge_round<<<grid, kMergeThreads, 0, st>>>(m, g, ms.ev_list, ms.ev_rec, ms.d_n_ev, cur, r == 0 ? 1 : 0);
+        VMP_NOTE_LAUNCH(); k_merge_clear<<<grid, kMergeThreads, 0, st>>>(g, cur);
+        VMP_NOTE_LAUNCH(); k_merge_reset_count<<<1, 32, 0, st>>>(g, cur);
+        VMP_NOTE_LAUNCH(); k_merge_round<<<grid, kMergeThreads, 0, st>>>(m, g, ms.ev_list, ms.ev_rec, ms.d_n_ev, cur, r == 0 ? 1 : 0);
         if ((e = cudaMemcpyAsync(g.h_ctl, g.ctl, sizeof(MergeCtl), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+        ms.merge_d2h += (long long)sizeof(MergeCtl);
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
         if (rounds_out) *rounds_out = r + 1;
         if (g.h_ctl->overflow) break;
@@ -310,9 +311,9 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
         cur ^= 1;
     }
     if (converged) {
-        k_merge_apply<<<grid, kMergeThreads, 0, st>>>(m, g, cur);
+        VMP_NOTE_LAUNCH(); k_merge_apply<<<grid, kMergeThreads, 0, st>>>(m, g, cur);
     } else {
-        k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev);
+        VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev);
         set_error_host_flag(m, st);
     }
     return cudaGetLastError();

@@ -43,9 +43,9 @@ static int grid_for(int n_max) {
 
 void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st) {
     int g = grid_for(n_max);
-    k_time_keys<<<g, kPtThreads, 0, st>>>(s.raw, s.d_n_raw, s.sort_k, s.sort_v);
+    VMP_NOTE_LAUNCH(); k_time_keys<<<g, kPtThreads, 0, st>>>(s.raw, s.d_n_raw, s.sort_k, s.sort_v);
     radix_sort_pairs(s.sort_k, s.sort_v, s.d_n_raw, 32, ss, st);
-    k_gather4<<<g, kPtThreads, 0, st>>>(s.raw, s.sort_v, s.d_n_raw, s.cloud);
+    VMP_NOTE_LAUNCH(); k_gather4<<<g, kPtThreads, 0, st>>>(s.raw, s.sort_v, s.d_n_raw, s.cloud);
 }
 
 // ---------------------------------------------------------------- downsample
@@ -155,15 +155,15 @@ __global__ void k_centroid(const float4* __restrict__ c, const uint32_t* __restr
 
 void launch_downsample(DScan& s, int n_max, double leaf, SortScratch& ss, ScanScratch& sc, cudaStream_t st) {
     int g = grid_for(n_max);
-    k_minmax_partial<<<kMinMaxBlocks, kPtThreads, 0, st>>>(s.cloud, s.d_n_raw, s.blk_minmax);
-    k_ds_params<<<1, 32, 0, st>>>(s.blk_minmax, kMinMaxBlocks, (float)leaf, s.ds_params, s.d_n_raw);
-    k_leaf_idx<<<g, kPtThreads, 0, st>>>(s.cloud, s.d_n_raw, s.ds_params, s.sort_k, s.sort_v);
+    VMP_NOTE_LAUNCH(); k_minmax_partial<<<kMinMaxBlocks, kPtThreads, 0, st>>>(s.cloud, s.d_n_raw, s.blk_minmax);
+    VMP_NOTE_LAUNCH(); k_ds_params<<<1, 32, 0, st>>>(s.blk_minmax, kMinMaxBlocks, (float)leaf, s.ds_params, s.d_n_raw);
+    VMP_NOTE_LAUNCH(); k_leaf_idx<<<g, kPtThreads, 0, st>>>(s.cloud, s.d_n_raw, s.ds_params, s.sort_k, s.sort_v);
     radix_sort_pairs(s.sort_k, s.sort_v, s.d_n_raw, 32, ss, st);
-    k_run_heads<<<g, kPtThreads, 0, st>>>(s.sort_k, s.d_n_raw, s.ds_params, s.flags);
+    VMP_NOTE_LAUNCH(); k_run_heads<<<g, kPtThreads, 0, st>>>(s.sort_k, s.d_n_raw, s.ds_params, s.flags);
     int* d_runs = s.ds_params + 12;
     exclusive_scan_u32(s.flags, s.scan_out, s.d_n_raw, d_runs, sc, st);
-    k_run_starts<<<g, kPtThreads, 0, st>>>(s.flags, s.scan_out, s.d_n_raw, s.ds_params, s.run_start, d_runs);
-    k_centroid<<<g, kPtThreads, 0, st>>>(s.cloud, s.sort_v, s.run_start, d_runs, s.ds_params, s.d_n_raw, s.down,
+    VMP_NOTE_LAUNCH(); k_run_starts<<<g, kPtThreads, 0, st>>>(s.flags, s.scan_out, s.d_n_raw, s.ds_params, s.run_start, d_runs);
+    VMP_NOTE_LAUNCH(); k_centroid<<<g, kPtThreads, 0, st>>>(s.cloud, s.sort_v, s.run_start, d_runs, s.ds_params, s.d_n_raw, s.down,
                                          s.d_n_down);
 }
 
@@ -173,7 +173,7 @@ __global__ void k_copy_down(const float4* __restrict__ c, const int* d_n, float4
     if (blockIdx.x == 0 && threadIdx.x == 0) *d_n_down = n;
 }
 void launch_copy_down(DScan& s, int n_max, cudaStream_t st) {
-    k_copy_down<<<grid_for(n_max), kPtThreads, 0, st>>>(s.cloud, s.d_n_raw, s.down, s.d_n_down);
+    VMP_NOTE_LAUNCH(); k_copy_down<<<grid_for(n_max), kPtThreads, 0, st>>>(s.cloud, s.d_n_raw, s.down, s.d_n_down);
 }
 
 // ---------------------------------------------------------------- calcBodyCov
@@ -225,7 +225,7 @@ __global__ void k_body_cov(const float4* __restrict__ down, const int* d_n, doub
     }
 }
 void launch_body_cov(DScan& s, int n_max, double range_inc, double sin_deg, cudaStream_t st) {
-    k_body_cov<<<grid_for(n_max), kPtThreads, 0, st>>>(s.down, s.d_n_down, range_inc, sin_deg, s.pl, s.covl);
+    VMP_NOTE_LAUNCH(); k_body_cov<<<grid_for(n_max), kPtThreads, 0, st>>>(s.down, s.d_n_down, range_inc, sin_deg, s.pl, s.covl);
 }
 
 // ---------------------------------------------------------------- map batch
@@ -278,6 +278,7 @@ __global__ void k_map_batch(const DFilter* __restrict__ f, const float4* __restr
 
 void launch_map_batch(DFilter* f, DScan& s, int n_max, bool from_full_cloud, double range_inc, double sin_deg,
                       cudaStream_t st) {
+    VMP_NOTE_LAUNCH();
     if (from_full_cloud)
         k_map_batch<<<grid_for(n_max), kPtThreads, 0, st>>>(f, s.cloud, s.d_n_raw, nullptr, nullptr, 1, range_inc,
                                                              sin_deg, s.bpts, s.bcov, s.d_n_batch);

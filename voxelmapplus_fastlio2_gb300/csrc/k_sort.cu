@@ -6,9 +6,12 @@
 // walks them 32 at a time in order, so the rank of an element is
 // (earlier warps' count of its digit) + (its warp's running count) + (its
 // rank among equal lanes of the same 32-element step) -- input order is kept.
+#include "common.cuh"
 #include "prims.cuh"
 
 namespace vmp {
+
+std::atomic<long long> g_launch_count{0};
 
 __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __restrict__ d_n, int shift,
                              uint32_t* __restrict__ hist, int blocks) {
@@ -133,9 +136,9 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, 
     uint32_t *ka = keys, *va = vals, *kb = s.k_alt, *vb = s.v_alt;
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
-        k_radix_hist<<<s.blocks, kSortThreads, 0, st>>>(ka, d_n, shift, s.hist, s.blocks);
-        k_radix_scan_hist<<<1, 1024, 0, st>>>(s.hist, 256 * s.blocks);
-        k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.blocks);
+        VMP_NOTE_LAUNCH(); k_radix_hist<<<s.blocks, kSortThreads, 0, st>>>(ka, d_n, shift, s.hist, s.blocks);
+        VMP_NOTE_LAUNCH(); k_radix_scan_hist<<<1, 1024, 0, st>>>(s.hist, 256 * s.blocks);
+        VMP_NOTE_LAUNCH(); k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.blocks);
         uint32_t* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
     }
@@ -234,9 +237,9 @@ void scan_scratch_free(ScanScratch& s) {
 
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, const int* d_n, int* d_total, ScanScratch& s,
                         cudaStream_t st) {
-    k_scan_tiles<<<s.blocks, kScanThreads, 0, st>>>(in, out, d_n, s.block_sums);
-    k_scan_top<<<1, 1024, 0, st>>>(s.block_sums, s.blocks, d_n, d_total);
-    k_scan_add<<<s.blocks, kScanThreads, 0, st>>>(out, d_n, s.block_sums);
+    VMP_NOTE_LAUNCH(); k_scan_tiles<<<s.blocks, kScanThreads, 0, st>>>(in, out, d_n, s.block_sums);
+    VMP_NOTE_LAUNCH(); k_scan_top<<<1, 1024, 0, st>>>(s.block_sums, s.blocks, d_n, d_total);
+    VMP_NOTE_LAUNCH(); k_scan_add<<<s.blocks, kScanThreads, 0, st>>>(out, d_n, s.block_sums);
 }
 
 }  // namespace vmp

@@ -87,6 +87,7 @@ struct MapScratch {
     void* merge;          // MergeScratch (k_merge.cu)
     int merge_mode;
     int merge_rounds;
+    long long merge_d2h;  // bytes read back by the merge rounds (cumulative)
     int* d_n;             // batch size
     int* d_n_new;
     int* d_n_seg;
@@ -108,6 +109,9 @@ void launch_map_walk(DMap& m, MapScratch& ms, cudaStream_t st);
 void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st);
 void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
                         cudaStream_t st);
+void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
+                      cudaStream_t st);
+void launch_map_finish(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st);
 void launch_rehash(DMap& m, cudaStream_t st);
 void launch_queue_compact(DMap& m, uint32_t* flag, uint32_t* rank, uint32_t* tr, uint64_t* ts, int* d_len,
                           int* d_live, int len_max, ScanScratch& sc, cudaStream_t st);

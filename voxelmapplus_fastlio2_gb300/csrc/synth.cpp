@@ -259,12 +259,26 @@ int vmp_synth_package(vmp_synth* s, int k, vmp_point* pts, int max_points, doubl
     double ts = s->t0 + k / c.scan_hz;
     double period = 1.0 / c.scan_hz;
     int nrays = c.points_per_scan;
-    std::mt19937_64 r(c.seed * 1315423911ULL + (unsigned long long)k * 2654435761ULL + 17);
-    std::normal_distribution<double> N01(0.0, 1.0);
-    std::uniform_real_distribution<double> U(0.0, 1.0);
-    std::vector<vmp_point> out;
-    out.reserve(nrays);
+    // per-ray counter-based random numbers: identical output for any thread count
+    const unsigned long long scan_key = c.seed * 1315423911ULL + (unsigned long long)k * 2654435761ULL + 17;
+    std::vector<vmp_point> rays((size_t)nrays);
+    std::vector<unsigned char> keep((size_t)nrays, 0);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (int j = 0; j < nrays; ++j) {
+        unsigned long long ctr = scan_key ^ (0x9E3779B97F4A7C15ULL * (unsigned long long)(j + 1));
+        auto uni = [&ctr]() {
+            unsigned long long z = (ctr += 0x9E3779B97F4A7C15ULL);
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+            z ^= z >> 31;
+            return ((z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        };
+        auto gauss = [&uni]() {
+            double u1 = uni(), u2 = uni();
+            return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979 * u2);
+        };
         double dt = j * (period / nrays);
         double t = ts + dt;
         // beam direction in the sensor frame
@@ -298,31 +312,34 @@ int vmp_synth_package(vmp_synth* s, int k, vmp_point* pts, int max_points, doubl
         }
         double range;
         V pl;
-        if (c.clutter_frac > 0 && !s->scene.clutter.empty() && U(r) < c.clutter_frac) {
+        if (c.clutter_frac > 0 && !s->scene.clutter.empty() && uni() < c.clutter_frac) {
             // non-planar clutter: a random point inside a random clutter volume
-            const Box& b = s->scene.clutter[(size_t)(U(r) * s->scene.clutter.size()) % s->scene.clutter.size()];
-            V q{b.c.x + (2 * U(r) - 1) * b.h.x, b.c.y + (2 * U(r) - 1) * b.h.y, b.c.z + (2 * U(r) - 1) * b.h.z};
+            const Box& b = s->scene.clutter[(size_t)(uni() * s->scene.clutter.size()) % s->scene.clutter.size()];
+            V q{b.c.x + (2 * uni() - 1) * b.h.x, b.c.y + (2 * uni() - 1) * b.h.y, b.c.z + (2 * uni() - 1) * b.h.z};
             pl = rtmul(R, sub(q, p));
             range = std::sqrt(dotv(pl, pl));
         } else {
             if (!hit) continue;
-            range = best + c.range_sigma * N01(r);
+            range = best + c.range_sigma * gauss();
             pl = mul(d, range);
         }
         if (range < c.min_range || range > c.max_range) continue;
         vmp_point q;
         q.x = (float)pl.x; q.y = (float)pl.y; q.z = (float)pl.z;
         q.t_ms = (float)(dt * 1000.0);
-        out.push_back(q);
+        rays[(size_t)j] = q;
+        keep[(size_t)j] = 1;
     }
+    std::vector<vmp_point> out;
+    out.reserve((size_t)nrays);
+    for (int j = 0; j < nrays; ++j)
+        if (keep[(size_t)j]) out.push_back(rays[(size_t)j]);
     int n = std::min((int)out.size(), max_points);
     if (n > 0) std::memcpy(pts, out.data(), sizeof(vmp_point) * n);
     *t_start = ts;
     *t_end = ts + (n > 0 ? (double)pts[n - 1].t_ms / double(1000.0) : 0.0);
     // IMU samples with t < t_end not yet handed out
     int m = 0;
-    std::normal_distribution<double> Ng(0.0, c.gyro_noise), Na(0.0, c.acc_noise), Nb(0.0, c.bias_walk);
-    std::mt19937_64 ri(c.seed * 7919ULL + 12345);
     while (true) {
         double ti = imuTime(s, s->next_imu);
         if (ti >= *t_end) break;
@@ -347,7 +364,6 @@ int vmp_synth_package(vmp_synth* s, int k, vmp_point* pts, int max_points, doubl
         s->next_imu++;
     }
     *n_imu = m;
-    (void)Ng; (void)Na; (void)Nb; (void)ri;
     return n;
 }
 

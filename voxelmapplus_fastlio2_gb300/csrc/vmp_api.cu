@@ -251,6 +251,62 @@ struct vmp_stream_s {
     std::vector<void*> allocs;
     bool broken = false;
     long long last_evicted_total = 0;
+    // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
+    // the stream's own CUDA stream, resolved after the call's final sync
+    struct ProfRec { int slot; int items_kind; cudaEvent_t a, b; };
+    long long io_h2d = 0, io_d2h = 0;  // bytes copied host<->device by the library
+    bool prof_on = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<ProfRec> prof_pending;
+    cudaEvent_t prof_open = nullptr;
+    double prof_ms[VMP_PROF_SLOTS] = {};
+    long long prof_launches[VMP_PROF_SLOTS] = {};
+    long long prof_items[VMP_PROF_SLOTS] = {};
+    int cur_batch_kind = 1;
+
+    cudaEvent_t ev() {
+        if (ev_used == ev_pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev_pool.push_back(e);
+        }
+        return ev_pool[ev_used++];
+    }
+    void pbeg() {
+        if (!prof_on) return;
+        prof_open = ev();
+        cudaEventRecord(prof_open, st);
+    }
+    // items_kind: 0 raw points, 1 downsampled points, 2 map batch points, -1 none
+    void pend(int slot, int items_kind) {
+        if (!prof_on || !prof_open) return;
+        cudaEvent_t b = ev();
+        cudaEventRecord(b, st);
+        prof_pending.push_back(ProfRec{slot, items_kind, prof_open, b});
+        prof_open = nullptr;
+    }
+    // after the stream is synchronised
+    void pflush(int iters, int n_raw, int n_down, int n_batch) {
+        if (!prof_on) { prof_pending.clear(); ev_used = 0; return; }
+        int res_seen = 0;
+        for (const ProfRec& r : prof_pending) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) { cudaGetLastError(); continue; }
+            int slot = r.slot;
+            if (slot == VMP_PROF_RESIDUAL) {
+                if (res_seen >= iters) slot = VMP_PROF_RESIDUAL_IDLE;
+                ++res_seen;
+            }
+            prof_ms[slot] += ms;
+            prof_launches[slot] += 1;
+            long long it = r.items_kind == 0 ? n_raw : r.items_kind == 1 ? n_down : r.items_kind == 2 ? n_batch : 0;
+            if (slot == VMP_PROF_RESIDUAL_IDLE) it = 0;
+            prof_items[slot] += it;
+        }
+        prof_pending.clear();
+        ev_used = 0;
+    }
 };
 
 static thread_local std::string g_create_error;
@@ -338,6 +394,7 @@ const char* vmp_last_error(vmp_stream_t s) { return s ? s->err.c_str() : g_creat
 vmp_status vmp_destroy(vmp_stream_t s) {
     if (!s) return VMP_ERR_INVALID_ARG;
     if (s->st) cudaStreamSynchronize(s->st);
+    for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     for (void* p : s->allocs) cudaFree(p);
     map_scratch_free(s->ms);
     sort_scratch_free(s->ss);
@@ -513,6 +570,7 @@ static bool is_pinned_or_device(const void* p) {
 
 static vmp_status read_counters(vmp_stream_t s) {
     VMP_TRY(cudaMemcpyAsync(s->h_cnt, s->cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s->st), "read counters");
+    s->io_d2h += (long long)sizeof(Counters);
     VMP_TRY(cudaStreamSynchronize(s->st), "sync");
     s->h_size = s->h_cnt->size;
     s->h_qlen = s->h_cnt->q_tail - s->h_cnt->q_head;
@@ -530,7 +588,7 @@ static void map_maintenance(vmp_stream_t s) {
         // queue length is read on the device
         int* d_len = s->qc_ints;
         int* d_live = s->qc_ints + 1;
-        k_set_int<<<1, 32, 0, s->st>>>(d_len, (int)s->h_qlen);
+        VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(d_len, (int)s->h_qlen);
         launch_queue_compact(m, s->qc_flag, s->qc_rank, s->qc_rec, s->qc_stamp, d_len, d_live,
                              (int)std::min<uint64_t>(m.q_cap, 0x7FFFFFF0ull), s->qsc, s->st);
         s->h_qlen = 0;  // refreshed at the next counter read
@@ -545,13 +603,21 @@ static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bc
     MapScratch& ms = s->ms;
     map_maintenance(s);
     const bool evict_possible = s->h_size + (long long)n_upper > m.capacity;
+    VMP_NOTE_LAUNCH();
     if (d_n_src) k_copy_int<<<1, 32, 0, s->st>>>(ms.d_n, d_n_src);
     else k_set_int<<<1, 32, 0, s->st>>>(ms.d_n, n_host);
     const int n_max = n_upper;
     if (!evict_possible) {
+        s->pbeg();
         launch_map_phase_a(m, ms, bpts, n_max, s->st);
         launch_map_segments(m, ms, n_max, s->st);
-        launch_map_phase_b(m, ms, bpts, bcov, n_max, build, s->st);
+        s->pend(VMP_PROF_MAP_GROUP, s->cur_batch_kind);
+        s->pbeg();
+        launch_map_state(m, ms, bpts, bcov, n_max, build, s->st);
+        s->pend(VMP_PROF_MAP_STATE, s->cur_batch_kind);
+        s->pbeg();
+        launch_map_finish(m, ms, n_max, build, s->st);
+        s->pend(VMP_PROF_MAP_FINISH, s->cur_batch_kind);
         VMP_TRY(cudaGetLastError(), "map update launch");
         s->h_size += n_upper;  // upper bound until the next counter read
         return VMP_OK;
@@ -560,9 +626,10 @@ static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bc
     int n = n_host;
     if (d_n_src) {
         VMP_TRY(cudaMemcpyAsync(s->h_int, d_n_src, sizeof(int), cudaMemcpyDeviceToHost, s->st), "read n");
+        s->io_d2h += (long long)sizeof(int);
         VMP_TRY(cudaStreamSynchronize(s->st), "sync");
         n = s->h_int[0];
-        k_set_int<<<1, 32, 0, s->st>>>(ms.d_n, n);
+        VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(ms.d_n, n);
     }
     if (n <= 0) return VMP_OK;
     launch_map_phase_a(m, ms, bpts, n, s->st);
@@ -588,6 +655,7 @@ static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bc
 }
 
 static vmp_status upload_scan(vmp_stream_t s, const vmp_point* pts, int n, bool device_ptr) {
+    if (!device_ptr) s->io_h2d += (long long)sizeof(vmp_point) * n;
     if (device_ptr) {
         VMP_TRY(cudaMemcpyAsync(s->s.raw, pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyDeviceToDevice, s->st), "scan copy");
     } else if (is_pinned_or_device(pts)) {
@@ -597,12 +665,13 @@ static vmp_status upload_scan(vmp_stream_t s, const vmp_point* pts, int n, bool 
         std::memcpy(s->h_pts, pts, sizeof(vmp_point) * (size_t)n);
         VMP_TRY(cudaMemcpyAsync(s->s.raw, s->h_pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyHostToDevice, s->st), "scan upload");
     }
-    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
+    VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
     return VMP_OK;
 }
 
 static vmp_status upload_imus(vmp_stream_t s, const vmp_imu* imus, int n, bool device_ptr) {
     if (n <= 0) return VMP_OK;
+    if (!device_ptr) s->io_h2d += (long long)sizeof(vmp_imu) * n;
     if (device_ptr) {
         VMP_TRY(cudaMemcpyAsync(s->s.imus, imus, sizeof(vmp_imu) * (size_t)n, cudaMemcpyDeviceToDevice, s->st), "imu copy");
     } else {
@@ -614,11 +683,15 @@ static vmp_status upload_imus(vmp_stream_t s, const vmp_imu* imus, int n, bool d
 }
 
 static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
-    k_gather_result<<<1, 256, 0, s->st>>>(s->f, s->s.d_n_down, s->cnt, s->d_res);
+    s->pbeg();
+    VMP_NOTE_LAUNCH(); k_gather_result<<<1, 256, 0, s->st>>>(s->f, s->s.d_n_down, s->cnt, s->d_res);
     VMP_TRY(cudaGetLastError(), "result launch");
     VMP_TRY(cudaMemcpyAsync(s->h_res, s->d_res, sizeof(DResult), cudaMemcpyDeviceToHost, s->st), "result copy");
+    s->io_d2h += (long long)sizeof(DResult);
+    s->pend(VMP_PROF_RESULT, -1);
     VMP_TRY(cudaStreamSynchronize(s->st), "scan");
     const DResult& r = *s->h_res;
+    s->pflush(r.iters, n_raw, r.n_down, r.n_down);
     s->h_size = r.cnt.size;
     s->h_qlen = r.cnt.q_tail - r.cnt.q_head;
     s->h_tomb = r.cnt.n_tomb;
@@ -638,7 +711,7 @@ static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
     s->last_evicted_total = r.cnt.evicted_total;
     if (r.cnt.error) {
         unsigned int e = r.cnt.error;
-        k_clear_error<<<1, 32, 0, s->st>>>(s->cnt);
+        VMP_NOTE_LAUNCH(); k_clear_error<<<1, 32, 0, s->st>>>(s->cnt);
         cudaStreamSynchronize(s->st);
         if (e & E_KEY_RANGE) return fail(s, VMP_ERR_KEY_RANGE, "a voxel index left the packed range [-2^20, 2^20)");
         if (e & E_HASH_FULL) return fail(s, VMP_ERR_HASH_FULL, "voxel hash table full");
@@ -678,34 +751,59 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
             s->imu_cache.clear();
             s->lio_status = VMP_MAP_INIT;
         }
-        k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
+        VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
         return finish_result(s, n, out);
     }
+    s->pbeg();
     vmp_status v = upload_scan(s, pts, n, device_ptrs);
     if (v != VMP_OK) return v;
     v = upload_imus(s, imus, n_imu, device_ptrs);
     if (v != VMP_OK) return v;
+    s->pend(VMP_PROF_UPLOAD, 0);
+    s->pbeg();
     launch_time_sort(s->s, n, s->ss, st);
+    s->pend(VMP_PROF_TIME_SORT, 0);
+    s->pbeg();
     launch_predict_chain(s->f, s->s, n_imu, t_start, t_end, st);
+    s->pend(VMP_PROF_PREDICT, -1);
+    s->pbeg();
     launch_undistort(s->f, s->s, n, st);
+    s->pend(VMP_PROF_UNDISTORT, 0);
     if (s->lio_status == VMP_MAP_INIT) {
+        s->pbeg();
         launch_map_batch(s->f, s->s, n, true, cfg.ranging_cov, s->sin_deg, st);
-        k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
+        s->pend(VMP_PROF_MAP_BATCH, 0);
+        VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
         VMP_TRY(cudaGetLastError(), "map init launch");
+        s->cur_batch_kind = 0;
         v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, n, true);
         if (v != VMP_OK) return v;
         s->lio_status = VMP_LIO_MAPPING;
         return finish_result(s, n, out);
     }
+    s->pbeg();
     if (cfg.scan_resolution > 0.0) launch_downsample(s->s, n, cfg.scan_resolution, s->ss, s->sc, st);
     else launch_copy_down(s->s, n, st);
+    s->pend(VMP_PROF_DOWNSAMPLE, 0);
+    s->pbeg();
     launch_body_cov(s->s, n, cfg.ranging_cov, s->sin_deg, st);
+    s->pend(VMP_PROF_BODY_COV, 1);
+    s->pbeg();
     launch_update_begin(s->f, st);
-    for (int it = 0; it < cfg.ieskf_max_iter; ++it)
+    s->pend(VMP_PROF_UPDATE_OTHER, -1);
+    for (int it = 0; it < cfg.ieskf_max_iter; ++it) {
+        s->pbeg();
         launch_residual_iter(s->f, s->s, s->m, n, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+        s->pend(VMP_PROF_RESIDUAL, 1);
+    }
+    s->pbeg();
     launch_update_end(s->f, st);
+    s->pend(VMP_PROF_UPDATE_OTHER, -1);
+    s->pbeg();
     launch_map_batch(s->f, s->s, n, false, cfg.ranging_cov, s->sin_deg, st);
+    s->pend(VMP_PROF_MAP_BATCH, 1);
     VMP_TRY(cudaGetLastError(), "scan launch");
+    s->cur_batch_kind = 1;
     v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, n, false);
     if (v != VMP_OK) return v;
     return finish_result(s, n, out);
@@ -758,7 +856,7 @@ static vmp_status map_component(vmp_stream_t s, const double* pts, const double*
     if (v != VMP_OK) return v;
     v = map_apply(s, s->s.bpts, s->s.bcov, nullptr, n, n, build);
     if (v != VMP_OK) return v;
-    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, 0);
+    VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, 0);
     return finish_result(s, n, nullptr);
 }
 
@@ -793,7 +891,7 @@ static vmp_status export_all(vmp_stream_t s, std::vector<vmp_voxel>& out) {
     VMP_TRY(cudaMalloc(&d, sizeof(vmp_voxel) * (size_t)n), "export alloc");
     VMP_TRY(cudaMalloc(&d_count, sizeof(int)), "export alloc");
     cudaMemsetAsync(d_count, 0, sizeof(int), s->st);
-    k_export<<<1216, 256, 0, s->st>>>(s->m, d, d_count, (int)n);
+    VMP_NOTE_LAUNCH(); k_export<<<1216, 256, 0, s->st>>>(s->m, d, d_count, (int)n);
     cudaMemcpyAsync(out.data(), d, sizeof(vmp_voxel) * (size_t)n, cudaMemcpyDeviceToHost, s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);
     cudaFree(d);
@@ -843,7 +941,7 @@ vmp_status vmp_map_export_points(vmp_stream_t s, double* pts, double* cov, long 
     VMP_TRY(cudaMalloc(&d_c, sizeof(double) * 9 * (size_t)total), "alloc");
     cudaMemcpyAsync(d_recs, recs.data(), sizeof(int) * recs.size(), cudaMemcpyHostToDevice, s->st);
     cudaMemcpyAsync(d_offs, offs.data(), sizeof(long long) * offs.size(), cudaMemcpyHostToDevice, s->st);
-    k_export_points<<<1216, 128, 0, s->st>>>(s->m, d_recs, d_offs, (int)recs.size(), d_p, d_c);
+    VMP_NOTE_LAUNCH(); k_export_points<<<1216, 128, 0, s->st>>>(s->m, d_recs, d_offs, (int)recs.size(), d_p, d_c);
     cudaMemcpyAsync(pts, d_p, sizeof(double) * 3 * (size_t)total, cudaMemcpyDeviceToHost, s->st);
     cudaMemcpyAsync(cov, d_c, sizeof(double) * 9 * (size_t)total, cudaMemcpyDeviceToHost, s->st);
     cudaError_t e = cudaStreamSynchronize(s->st);
@@ -879,14 +977,14 @@ vmp_status vmp_map_import(vmp_stream_t s, const vmp_voxel* vox, long long n, con
             cudaMemcpyAsync(d_c, cov, sizeof(double) * 9 * (size_t)total, cudaMemcpyHostToDevice, s->st);
         }
         const unsigned long long stamp_top = (unsigned long long)n + 1;
-        k_set_int<<<1, 32, 0, s->st>>>(&s->cnt->chunk_freed_top, 0);
-        k_import<<<1216, 128, 0, s->st>>>(s->m, d_v, (int)n, d_o, d_p, d_c, stamp_top);
-        k_import_counters<<<1, 32, 0, s->st>>>(s->m, (int)n, group_counter, stamp_top);
+        VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(&s->cnt->chunk_freed_top, 0);
+        VMP_NOTE_LAUNCH(); k_import<<<1216, 128, 0, s->st>>>(s->m, d_v, (int)n, d_o, d_p, d_c, stamp_top);
+        VMP_NOTE_LAUNCH(); k_import_counters<<<1, 32, 0, s->st>>>(s->m, (int)n, group_counter, stamp_top);
         cudaError_t e = cudaStreamSynchronize(s->st);
         cudaFree(d_v); cudaFree(d_o); cudaFree(d_p); cudaFree(d_c);
         if (e != cudaSuccess) return cuda_fail(s, e, "import");
     } else {
-        k_import_counters<<<1, 32, 0, s->st>>>(s->m, 0, group_counter, 1ull);
+        VMP_NOTE_LAUNCH(); k_import_counters<<<1, 32, 0, s->st>>>(s->m, 0, group_counter, 1ull);
     }
     return read_counters(s);
 }
@@ -921,8 +1019,8 @@ vmp_status vmp_ieskf_update(vmp_stream_t s, const float* pts_l, int n, int* iter
     if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
     float* d_f = reinterpret_cast<float*>(s->s.bcov);
     VMP_TRY(cudaMemcpyAsync(d_f, pts_l, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->st), "upload");
-    k_floats_to_points<<<152, 256, 0, s->st>>>(d_f, n, s->s.down);
-    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
+    VMP_NOTE_LAUNCH(); k_floats_to_points<<<152, 256, 0, s->st>>>(d_f, n, s->s.down);
+    VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
     launch_body_cov(s->s, n, s->cfg.ranging_cov, s->sin_deg, s->st);
     launch_update_begin(s->f, s->st);
     for (int it = 0; it < s->cfg.ieskf_max_iter; ++it)
@@ -945,12 +1043,12 @@ vmp_status vmp_residual_reduce(vmp_stream_t s, const vmp_state* x, const double*
     if (v != VMP_OK) return v;
     v = stage_doubles(s, s->s.covl, cov_l, (size_t)n * 9);
     if (v != VMP_OK) return v;
-    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
-    k_reset_filter_iter<<<1, 32, 0, s->st>>>(s->f);
+    VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
+    VMP_NOTE_LAUNCH(); k_reset_filter_iter<<<1, 32, 0, s->st>>>(s->f);
     launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 0);
     double* d_h = s->s.bcov;  // scratch
     int* d_e = reinterpret_cast<int*>(s->s.bcov + 160);
-    k_read_hm<<<1, 256, 0, s->st>>>(s->f, d_h, d_h + 144, d_e);
+    VMP_NOTE_LAUNCH(); k_read_hm<<<1, 256, 0, s->st>>>(s->f, d_h, d_h + 144, d_e);
     VMP_TRY(cudaMemcpyAsync(H, d_h, sizeof(double) * 144, cudaMemcpyDeviceToHost, s->st), "H");
     VMP_TRY(cudaMemcpyAsync(b, d_h + 144, sizeof(double) * 12, cudaMemcpyDeviceToHost, s->st), "b");
     VMP_TRY(cudaMemcpyAsync(s->h_int, d_e, sizeof(int), cudaMemcpyDeviceToHost, s->st), "eff");
@@ -982,7 +1080,7 @@ vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double le
     if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "n larger than max_scan_points");
     if (!(leaf > 0)) return fail(s, VMP_ERR_INVALID_ARG, "leaf must be > 0");
     VMP_TRY(cudaMemcpyAsync(s->s.cloud, pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyHostToDevice, s->st), "upload");
-    k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
+    VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
     launch_downsample(s->s, n > 0 ? n : 1, leaf, s->ss, s->sc, s->st);
     VMP_TRY(cudaMemcpyAsync(s->h_int, s->s.d_n_down, sizeof(int), cudaMemcpyDeviceToHost, s->st), "n");
     VMP_TRY(cudaStreamSynchronize(s->st), "downsample");
@@ -1019,6 +1117,37 @@ vmp_status vmp_last_cloud(vmp_stream_t s, int kind, vmp_point* out, int max, int
     }
     return VMP_OK;
 }
+
+vmp_status vmp_profile_enable(vmp_stream_t s, int on) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    cudaStreamSynchronize(s->st);
+    s->prof_on = on != 0;
+    s->prof_pending.clear();
+    s->ev_used = 0;
+    for (int i = 0; i < VMP_PROF_SLOTS; ++i) { s->prof_ms[i] = 0; s->prof_launches[i] = 0; s->prof_items[i] = 0; }
+    return VMP_OK;
+}
+
+vmp_status vmp_profile_read(vmp_stream_t s, double* ms, long long* launches, long long* items) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    for (int i = 0; i < VMP_PROF_SLOTS; ++i) {
+        if (ms) ms[i] = s->prof_ms[i];
+        if (launches) launches[i] = s->prof_launches[i];
+        if (items) items[i] = s->prof_items[i];
+    }
+    return VMP_OK;
+}
+
+void* vmp_cuda_stream(vmp_stream_t s) { return s ? (void*)s->st : nullptr; }
+
+vmp_status vmp_io_bytes(vmp_stream_t s, long long* h2d, long long* d2h) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    if (h2d) *h2d = s->io_h2d;
+    if (d2h) *d2h = s->io_d2h + s->ms.merge_d2h;
+    return VMP_OK;
+}
+
+long long vmp_launch_count(void) { return g_launch_count.load(std::memory_order_relaxed); }
 
 // Selects the merge resolution: 0 = parallel fixed point (default),
 // 1 = single-thread replay in point order (both exact).
