@@ -226,6 +226,20 @@ vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* im
 /* pcl::VoxelGrid leaf-centroid downsample at the given leaf size. */
 vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double leaf,
                           vmp_point* out, int* n_out);
+/* The same leaf-centroid downsample for callers that cannot allocate device
+ * memory (no counterpart in the reference): a real-time sensor thread that
+ * must not call cudaMalloc/cudaFree, or a host framework whose own allocator
+ * owns the GPU's memory.  d_in / d_out are device buffers the caller owns
+ * (d_out holds up to n points); *n_out (host) receives the output count.  The
+ * working memory is a fixed 2 MiB __device__ array inside libvmp, held by
+ * every GPU that loads the library until exit; at most 65536 input points
+ * (VMP_ERR_CAPACITY above that).  The call allocates nothing.  Its first call
+ * on a device resolves the array's device address, so make that first call
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  cuda_stream may be
+ * NULL (default stream); the call returns after that stream finished. */
+vmp_status vmp_downsample_noalloc(const vmp_point* d_in, int n, double leaf, vmp_point* d_out, int* n_out,
+                                  void* cuda_stream);
 
 /* ---- measurement hooks (no reference counterpart) ----
  * Per-phase device time of vmp_process, from CUDA events recorded on the

@@ -31,6 +31,7 @@ CU_SOURCES = [
     "k_filter.cu",
     "k_map.cu",
     "k_merge.cu",
+    "vmp_noalloc.cu",
 ]
 
 
