@@ -200,3 +200,34 @@ def test_process_sequence_room(lio_mod, oracle_lib):
         dp = np.max(np.abs(np.array(rg.x.pos[:]) - np.array(ro.x.pos[:])))
         da = rot_angle(rg.x.rot[:], ro.x.rot[:])
         assert dp < 1e-6 and da < 1e-6, (k, dp, da)
+
+
+def test_undistort_and_predict_chain_match_oracle(lio_mod, oracle_lib):
+    """undistortCloud after IMU init + map init: the time-sorted compensated
+    cloud and the filter state / covariance at the scan end."""
+    import oracle as orc
+    seq_g = synth.Sequence(synth.KIND_ROOM, points_per_scan=6000)
+    seq_o = synth.Sequence(synth.KIND_ROOM, points_per_scan=6000)
+    cfg = abi.default_config(scan_resolution=0.2, max_scan_points=8192)
+    g = lio_mod.LIOBuilder(cfg)
+    o = orc.Oracle(cfg)
+    for _ in range(2):  # IMU_INIT, MAP_INIT
+        g.process(seq_g.next())
+        o.process(seq_o.next())
+    for _ in range(3):
+        pg, po = seq_g.next(), seq_o.next()
+        cg = g.undistort(pg)
+        out = (abi.vmp_point * po.n)()
+        scan = po.scan()
+        oracle_lib.orc_undistort(o.h, C.byref(scan), po.imus, po.n_imu, out)
+        co = np.ctypeslib.as_array(C.cast(out, C.POINTER(C.c_float)), shape=(po.n, 4))
+        assert np.array_equal(cg[:, 3], co[:, 3])  # same time order
+        same = np.mean(np.all(cg.view(np.uint32) == co.view(np.uint32), axis=1))
+        assert same > 0.999 and np.max(np.abs(cg - co)) < 1e-5, (same, np.max(np.abs(cg - co)))
+        xg, Pg = g.kf.get()
+        xo = abi.vmp_state()
+        Po = np.zeros(529)
+        oracle_lib.orc_get_state(o.h, C.byref(xo), _dp(Po))
+        for fld in ("pos", "rot", "vel"):
+            assert np.allclose(np.array(getattr(xg, fld)[:]), np.array(getattr(xo, fld)[:]), rtol=0, atol=1e-12), fld
+        assert np.max(np.abs(Pg.reshape(529) - Po)) <= 1e-12 * np.max(np.abs(Po))

@@ -29,6 +29,7 @@ CU_SOURCES = [
     "k_sort.cu",
     "k_points.cu",
     "k_filter.cu",
+    "k_predict.cu",
     "k_map.cu",
     "k_merge.cu",
     "vmp_noalloc.cu",

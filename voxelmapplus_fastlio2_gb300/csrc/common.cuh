@@ -60,6 +60,22 @@ struct DPose {
     double rot[9];
 };
 
+// Per-step terms of the IMU predict chain (k_predict.cu).
+struct DStep {
+    double dt, offset;
+    double acc[3], gyro[3], ab[3];
+    double E[9];     // Exp((gyro - bg) dt)
+    double nJr[9];   // -Jr((gyro - bg) dt) dt
+    double rot[9];   // rotation before the step
+    double FRa[9];   // (-rot [acc - ba]x) dt
+    double nRdt[9];  // -rot dt
+    double Mxdt[6];  // Mx dt
+    double B[24];    // G Q G^T: block 3-5, block 12-14, diagonal 15-20
+    double vinc[3], velA[3], posA[3];
+    int pose;
+    int pad;
+};
+
 // Filter state + LIO bookkeeping that lives on the device between scans.
 struct DFilter {
     DState x;

@@ -37,6 +37,7 @@ struct DScan {
     // IMU package
     vmp_imu* imus;         // [max_imu]
     DPose* poses;          // [max_imu + 2]
+    DStep* steps;          // [max_imu + 2] per-step terms of the predict chain
     // reduction partials
     double* partials;      // [res_blocks * 80]
     unsigned int* done_ctr;
@@ -50,6 +51,8 @@ void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& c
                      cudaStream_t st);
 void launch_predict_chain(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st);
 void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st);
+// ---- k_predict.cu
+void launch_predict_chain2(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st);
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st);
 void launch_update_begin(DFilter* f, cudaStream_t st);
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,

@@ -495,6 +495,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     CREATE_TRY(dalloc(s, &sc.d_n_batch, 4));
     CREATE_TRY(dalloc(s, &sc.imus, max_imu + 8));
     CREATE_TRY(dalloc(s, &sc.poses, max_imu + 8));
+    CREATE_TRY(dalloc(s, &sc.steps, max_imu + 8));
     CREATE_TRY(dalloc(s, &sc.partials, (size_t)sc.res_blocks * 160));
     CREATE_TRY(dalloc(s, &sc.done_ctr, 4));
     CREATE_TRY(cudaMemset(sc.done_ctr, 0, sizeof(unsigned int) * 4));
@@ -764,7 +765,7 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
     launch_time_sort(s->s, n, s->ss, st);
     s->pend(VMP_PROF_TIME_SORT, 0);
     s->pbeg();
-    launch_predict_chain(s->f, s->s, n_imu, t_start, t_end, st);
+    launch_predict_chain2(s->f, s->s, n_imu, t_start, t_end, st);
     s->pend(VMP_PROF_PREDICT, -1);
     s->pbeg();
     launch_undistort(s->f, s->s, n, st);
@@ -1067,7 +1068,7 @@ vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* im
     v = upload_imus(s, imus, n_imu, false);
     if (v != VMP_OK) return v;
     launch_time_sort(s->s, n, s->ss, s->st);
-    launch_predict_chain(s->f, s->s, n_imu, scan->t_start, scan->t_end, s->st);
+    launch_predict_chain2(s->f, s->s, n_imu, scan->t_start, scan->t_end, s->st);
     launch_undistort(s->f, s->s, n, s->st);
     VMP_TRY(cudaGetLastError(), "undistort");
     VMP_TRY(cudaMemcpyAsync(out, s->s.cloud, sizeof(vmp_point) * (size_t)n, cudaMemcpyDeviceToHost, s->st), "cloud");
