@@ -7,9 +7,12 @@ from voxelmapplus_fastlio2_gb300 import abi
 
 
 def rot_angle(Ra, Rb):
+    """Angle of Ra^T Rb, accurate for small angles (atan2 of the skew part
+    against the trace, not arccos of the trace)."""
     R = np.asarray(Ra).reshape(3, 3).T @ np.asarray(Rb).reshape(3, 3)
-    c = np.clip((np.trace(R) - 1.0) / 2.0, -1.0, 1.0)
-    return float(np.arccos(c))
+    s = 0.5 * np.linalg.norm([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]])
+    c = (np.trace(R) - 1.0) / 2.0
+    return float(np.arctan2(s, c))
 
 
 def plane_points(rng, n_planes=40, pts_per=(5, 160), extent=20.0, noise=0.01, iso_frac=0.1):

@@ -30,6 +30,7 @@ CU_SOURCES = [
     "k_points.cu",
     "k_filter.cu",
     "k_predict.cu",
+    "k_iekf.cu",
     "k_map.cu",
     "k_merge.cu",
     "vmp_noalloc.cu",

@@ -82,8 +82,8 @@ struct DFilter {
     double P[529];
     double Q[144];
     DState x_pred;
-    double Pinv[529];
-    double Hinv[529];
+    double K[23 * 12];  // gain M_E S^-1 of the last iteration (ld 12)
+    double Hinv[529];   // M = D P D^T of the last iteration
     double delta[23];
     double Hm[144];
     double bm[12];
@@ -378,24 +378,31 @@ __device__ inline void s2_Nx(const double* g, double* r /*2x3*/) {
     mm<2, 3, 3>(bxT, H, r);
 }
 
+// Boxplus pieces: R <- R Exp(d) and the S2 gravity update (ieskf.cpp:11-21).
+__device__ inline void rot_plus(double* R, const double* d) {
+    double E[9], T[9];
+    so3_exp(d, E); mm<3, 3, 3>(R, E, T); for (int i = 0; i < 9; ++i) R[i] = T[i];
+}
+__device__ inline void s2_plus(double* g, const double* d) {
+    double bx[6], w[3], E[9], g2[3];
+    s2_Bx(g, bx);
+    mm<3, 2, 1>(bx, d, w);
+    so3_exp(w, E);
+    m3v(E, g, g2);
+    for (int i = 0; i < 3; ++i) g[i] = g2[i];
+}
 // State boxplus with a 23-vector (ieskf.cpp:11-21)
 __device__ inline void state_plus23(DState& x, const double* d) {
-    double E[9], T[9];
     for (int i = 0; i < 3; ++i) x.pos[i] = x.pos[i] + d[i];
-    so3_exp(d + 3, E); mm<3, 3, 3>(x.rot, E, T); for (int i = 0; i < 9; ++i) x.rot[i] = T[i];
-    so3_exp(d + 6, E); mm<3, 3, 3>(x.rot_ext, E, T); for (int i = 0; i < 9; ++i) x.rot_ext[i] = T[i];
+    rot_plus(x.rot, d + 3);
+    rot_plus(x.rot_ext, d + 6);
     for (int i = 0; i < 3; ++i) {
         x.pos_ext[i] = x.pos_ext[i] + d[9 + i];
         x.vel[i] = x.vel[i] + d[12 + i];
         x.bg[i] = x.bg[i] + d[15 + i];
         x.ba[i] = x.ba[i] + d[18 + i];
     }
-    double bx[6], w[3], g2[3];
-    s2_Bx(x.g, bx);
-    mm<3, 2, 1>(bx, d + 21, w);
-    so3_exp(w, E);
-    m3v(E, x.g, g2);
-    for (int i = 0; i < 3; ++i) x.g[i] = g2[i];
+    s2_plus(x.g, d + 21);
 }
 // State boxplus with a 24-vector (ieskf.cpp:23-33)
 __device__ inline void state_plus24(DState& x, const double* d) {
@@ -414,39 +421,47 @@ __device__ inline void state_plus24(DState& x, const double* d) {
     m3v(E, x.g, g2);
     for (int i = 0; i < 3; ++i) x.g[i] = g2[i];
 }
+// Boxminus pieces (ieskf.cpp:35-67): Log(o^T x) and the S2 difference of
+// two gravity vectors.
+__device__ inline void rot_minus(const double* xr, const double* orr, double* d) {
+    double RT[9], M[9];
+    tr<3, 3>(orr, RT); mm<3, 3, 3>(RT, xr, M); so3_log(M, d);
+}
+__device__ inline void s2_minus(const double* xg, const double* og, double* d) {
+    double H[9], hg[3];
+    hat3(xg, H);
+    m3v(H, og, hg);
+    double v_sin = sqrt(dot3(hg, hg));
+    double v_cos = dot3(xg, og);
+    double theta = atan2(v_sin, v_cos);
+    if (v_sin < 1e-11) {
+        if (fabs(theta) > 1e-11) { d[0] = 3.1415926; d[1] = 0; }
+        else { d[0] = 0; d[1] = 0; }
+    } else {
+        double bx[6], bxT[6], Ho[9], T1[6], T2[2];
+        s2_Bx(og, bx);
+        tr<3, 2>(bx, bxT);
+        const double s = theta / v_sin;
+        for (int i = 0; i < 6; ++i) bxT[i] = s * bxT[i];
+        hat3(og, Ho);
+        mm<2, 3, 3>(bxT, Ho, T1);
+        mm<2, 3, 1>(T1, xg, T2);
+        d[0] = T2[0]; d[1] = T2[1];
+    }
+}
 // State boxminus (ieskf.cpp:35-67)
 __device__ inline void state_minus(const DState& x, const DState& o, double* d) {
-    double RT[9], M[9];
     for (int i = 0; i < 23; ++i) d[i] = 0.0;
     for (int i = 0; i < 3; ++i) d[i] = x.pos[i] - o.pos[i];
-    tr<3, 3>(o.rot, RT); mm<3, 3, 3>(RT, x.rot, M); so3_log(M, d + 3);
-    tr<3, 3>(o.rot_ext, RT); mm<3, 3, 3>(RT, x.rot_ext, M); so3_log(M, d + 6);
+    rot_minus(x.rot, o.rot, d + 3);
+    rot_minus(x.rot_ext, o.rot_ext, d + 6);
     for (int i = 0; i < 3; ++i) {
         d[9 + i] = x.pos_ext[i] - o.pos_ext[i];
         d[12 + i] = x.vel[i] - o.vel[i];
         d[15 + i] = x.bg[i] - o.bg[i];
         d[18 + i] = x.ba[i] - o.ba[i];
     }
-    double H[9], hg[3];
-    hat3(x.g, H);
-    m3v(H, o.g, hg);
-    double v_sin = sqrt(dot3(hg, hg));
-    double v_cos = dot3(x.g, o.g);
-    double theta = atan2(v_sin, v_cos);
-    if (v_sin < 1e-11) {
-        if (fabs(theta) > 1e-11) { d[21] = 3.1415926; d[22] = 0; }
-        else { d[21] = 0; d[22] = 0; }
-    } else {
-        double bx[6], bxT[6], Ho[9], T1[6], T2[2];
-        s2_Bx(o.g, bx);
-        tr<3, 2>(bx, bxT);
-        const double s = theta / v_sin;
-        for (int i = 0; i < 6; ++i) bxT[i] = s * bxT[i];
-        hat3(o.g, Ho);
-        mm<2, 3, 3>(bxT, Ho, T1);
-        mm<2, 3, 1>(T1, x.g, T2);
-        d[21] = T2[0]; d[22] = T2[1];
-    }
+    s2_minus(x.g, o.g, d + 21);
 }
 
 // ----- error reporting

@@ -1,106 +1,13 @@
 // Small-state FP64 kernels of the iterated error-state Kalman filter and the
 // per-point measurement model:
 //   k_imu_init        LIOBuilder::initializeImu        lio_builder.cpp:28-63
-//   k_predict_chain   undistortCloud's IMU loop        lio_builder.cpp:65-123
-//                     + IESKF::predict                 ieskf.cpp:101-123
+//   k_predict_once    one IESKF::predict               ieskf.cpp:101-123
 //   k_undistort       undistortCloud's point loop      lio_builder.cpp:125-152
-//   k_update_begin / k_residual / k_update_end
-//                     IESKF::update                    ieskf.cpp:125-156
-//                     + sharedUpdateFunc               lio_builder.cpp:250-311
-//                     + VoxelMap::buildResidual        voxel_map.cpp:258-276
-// The residual kernel is the hot one: one thread per downsampled point
-// (grid-stride over a fixed grid), FP64 world transform, hash probe, gate and
-// Jacobian row, a warp-shuffle + per-block reduction of H / b, and the last
-// CTA to finish folds the block partials in a fixed order (deterministic) and
-// runs the 23x23 FP64 iteration step of the filter.
+// The IMU loop of undistortCloud is k_predict.cu; IESKF::update with the
+// residual kernel is k_iekf.cu.
 #include "kernels.cuh"
 
 namespace vmp {
-
-// ---------------------------------------------------------------- block algebra
-// All matrices 23x23 row-major in shared memory; sums in k order so that the
-// result equals the reference's dense Eigen products.
-__device__ void blk_mm23(const double* A, const double* B, double* C) {
-    for (int e = threadIdx.x; e < 529; e += blockDim.x) {
-        int i = e / 23, j = e % 23;
-        double s = A[i * 23] * B[j];
-        for (int k = 1; k < 23; ++k) s = s + A[i * 23 + k] * B[k * 23 + j];
-        C[e] = s;
-    }
-    __syncthreads();
-}
-// C = A^T * B
-__device__ void blk_mm23_tn(const double* A, const double* B, double* C) {
-    for (int e = threadIdx.x; e < 529; e += blockDim.x) {
-        int i = e / 23, j = e % 23;
-        double s = A[i] * B[j];
-        for (int k = 1; k < 23; ++k) s = s + A[k * 23 + i] * B[k * 23 + j];
-        C[e] = s;
-    }
-    __syncthreads();
-}
-// C = A * B^T
-__device__ void blk_mm23_nt(const double* A, const double* B, double* C) {
-    for (int e = threadIdx.x; e < 529; e += blockDim.x) {
-        int i = e / 23, j = e % 23;
-        double s = A[i * 23] * B[j * 23];
-        for (int k = 1; k < 23; ++k) s = s + A[i * 23 + k] * B[j * 23 + k];
-        C[e] = s;
-    }
-    __syncthreads();
-}
-
-// Inverse by LU with partial pivoting (first maximum), then per-column
-// forward / back substitution -- the same operation sequence as the oracle's
-// restatement of Eigen's PartialPivLU inverse.
-__device__ void blk_inverse23(const double* A, double* inv, double* lu, int* perm) {
-    for (int e = threadIdx.x; e < 529; e += blockDim.x) lu[e] = A[e];
-    if (threadIdx.x < 23) perm[threadIdx.x] = threadIdx.x;
-    __shared__ int s_piv;
-    __syncthreads();
-    for (int k = 0; k < 23; ++k) {
-        if (threadIdx.x == 0) {
-            int p = k;
-            double best = fabs(lu[k * 23 + k]);
-            for (int i = k + 1; i < 23; ++i) {
-                double v = fabs(lu[i * 23 + k]);
-                if (v > best) { best = v; p = i; }
-            }
-            s_piv = p;
-            if (p != k) { int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
-        }
-        __syncthreads();
-        int p = s_piv;
-        if (p != k && threadIdx.x < 23) {
-            double t = lu[k * 23 + threadIdx.x];
-            lu[k * 23 + threadIdx.x] = lu[p * 23 + threadIdx.x];
-            lu[p * 23 + threadIdx.x] = t;
-        }
-        __syncthreads();
-        double piv = lu[k * 23 + k];
-        if (threadIdx.x > k && threadIdx.x < 23) lu[threadIdx.x * 23 + k] = lu[threadIdx.x * 23 + k] / piv;
-        __syncthreads();
-        int rows = 22 - k;
-        for (int e = threadIdx.x; e < rows * rows; e += blockDim.x) {
-            int i = k + 1 + e / rows, j = k + 1 + e % rows;
-            lu[i * 23 + j] = lu[i * 23 + j] - lu[i * 23 + k] * lu[k * 23 + j];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x < 23) {
-        const int c = threadIdx.x;
-        double x[23];
-        for (int i = 0; i < 23; ++i) x[i] = (perm[i] == c) ? 1.0 : 0.0;
-        for (int i = 0; i < 23; ++i)
-            for (int j = 0; j < i; ++j) x[i] = x[i] - lu[i * 23 + j] * x[j];
-        for (int i = 22; i >= 0; --i) {
-            for (int j = i + 1; j < 23; ++j) x[i] = x[i] - lu[i * 23 + j] * x[j];
-            x[i] = x[i] / lu[i * 23 + i];
-        }
-        for (int i = 0; i < 23; ++i) inv[i * 23 + c] = x[i];
-    }
-    __syncthreads();
-}
 
 __device__ inline void set_block3(double* M, int ld, int r0, int c0, const double* b) {
     for (int i = 0; i < 3; ++i)
@@ -305,95 +212,6 @@ __device__ void predict_step(PredSmem& s, const double* acc, const double* gyro,
     __syncthreads();
 }
 
-__global__ void k_predict_chain(DFilter* f, const vmp_imu* imus, int n_imu, double t_begin, double t_end,
-                                DPose* poses) {
-    __shared__ PredSmem s;
-    __shared__ double s_in[6];
-    __shared__ int s_go;
-    const int t = threadIdx.x;
-    for (int e = t; e < 529; e += blockDim.x) s.P[e] = f->P[e];
-    for (int e = t; e < 144; e += blockDim.x) s.Q[e] = f->Q[e];
-    if (t == 0) s.x = f->x;
-    __syncthreads();
-    const double last_end = f->last_cloud_end_time;
-    if (t == 0) {
-        DPose& p0 = poses[0];
-        p0.offset = 0.0;
-        for (int a = 0; a < 3; ++a) {
-            p0.acc[a] = f->last_acc[a]; p0.gyro[a] = f->last_gyro[a];
-            p0.vel[a] = s.x.vel[a]; p0.pos[a] = s.x.pos[a];
-        }
-        for (int a = 0; a < 9; ++a) p0.rot[a] = s.x.rot[a];
-    }
-    int npose = 1;
-    double inp_acc[3] = {0, 0, 0}, inp_gyro[3] = {0, 0, 0};
-    // imu_cache = [last_imu] + package imus
-    for (int k = 0; k < n_imu; ++k) {
-        double ht, hacc[3], hgyro[3];
-        if (k == 0) {
-            ht = f->last_imu_t;
-            for (int a = 0; a < 3; ++a) { hacc[a] = f->last_imu_acc[a]; hgyro[a] = f->last_imu_gyro[a]; }
-        } else {
-            ht = imus[k - 1].t;
-            for (int a = 0; a < 3; ++a) { hacc[a] = imus[k - 1].acc[a]; hgyro[a] = imus[k - 1].gyro[a]; }
-        }
-        const vmp_imu& tail = imus[k];
-        if (tail.t < last_end) continue;
-        double dt;
-        if (t == 0) {
-            for (int a = 0; a < 3; ++a) {
-                double gv = 0.5 * (hgyro[a] + tail.gyro[a]);
-                double av = 0.5 * (hacc[a] + tail.acc[a]);
-                av = av * 9.81 / f->gravity_norm;
-                s_in[a] = av;
-                s_in[3 + a] = gv;
-            }
-        }
-        __syncthreads();
-        dt = (ht < last_end) ? tail.t - last_end : tail.t - ht;
-        for (int a = 0; a < 3; ++a) { inp_acc[a] = s_in[a]; inp_gyro[a] = s_in[3 + a]; }
-        predict_step(s, inp_acc, inp_gyro, dt);
-        if (t == 0) {
-            DPose& p = poses[npose];
-            double ab[3], ra[3];
-            for (int a = 0; a < 3; ++a) ab[a] = inp_acc[a] - s.x.ba[a];
-            m3v(s.x.rot, ab, ra);
-            for (int a = 0; a < 3; ++a) {
-                f->last_gyro[a] = inp_gyro[a] - s.x.bg[a];
-                f->last_acc[a] = ra[a] + s.x.g[a];
-                p.acc[a] = f->last_acc[a];
-                p.gyro[a] = f->last_gyro[a];
-                p.vel[a] = s.x.vel[a];
-                p.pos[a] = s.x.pos[a];
-            }
-            for (int a = 0; a < 9; ++a) p.rot[a] = s.x.rot[a];
-            p.offset = tail.t - t_begin;
-        }
-        npose++;
-        __syncthreads();
-    }
-    // final predict to the scan end with the last input
-    {
-        const double imu_time_end = n_imu > 0 ? imus[n_imu - 1].t : f->last_imu_t;
-        double dt = t_end - imu_time_end;
-        if (t == 0) s_go = 1;
-        __syncthreads();
-        predict_step(s, inp_acc, inp_gyro, dt);
-    }
-    for (int e = t; e < 529; e += blockDim.x) f->P[e] = s.P[e];
-    if (t == 0) {
-        f->x = s.x;
-        f->npose = npose;
-        if (n_imu > 0) {
-            const vmp_imu& last = imus[n_imu - 1];
-            f->last_imu_t = last.t;
-            for (int a = 0; a < 3; ++a) { f->last_imu_acc[a] = last.acc[a]; f->last_imu_gyro[a] = last.gyro[a]; }
-        }
-        f->last_cloud_end_time = t_end;
-        for (int a = 0; a < 3; ++a) { f->inp_acc[a] = inp_acc[a]; f->inp_gyro[a] = inp_gyro[a]; }
-    }
-}
-
 // Single IESKF::predict (component entry point).
 __global__ void k_predict_once(DFilter* f, double a0, double a1, double a2, double g0, double g1, double g2,
                                double dt) {
@@ -467,266 +285,12 @@ __global__ void k_undistort(const DFilter* __restrict__ f, const DPose* __restri
     }
 }
 
-// ---------------------------------------------------------------- update
-__global__ void k_update_begin(DFilter* f) {
-    __shared__ double sP[529], sInv[529], lu[529];
-    __shared__ int perm[23];
-    for (int e = threadIdx.x; e < 529; e += blockDim.x) sP[e] = f->P[e];
-    if (threadIdx.x == 0) {
-        f->x_pred = f->x;
-        f->converged = 0;
-        f->iters = 0;
-        f->effect_num = 0;
-        f->no_effect = 0;
-        for (int i = 0; i < 23; ++i) f->delta[i] = 0.0;
-    }
-    __syncthreads();
-    blk_inverse23(sP, sInv, lu, perm);
-    for (int e = threadIdx.x; e < 529; e += blockDim.x) f->Pinv[e] = sInv[e];
-}
-
-constexpr int kResThreads = 256;
-constexpr int kPartStride = 160;  // >= 12*12 + 12 + 1
-
-// IESKF::update loop body after func_ (ieskf.cpp:135-148), one CTA.
-__device__ void ieskf_iteration_step(DFilter* f, double eps) {
-    __shared__ double sJ[529], sA[529], sH[529], sInv[529], lu[529];
-    __shared__ double sd[23], sb[23];
-    __shared__ int perm[23];
-    const int t = threadIdx.x;
-    for (int e = t; e < 529; e += blockDim.x) { sJ[e] = (e % 24 == 0) ? 1.0 : 0.0; sInv[e] = f->Pinv[e]; }
-    __syncthreads();
-    if (t == 0) {
-        state_minus(f->x, f->x_pred, sd);
-        double Jr[9];
-        so3_right_jac(sd + 3, Jr);
-        set_block3(sJ, 23, 3, 3, Jr);
-        so3_right_jac(sd + 6, Jr);
-        set_block3(sJ, 23, 6, 6, Jr);
-        double Nx[6], Mx[6], NM[4];
-        s2_Nx(f->x.g, Nx);
-        s2_Mx_res(f->x_pred.g, sd + 21, Mx);
-        mm<2, 3, 2>(Nx, Mx, NM);
-        sJ[21 * 23 + 21] = NM[0]; sJ[21 * 23 + 22] = NM[1];
-        sJ[22 * 23 + 21] = NM[2]; sJ[22 * 23 + 22] = NM[3];
-    }
-    __syncthreads();
-    blk_mm23_tn(sJ, sInv, sA);  // A = J^T P^-1
-    // b = A * delta ; H = A * J
-    if (t < 23) {
-        double s = sA[t * 23] * sd[0];
-        for (int k = 1; k < 23; ++k) s = s + sA[t * 23 + k] * sd[k];
-        sb[t] = s;
-    }
-    blk_mm23(sA, sJ, sH);
-    for (int e = t; e < 144; e += blockDim.x) {
-        int r = e / 12, c = e % 12;
-        sH[r * 23 + c] = sH[r * 23 + c] + f->Hm[e];
-    }
-    if (t < 12) sb[t] = sb[t] + f->bm[t];
-    __syncthreads();
-    blk_inverse23(sH, sInv, lu, perm);
-    if (t < 23) {
-        double s = sInv[t * 23] * sb[0];
-        for (int k = 1; k < 23; ++k) s = s + sInv[t * 23 + k] * sb[k];
-        sd[t] = -s;
-    }
-    __syncthreads();
-    for (int e = t; e < 529; e += blockDim.x) f->Hinv[e] = sInv[e];
-    if (t == 0) {
-        state_plus23(f->x, sd);
-        double mx = sd[0];
-        for (int i = 1; i < 23; ++i) mx = fmax(mx, sd[i]);
-        for (int i = 0; i < 23; ++i) f->delta[i] = sd[i];
-        f->iters = f->iters + 1;
-        if (mx < eps) f->converged = 1;
-    }
-}
-
-template <int NJ>
-__global__ void __launch_bounds__(kResThreads) k_residual(DFilter* f, DScan s, DMap m, double eps, int do_step) {
-    constexpr int NV = NJ * NJ + NJ;
-    __shared__ double s_red[kResThreads / 32][NV + 1];
-    __shared__ double s_rwl[9], s_pwl[3], s_rot[9], s_rext[9], s_pext[3], s_prr[9], s_ppp[9];
-    __shared__ int s_last;
-    if (f->converged) return;  // written by the previous launch; uniform
-    const int n = *s.d_n_down;
-    const int t = threadIdx.x;
-    if (t == 0) {
-        const DState& x = f->x;
-        mm<3, 3, 3>(x.rot, x.rot_ext, s_rwl);
-        double rp[3];
-        m3v(x.rot, x.pos_ext, rp);
-        for (int a = 0; a < 3; ++a) s_pwl[a] = rp[a] + x.pos[a];
-        for (int a = 0; a < 9; ++a) { s_rot[a] = x.rot[a]; s_rext[a] = x.rot_ext[a]; }
-        for (int a = 0; a < 3; ++a) s_pext[a] = x.pos_ext[a];
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                s_prr[i * 3 + j] = f->P[(3 + i) * 23 + 3 + j];
-                s_ppp[i * 3 + j] = f->P[i * 23 + j];
-            }
-    }
-    __syncthreads();
-    double accH[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) accH[k] = 0.0;
-    double cnt = 0.0;
-    for (int i = blockIdx.x * blockDim.x + t; i < n; i += gridDim.x * blockDim.x) {
-        double pl[3] = {s.pl[i * 3], s.pl[i * 3 + 1], s.pl[i * 3 + 2]};
-        double cl[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) cl[k] = s.covl[i * 9 + k];
-        double pw[3];
-        m3v(s_rwl, pl, pw);
-        for (int a = 0; a < 3; ++a) pw[a] = pw[a] + s_pwl[a];
-        int64_t key[3];
-        bool inr = voxel_index(pw, m.voxel_size, key);
-        uint32_t rec = inr ? map_find(m, pack_key(key[0], key[1], key[2])) : kNoRec;
-        if (rec != kNoRec) {
-            const RecHot hot = m.hot[rec];
-            if (hot.flags & F_PLANE) {
-                // cov_world = r_wl cov_l r_wl^T + [p]x P_rr [p]x^T + P_pp
-                double T1[9], T2[9], rT[9], cm[9], cmT[9], T3[9], T4[9], cw[9];
-                mm<3, 3, 3>(s_rwl, cl, T1);
-                tr<3, 3>(s_rwl, rT);
-                mm<3, 3, 3>(T1, rT, T2);
-                hat3(pl, cm);
-                mm<3, 3, 3>(cm, s_prr, T3);
-                tr<3, 3>(cm, cmT);
-                mm<3, 3, 3>(T3, cmT, T4);
-                for (int k = 0; k < 9; ++k) cw[k] = (T2[k] + T4[k]) + s_ppp[k];
-                double p2m[3] = {pw[0] - hot.mean[0], pw[1] - hot.mean[1], pw[2] - hot.mean[2]};
-                double r = dot3(hot.norm, p2m);
-                double nc[3];
-                for (int j = 0; j < 3; ++j) nc[j] = (hot.norm[0] * cw[j] + hot.norm[1] * cw[3 + j]) + hot.norm[2] * cw[6 + j];
-                double sigma = dot3(nc, hot.norm);
-                uint8_t valid = fabs(r) < 3.0 * sqrt(sigma) ? 1 : 0;
-                s.rvalid[i] = valid;
-                s.rnorm[i * 3] = hot.norm[0]; s.rnorm[i * 3 + 1] = hot.norm[1]; s.rnorm[i * 3 + 2] = hot.norm[2];
-                s.rres[i] = r;
-            } else {
-                s.rvalid[i] = 0;
-            }
-        }
-        if (s.rvalid[i]) {
-            double nn[3] = {s.rnorm[i * 3], s.rnorm[i * 3 + 1], s.rnorm[i * 3 + 2]};
-            double r = s.rres[i];
-            // r_cov = n^T r_wl cov_l r_wl^T n
-            double u1[3], u2[3], u3[3];
-            for (int j = 0; j < 3; ++j) u1[j] = (nn[0] * s_rwl[j] + nn[1] * s_rwl[3 + j]) + nn[2] * s_rwl[6 + j];
-            for (int j = 0; j < 3; ++j) u2[j] = (u1[0] * cl[j] + u1[1] * cl[3 + j]) + u1[2] * cl[6 + j];
-            for (int j = 0; j < 3; ++j) u3[j] = (u2[0] * s_rwl[j * 3] + u2[1] * s_rwl[j * 3 + 1]) + u2[2] * s_rwl[j * 3 + 2];
-            double r_cov = dot3(u3, nn);
-            double w = r_cov < 0.0002 ? 5000 : 1.0 / r_cov;
-            double J[NJ];
-            J[0] = nn[0]; J[1] = nn[1]; J[2] = nn[2];
-            double q[3], Hq[9], v1[3];
-            m3v(s_rext, pl, q);
-            for (int a = 0; a < 3; ++a) q[a] = q[a] + s_pext[a];
-            hat3(q, Hq);
-            for (int j = 0; j < 3; ++j) v1[j] = ((-nn[0]) * s_rot[j] + (-nn[1]) * s_rot[3 + j]) + (-nn[2]) * s_rot[6 + j];
-            for (int j = 0; j < 3; ++j) J[3 + j] = (v1[0] * Hq[j] + v1[1] * Hq[3 + j]) + v1[2] * Hq[6 + j];
-            if (NJ == 12) {
-                double v2[3], Hp[9];
-                for (int j = 0; j < 3; ++j) v2[j] = ((-nn[0]) * s_rwl[j] + (-nn[1]) * s_rwl[3 + j]) + (-nn[2]) * s_rwl[6 + j];
-                hat3(pl, Hp);
-                for (int j = 0; j < 3; ++j) J[(6 + j) % NJ] = (v2[0] * Hp[j] + v2[1] * Hp[3 + j]) + v2[2] * Hp[6 + j];
-                for (int j = 0; j < 3; ++j) J[(9 + j) % NJ] = (nn[0] * s_rot[j] + nn[1] * s_rot[3 + j]) + nn[2] * s_rot[6 + j];
-            }
-#pragma unroll
-            for (int a = 0; a < NJ; ++a) {
-                double u = J[a] * w;
-#pragma unroll
-                for (int c = 0; c < NJ; ++c) accH[a * NJ + c] = accH[a * NJ + c] + u * J[c];
-                accH[NJ * NJ + a] = accH[NJ * NJ + a] + u * r;
-            }
-            cnt = cnt + 1.0;
-        }
-    }
-    // block reduction (fixed order)
-    const int lane = t & 31, warp = t >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        double v = warp_sum(accH[k]);
-        if (lane == 0) s_red[warp][k] = v;
-    }
-    {
-        double v = warp_sum(cnt);
-        if (lane == 0) s_red[warp][NV] = v;
-    }
-    __syncthreads();
-    for (int k = t; k <= NV; k += blockDim.x) {
-        double v = s_red[0][k];
-        for (int w = 1; w < kResThreads / 32; ++w) v = v + s_red[w][k];
-        s.partials[blockIdx.x * kPartStride + k] = v;
-    }
-    __threadfence();
-    __syncthreads();
-    if (t == 0) {
-        unsigned int ticket = atomicAdd(s.done_ctr, 1u);
-        s_last = (ticket == gridDim.x - 1) ? 1 : 0;
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    // last CTA: fold block partials in block order -> H_meas (12x12), b_meas
-    for (int k = t; k <= NV; k += blockDim.x) {
-        double v = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) v = (b == 0) ? s.partials[k] : v + s.partials[b * kPartStride + k];
-        s_red[0][k] = v;
-    }
-    __syncthreads();
-    for (int e = t; e < 144; e += blockDim.x) {
-        int r = e / 12, c = e % 12;
-        f->Hm[e] = (r < NJ && c < NJ) ? s_red[0][r * NJ + c] : 0.0;
-    }
-    if (t < 12) f->bm[t] = t < NJ ? s_red[0][NJ * NJ + t] : 0.0;
-    if (t == 0) {
-        int eff = (int)s_red[0][NV];
-        f->effect_num = eff;
-        if (eff < 1) f->no_effect = 1;
-        *s.done_ctr = 0;
-    }
-    __syncthreads();
-    if (do_step) ieskf_iteration_step(f, eps);
-}
-
-// P = L H^-1 L^T (ieskf.cpp:151-155)
-__global__ void k_update_end(DFilter* f) {
-    __shared__ double sL[529], sI[529], sT[529];
-    const int t = threadIdx.x;
-    for (int e = t; e < 529; e += blockDim.x) { sL[e] = (e % 24 == 0) ? 1.0 : 0.0; sI[e] = f->Hinv[e]; }
-    __syncthreads();
-    if (f->iters == 0) return;
-    if (t == 0) {
-        const double* d = f->delta;
-        double Jr[9];
-        so3_right_jac(d + 3, Jr);
-        set_block3(sL, 23, 3, 3, Jr);
-        so3_right_jac(d + 6, Jr);
-        set_block3(sL, 23, 6, 6, Jr);
-        double Nx[6], Mx[6], NM[4];
-        s2_Nx(f->x.g, Nx);
-        s2_Mx_res(f->x_pred.g, d + 21, Mx);
-        mm<2, 3, 2>(Nx, Mx, NM);
-        sL[21 * 23 + 21] = NM[0]; sL[21 * 23 + 22] = NM[1];
-        sL[22 * 23 + 21] = NM[2]; sL[22 * 23 + 22] = NM[3];
-    }
-    __syncthreads();
-    blk_mm23(sL, sI, sT);
-    blk_mm23_nt(sT, sL, sI);
-    for (int e = t; e < 529; e += blockDim.x) f->P[e] = sI[e];
-}
-
 // ---------------------------------------------------------------- launchers
 void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& cfg, double t_end, cudaStream_t st) {
     DState ext{};
     for (int i = 0; i < 9; ++i) ext.rot_ext[i] = cfg.r_il[i];
     for (int i = 0; i < 3; ++i) ext.pos_ext[i] = cfg.p_il[i];
     VMP_NOTE_LAUNCH(); k_imu_init<<<1, 32, 0, st>>>(f, imus, n, cfg.gravity_align, ext, t_end);
-}
-void launch_predict_chain(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st) {
-    VMP_NOTE_LAUNCH(); k_predict_chain<<<1, 256, 0, st>>>(f, s.imus, n_imu, t_start, t_end, s.poses);
 }
 void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st) {
     int blocks = (n_max + 255) / 256;
@@ -737,16 +301,4 @@ void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st) {
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st) {
     VMP_NOTE_LAUNCH(); k_predict_once<<<1, 256, 0, st>>>(f, acc[0], acc[1], acc[2], gyro[0], gyro[1], gyro[2], dt);
 }
-void launch_update_begin(DFilter* f, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_update_begin<<<1, 256, 0, st>>>(f); }
-void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
-                          cudaStream_t st, int do_step) {
-    (void)n_max;
-    VMP_NOTE_LAUNCH();
-    if (estimate_ext)
-        k_residual<12><<<s.res_blocks, kResThreads, 0, st>>>(f, s, m, eps, do_step);
-    else
-        k_residual<6><<<s.res_blocks, kResThreads, 0, st>>>(f, s, m, eps, do_step);
-}
-void launch_update_end(DFilter* f, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_update_end<<<1, 256, 0, st>>>(f); }
-
 }  // namespace vmp

@@ -1,0 +1,505 @@
+// IESKF::update (ieskf.cpp:125-156) with the measurement model of
+// LIOBuilder::sharedUpdateFunc (lio_builder.cpp:250-311) and
+// VoxelMap::buildResidual (voxel_map.cpp:258-276).
+//
+// k_residual: one thread per downsampled point (grid-stride over a fixed
+// grid).  What decides a voxel key or the residual value is computed exactly
+// as the reference does (FP64, its operation order, no FMA): the world point
+// r_wl p + p_wl, floor(p / voxel_size) and r = n . (p_w - mean).  The gate's
+// variance and the weight use the reduced forms
+//     n^T (R S R^T + [p]x Prr [p]x^T + Ppp) n = u^T S u + v^T Prr v + n^T Ppp n,
+//     u = R^T n, v = n x p,      r_cov = u^T S u,
+// and the H / b accumulation uses FMA; these differ from the reference's
+// dense evaluation only by rounding (relative 1e-16), which cannot move a gate
+// decision except for a residual within that distance of its threshold.  The
+// upper triangle of H (and b, and the valid count) is reduced by warp shuffles
+// and a per-block fold; the last CTA to finish folds the block partials in a
+// fixed order (deterministic) and runs the filter step.
+//
+// The filter step solves the reference's information-form normal equations
+//     H = J^T P^-1 J + E Hm E^T,  b = J^T P^-1 d + E bm,  step = -H^-1 b
+// (E selects the 6 -- or 12 -- measured coordinates) without a 23x23 inverse:
+// with D = J^-1 (block diagonal: identity except the rot, rot_ext and S2
+// blocks), M = D P D^T and d' = D d,
+//     S = I + Hm M_EE,  K = M_E S^-1,  step = -d' + K (Hm d'_E - bm),
+//     H^-1 = M - K Hm (E^T M),
+// which is the same solution (Woodbury identity); it needs one NJ x NJ
+// Gauss-Jordan solve and products with block-diagonal matrices, all spread
+// over the lanes, with the transcendental functions of the boxminus / boxplus
+// on separate lanes.
+#include "kernels.cuh"
+
+namespace vmp {
+
+constexpr int kIekfThreads = 256;
+constexpr int kPartStride2 = 96;  // >= NJ(NJ+1)/2 + NJ + 1 for NJ = 12
+
+template <int NJ>
+struct Red {
+    static constexpr int NH = NJ * (NJ + 1) / 2;
+    static constexpr int NV = NH + NJ + 1;  // H upper triangle, b, count
+    static constexpr int NP = (NV + 31) / 32 * 32;  // padded to whole warps
+};
+
+// ---------------------------------------------------------------- point part
+template <int NJ>
+__device__ inline void residual_point(int i, const DScan& s, const DMap& m, const double* rwl, const double* pwl,
+                                      const double* rot, const double* rext, const double* pext, const double* Prr,
+                                      const double* Ppp, double* acc) {
+    const double pl[3] = {s.pl[i * 3], s.pl[i * 3 + 1], s.pl[i * 3 + 2]};
+    double pw[3];
+    m3v(rwl, pl, pw);
+    for (int a = 0; a < 3; ++a) pw[a] = pw[a] + pwl[a];
+    int64_t key[3];
+    const bool inr = voxel_index(pw, m.voxel_size, key);
+    const uint32_t rec = inr ? map_find(m, pack_key(key[0], key[1], key[2])) : kNoRec;
+    const double* cl = s.covl + (size_t)i * 9;
+    if (rec != kNoRec) {
+        const RecHot hot = m.hot[rec];
+        if (hot.flags & F_PLANE) {
+            const double* n = hot.norm;
+            const double p2m[3] = {pw[0] - hot.mean[0], pw[1] - hot.mean[1], pw[2] - hot.mean[2]};
+            const double r = dot3(n, p2m);
+            // u = R^T n ; v = n x p_l
+            double u[3], v[3], su[3], pv[3], pn[3];
+            for (int c = 0; c < 3; ++c) u[c] = fma(rwl[6 + c], n[2], fma(rwl[3 + c], n[1], rwl[c] * n[0]));
+            v[0] = fma(n[1], pl[2], -n[2] * pl[1]);
+            v[1] = fma(n[2], pl[0], -n[0] * pl[2]);
+            v[2] = fma(n[0], pl[1], -n[1] * pl[0]);
+            for (int c = 0; c < 3; ++c) {
+                su[c] = fma(cl[c * 3 + 2], u[2], fma(cl[c * 3 + 1], u[1], cl[c * 3] * u[0]));
+                pv[c] = fma(Prr[c * 3 + 2], v[2], fma(Prr[c * 3 + 1], v[1], Prr[c * 3] * v[0]));
+                pn[c] = fma(Ppp[c * 3 + 2], n[2], fma(Ppp[c * 3 + 1], n[1], Ppp[c * 3] * n[0]));
+            }
+            const double t1 = fma(u[2], su[2], fma(u[1], su[1], u[0] * su[0]));
+            const double t2 = fma(v[2], pv[2], fma(v[1], pv[1], v[0] * pv[0]));
+            const double t3 = fma(n[2], pn[2], fma(n[1], pn[1], n[0] * pn[0]));
+            const double sigma = t1 + t2 + t3;
+            s.rvalid[i] = fabs(r) < 3.0 * sqrt(sigma) ? 1 : 0;
+            s.rnorm[i * 3] = n[0]; s.rnorm[i * 3 + 1] = n[1]; s.rnorm[i * 3 + 2] = n[2];
+            s.rres[i] = r;
+        } else {
+            s.rvalid[i] = 0;
+        }
+    }
+    if (!s.rvalid[i]) return;  // a miss keeps the record of the previous iteration / scan
+    const double n[3] = {s.rnorm[i * 3], s.rnorm[i * 3 + 1], s.rnorm[i * 3 + 2]};
+    const double r = s.rres[i];
+    double u[3], su[3];
+    for (int c = 0; c < 3; ++c) u[c] = fma(rwl[6 + c], n[2], fma(rwl[3 + c], n[1], rwl[c] * n[0]));
+    for (int c = 0; c < 3; ++c) su[c] = fma(cl[c * 3 + 2], u[2], fma(cl[c * 3 + 1], u[1], cl[c * 3] * u[0]));
+    const double r_cov = fma(u[2], su[2], fma(u[1], su[1], u[0] * su[0]));
+    const double w = r_cov < 0.0002 ? 5000 : 1.0 / r_cov;
+    // J = [n, (-rot^T n) x q, ...]  with q = rot_ext p_l + pos_ext
+    double J[NJ], q[3], v1[3];
+    for (int c = 0; c < 3; ++c) {
+        q[c] = fma(rext[c * 3 + 2], pl[2], fma(rext[c * 3 + 1], pl[1], rext[c * 3] * pl[0])) + pext[c];
+        v1[c] = -fma(rot[6 + c], n[2], fma(rot[3 + c], n[1], rot[c] * n[0]));
+    }
+    J[0] = n[0]; J[1] = n[1]; J[2] = n[2];
+    J[3] = fma(v1[1], q[2], -v1[2] * q[1]);
+    J[4] = fma(v1[2], q[0], -v1[0] * q[2]);
+    J[5] = fma(v1[0], q[1], -v1[1] * q[0]);
+    if (NJ == 12) {
+        // (-(r_wl^T n)) x p_l and rot^T n
+        J[6 % NJ] = -fma(u[1], pl[2], -u[2] * pl[1]);
+        J[7 % NJ] = -fma(u[2], pl[0], -u[0] * pl[2]);
+        J[8 % NJ] = -fma(u[0], pl[1], -u[1] * pl[0]);
+        J[9 % NJ] = -v1[0]; J[10 % NJ] = -v1[1]; J[11 % NJ] = -v1[2];
+    }
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < NJ; ++a) {
+        const double ua = J[a] * w;
+#pragma unroll
+        for (int b = a; b < NJ; ++b) { acc[k] = fma(ua, J[b], acc[k]); ++k; }
+    }
+#pragma unroll
+    for (int a = 0; a < NJ; ++a) acc[Red<NJ>::NH + a] = fma(J[a] * w, r, acc[Red<NJ>::NH + a]);
+    acc[Red<NJ>::NH + NJ] += 1.0;
+}
+
+// ---------------------------------------------------------------- reductions
+// Butterfly reduce-scatter of 32 values per lane: after it, lane l holds the
+// warp's sum of value l (31 additions per lane instead of 5 x 32).  The tree
+// order is fixed, so the result is deterministic.
+__device__ inline double warp_reduce_scatter32(double* v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16, L = 32; o > 0; o >>= 1, L >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < L / 2; ++i) {
+            const double send = up ? v[i] : v[i + L / 2];
+            const double keep = up ? v[i + L / 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+// ---------------------------------------------------------------- filter step
+// Block-diagonal factor with identity outside the rot (3-5), rot_ext (6-8) and
+// S2 (21-22) blocks: D = J^-1 during the iterations, L at the end.
+struct BlkDiag {
+    double r[9], e[9], g[4];
+};
+
+struct IekfSm {
+    double M[529];  // D P D^T
+    double T[529];  // scratch
+    double aug[12 * 24];
+    double K[23 * 12];
+    double prow[24], col[12];
+    double d[23], dp[23], y[12], step[23];
+    BlkDiag D;
+    double ip;
+    int piv;
+};
+
+__device__ inline void inv3(const double* A, double* o) {
+    const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
+    const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+    const double id = 1.0 / det;
+    o[0] = c00 * id; o[1] = (A[2] * A[7] - A[1] * A[8]) * id; o[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+    o[3] = c01 * id; o[4] = (A[0] * A[8] - A[2] * A[6]) * id; o[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+    o[6] = c02 * id; o[7] = (A[1] * A[6] - A[0] * A[7]) * id; o[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
+__device__ inline int blk_of(int i) { return (i >= 3 && i < 6) ? 0 : (i >= 6 && i < 9) ? 1 : (i >= 21) ? 2 : -1; }
+
+// (B X)(i, j), X with leading dimension ld
+__device__ inline double bd_row(const BlkDiag& B, const double* X, int ld, int i, int j) {
+    const int b = blk_of(i);
+    if (b < 0) return X[i * ld + j];
+    if (b == 2) {
+        const int a = i - 21;
+        return fma(B.g[a * 2 + 1], X[22 * ld + j], B.g[a * 2] * X[21 * ld + j]);
+    }
+    const double* Dm = b == 0 ? B.r : B.e;
+    const int o = b == 0 ? 3 : 6, a = i - o;
+    return fma(Dm[a * 3 + 2], X[(o + 2) * ld + j], fma(Dm[a * 3 + 1], X[(o + 1) * ld + j], Dm[a * 3] * X[o * ld + j]));
+}
+// (X B^T)(i, j), X 23 x 23
+__device__ inline double bd_col(const BlkDiag& B, const double* X, int i, int j) {
+    const int b = blk_of(j);
+    const double* r = X + i * 23;
+    if (b < 0) return r[j];
+    if (b == 2) {
+        const int a = j - 21;
+        return fma(B.g[a * 2 + 1], r[22], B.g[a * 2] * r[21]);
+    }
+    const double* Dm = b == 0 ? B.r : B.e;
+    const int o = b == 0 ? 3 : 6, a = j - o;
+    return fma(Dm[a * 3 + 2], r[o + 2], fma(Dm[a * 3 + 1], r[o + 1], Dm[a * 3] * r[o]));
+}
+
+// out = B X B^T for a 23 x 23 X (global or shared), tmp 529 doubles; all threads.
+__device__ void bd_sandwich(const BlkDiag& B, const double* X, double* tmp, double* out) {
+    for (int e = threadIdx.x; e < 529; e += blockDim.x) tmp[e] = bd_row(B, X, 23, e / 23, e % 23);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 529; e += blockDim.x) out[e] = bd_col(B, tmp, e / 23, e % 23);
+    __syncthreads();
+}
+
+// Gauss-Jordan with partial pivoting on s.aug = [S | I] (nj x 2nj); S^-1 ends
+// in the right half.  All threads of the block take part.
+__device__ void gauss_jordan(IekfSm& s, int nj) {
+    const int t = threadIdx.x, lane = t & 31;
+    const int w = 2 * nj;
+    for (int k = 0; k < nj; ++k) {
+        if (t < 32) {
+            // pivot: largest |a_ik|, i >= k; magnitudes of doubles order like
+            // the integers of their high words (ties go to the lower row)
+            const int i = k + lane;
+            int key = -1;
+            if (i < nj) key = __double2hiint(s.aug[i * w + k]) & 0x7fffffff;
+            int best = i;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const int ok = __shfl_xor_sync(0xffffffffu, key, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, best, o);
+                if (ok > key || (ok == key && oi < best)) { key = ok; best = oi; }
+            }
+            if (lane == 0) s.piv = best;
+        }
+        __syncthreads();
+        const int p = s.piv;
+        if (p != k && t < w) {
+            const double a = s.aug[k * w + t];
+            s.aug[k * w + t] = s.aug[p * w + t];
+            s.aug[p * w + t] = a;
+        }
+        __syncthreads();
+        if (t < w) s.prow[t] = s.aug[k * w + t] * (1.0 / s.aug[k * w + k]);
+        else if (t >= 32 && t < 32 + nj) s.col[t - 32] = s.aug[(t - 32) * w + k];
+        __syncthreads();
+        for (int e = t; e < nj * w; e += blockDim.x) {
+            const int i = e / w, j = e - i * w;
+            s.aug[e] = (i == k) ? s.prow[j] : fma(-s.col[i], s.prow[j], s.aug[e]);
+        }
+        __syncthreads();
+    }
+}
+
+// The 15 linear coordinates of the error state: pos (0-2) and pos_ext, vel,
+// bg, ba (9-20); their offsets in DState (doubles) and in the 23-vector.
+__device__ inline int lin_state_off(int u) { return u < 3 ? u : u + 18; }
+__device__ inline int lin_delta_idx(int u) { return u < 3 ? u : u + 6; }
+
+// One pass of the IESKF::update loop body after func_ (ieskf.cpp:135-148) in
+// the information-form rewrite described at the top of this file.  H / b of
+// the measurement (nj x nj, nj) are in shared memory.  One CTA.
+__device__ void iekf_step(DFilter* f, IekfSm& s, const double* Hm, const double* bm, int nj, double eps) {
+    const int t = threadIdx.x;
+    const DState& x = f->x;
+    const DState& xp = f->x_pred;
+    // boxminus delta and D = J^-1, the transcendental pieces in separate warps
+    if (t == 0) {
+        double J[9];
+        rot_minus(x.rot, xp.rot, s.d + 3);
+        so3_right_jac(s.d + 3, J);
+        inv3(J, s.D.r);
+    } else if (t == 32) {
+        double J[9];
+        rot_minus(x.rot_ext, xp.rot_ext, s.d + 6);
+        so3_right_jac(s.d + 6, J);
+        inv3(J, s.D.e);
+    } else if (t == 64) {
+        double Nx[6], Mx[6], A[4];
+        s2_minus(x.g, xp.g, s.d + 21);
+        s2_Nx(x.g, Nx);
+        s2_Mx_res(xp.g, s.d + 21, Mx);
+        mm<2, 3, 2>(Nx, Mx, A);
+        const double id = 1.0 / (A[0] * A[3] - A[1] * A[2]);
+        s.D.g[0] = A[3] * id; s.D.g[1] = -A[1] * id;
+        s.D.g[2] = -A[2] * id; s.D.g[3] = A[0] * id;
+    } else if (t >= 96 && t < 111) {
+        const int u = t - 96;
+        const double* xs = reinterpret_cast<const double*>(&x);
+        const double* ps = reinterpret_cast<const double*>(&xp);
+        s.d[lin_delta_idx(u)] = xs[lin_state_off(u)] - ps[lin_state_off(u)];
+    }
+    __syncthreads();
+    if (t < 23) s.dp[t] = bd_row(s.D, s.d, 1, t, 0);
+    bd_sandwich(s.D, f->P, s.T, s.M);  // M = D P D^T
+    // S = I + Hm M_EE as [S | I];  y = Hm d'_E - bm
+    const int w = 2 * nj;
+    for (int e = t; e < nj * w; e += blockDim.x) {
+        const int i = e / w, j = e - i * w;
+        double v;
+        if (j < nj) {
+            double a = 0.0;
+            for (int k = 0; k < nj; ++k) a = fma(Hm[i * 12 + k], s.M[k * 23 + j], a);
+            v = (i == j ? 1.0 : 0.0) + a;
+        } else {
+            v = (j - nj == i) ? 1.0 : 0.0;
+        }
+        s.aug[e] = v;
+    }
+    if (t >= 224 && t - 224 < nj) {
+        const int i = t - 224;
+        double a = 0.0;
+        for (int k = 0; k < nj; ++k) a = fma(Hm[i * 12 + k], s.dp[k], a);
+        s.y[i] = a - bm[i];
+    }
+    __syncthreads();
+    gauss_jordan(s, nj);
+    // K = M_E S^-1
+    for (int e = t; e < 23 * nj; e += blockDim.x) {
+        const int i = e / nj, j = e - i * nj;
+        double a = 0.0;
+        for (int k = 0; k < nj; ++k) a = fma(s.M[i * 23 + k], s.aug[k * w + nj + j], a);
+        s.K[i * 12 + j] = a;
+    }
+    __syncthreads();
+    if (t < 23) {
+        double a = 0.0;
+        for (int j = 0; j < nj; ++j) a = fma(s.K[t * 12 + j], s.y[j], a);
+        s.step[t] = a - s.dp[t];
+    }
+    __syncthreads();
+    // x = x boxplus step, again one warp per transcendental piece
+    DState& xm = f->x;
+    if (t == 0) {
+        rot_plus(xm.rot, s.step + 3);
+    } else if (t == 32) {
+        rot_plus(xm.rot_ext, s.step + 6);
+    } else if (t == 64) {
+        s2_plus(xm.g, s.step + 21);
+    } else if (t >= 96 && t < 111) {
+        const int u = t - 96;
+        double* xs = reinterpret_cast<double*>(&xm);
+        xs[lin_state_off(u)] = xs[lin_state_off(u)] + s.step[lin_delta_idx(u)];
+    } else if (t == 128) {
+        double mx = s.step[0];
+        for (int i = 1; i < 23; ++i) mx = fmax(mx, s.step[i]);
+        f->iters = f->iters + 1;
+        if (mx < eps) f->converged = 1;
+    }
+    for (int e = t; e < 529; e += blockDim.x) f->Hinv[e] = s.M[e];
+    for (int e = t; e < 23 * 12; e += blockDim.x) f->K[e] = s.K[e];
+    if (t < 23) f->delta[t] = s.step[t];
+}
+
+// ---------------------------------------------------------------- kernels
+// IESKF::update entry (ieskf.cpp:125-130): predict_x = x, delta = 0.
+__global__ void k_update_begin(DFilter* f) {
+    const int t = threadIdx.x;
+    const double* xs = reinterpret_cast<const double*>(&f->x);
+    double* ps = reinterpret_cast<double*>(&f->x_pred);
+    for (int e = t; e < (int)(sizeof(DState) / sizeof(double)); e += blockDim.x) ps[e] = xs[e];
+    if (t < 23) f->delta[t] = 0.0;
+    if (t == 0) {
+        f->converged = 0;
+        f->iters = 0;
+        f->effect_num = 0;
+        f->no_effect = 0;
+    }
+}
+
+// func_ (sharedUpdateFunc) over all downsampled points, then -- in the last
+// CTA to finish -- the filter step of this iteration.
+template <int NJ>
+__global__ void __launch_bounds__(kIekfThreads) k_residual(DFilter* f, DScan s, DMap m, double eps, int do_step) {
+    using R = Red<NJ>;
+    constexpr int kWarps = kIekfThreads / 32;
+    static_assert(sizeof(double) * kWarps * R::NP <= sizeof(IekfSm), "partials fit in the step scratch");
+    __shared__ __align__(16) unsigned char smem_raw[sizeof(IekfSm)];
+    __shared__ double s_rwl[9], s_pwl[3], s_rot[9], s_rext[9], s_pext[3], s_prr[9], s_ppp[9];
+    __shared__ double sH[144], sb[12];
+    __shared__ int s_last;
+    if (f->converged) return;  // written by the previous launch; uniform
+    const int n = *s.d_n_down;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {
+        const DState& x = f->x;
+        mm<3, 3, 3>(x.rot, x.rot_ext, s_rwl);
+        double rp[3];
+        m3v(x.rot, x.pos_ext, rp);
+        for (int a = 0; a < 3; ++a) s_pwl[a] = rp[a] + x.pos[a];
+    } else if (t >= 32 && t < 41) {
+        const int a = t - 32;
+        s_rot[a] = f->x.rot[a];
+        s_rext[a] = f->x.rot_ext[a];
+        s_prr[a] = f->P[(3 + a / 3) * 23 + 3 + a % 3];
+        s_ppp[a] = f->P[(a / 3) * 23 + a % 3];
+        if (a < 3) s_pext[a] = f->x.pos_ext[a];
+    }
+    __syncthreads();
+    double acc[R::NP];
+#pragma unroll
+    for (int k = 0; k < R::NP; ++k) acc[k] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + t; i < n; i += gridDim.x * blockDim.x)
+        residual_point<NJ>(i, s, m, s_rwl, s_pwl, s_rot, s_rext, s_pext, s_prr, s_ppp, acc);
+    // warp -> block -> grid, each in a fixed order
+    double* s_red = reinterpret_cast<double*>(smem_raw);
+#pragma unroll
+    for (int c = 0; c < R::NP / 32; ++c) {
+        const double v = warp_reduce_scatter32(acc + 32 * c);
+        s_red[warp * R::NP + 32 * c + lane] = v;
+    }
+    __syncthreads();
+    for (int k = t; k < R::NV; k += blockDim.x) {
+        double v = s_red[k];
+        for (int w = 1; w < kWarps; ++w) v = v + s_red[w * R::NP + k];
+        s.partials[blockIdx.x * kPartStride2 + k] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) {
+        const unsigned int ticket = atomicAdd(s.done_ctr, 1u);
+        s_last = (ticket == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int k = t; k < R::NV; k += blockDim.x) {
+        double v = __ldcg(s.partials + k);
+        for (int b = 1; b < (int)gridDim.x; ++b) v = v + __ldcg(s.partials + b * kPartStride2 + k);
+        s_red[k] = v;
+    }
+    __syncthreads();
+    for (int e = t; e < 144; e += blockDim.x) {
+        const int r = e / 12, c = e % 12;
+        double v = 0.0;
+        if (r < NJ && c < NJ) {
+            const int a = r < c ? r : c, b = r < c ? c : r;
+            v = s_red[a * NJ - a * (a - 1) / 2 + (b - a)];
+        }
+        sH[e] = v;
+        f->Hm[e] = v;
+    }
+    if (t < 12) {
+        sb[t] = t < NJ ? s_red[R::NH + t] : 0.0;
+        f->bm[t] = sb[t];
+    }
+    if (t == 0) {
+        const int eff = (int)s_red[R::NH + NJ];
+        f->effect_num = eff;
+        if (eff < 1) f->no_effect = 1;
+        *s.done_ctr = 0;
+    }
+    __syncthreads();
+    if (do_step) iekf_step(f, *reinterpret_cast<IekfSm*>(smem_raw), sH, sb, NJ, eps);
+}
+
+// P = L H^-1 L^T (ieskf.cpp:149-155) with H^-1 = M - K Hm (E^T M) of the last
+// iteration.  P is not exactly symmetric after the reference's own recursion,
+// and neither is M: the row block E^T M (not the transposed column block)
+// keeps this the exact inverse of the nonsymmetric H.
+__global__ void k_update_end(DFilter* f, int nj) {
+    __shared__ double sM[529], sT[529], sKH[23 * 12];
+    __shared__ BlkDiag L;
+    const int t = threadIdx.x;
+    if (f->iters == 0) return;  // uniform
+    for (int e = t; e < 529; e += blockDim.x) sM[e] = f->Hinv[e];
+    const double* d = f->delta;
+    if (t == 0) {
+        so3_right_jac(d + 3, L.r);
+    } else if (t == 32) {
+        so3_right_jac(d + 6, L.e);
+    } else if (t == 64) {
+        double Nx[6], Mx[6];
+        s2_Nx(f->x.g, Nx);
+        s2_Mx_res(f->x_pred.g, d + 21, Mx);
+        mm<2, 3, 2>(Nx, Mx, L.g);
+    }
+    for (int e = t; e < 23 * nj; e += blockDim.x) {
+        const int i = e / nj, j = e - i * nj;
+        double a = 0.0;
+        for (int k = 0; k < nj; ++k) a = fma(f->K[i * 12 + k], f->Hm[k * 12 + j], a);
+        sKH[i * 12 + j] = a;
+    }
+    __syncthreads();
+    for (int e = t; e < 529; e += blockDim.x) {
+        const int i = e / 23, j = e - i * 23;
+        double a = 0.0;
+        for (int k = 0; k < nj; ++k) a = fma(sKH[i * 12 + k], sM[k * 23 + j], a);
+        sT[e] = sM[e] - a;
+    }
+    __syncthreads();
+    bd_sandwich(L, sT, sM, sT);
+    for (int e = t; e < 529; e += blockDim.x) f->P[e] = sT[e];
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_update_begin(DFilter* f, cudaStream_t st) {
+    VMP_NOTE_LAUNCH();
+    k_update_begin<<<1, 64, 0, st>>>(f);
+}
+void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
+                          cudaStream_t st, int do_step) {
+    (void)n_max;
+    VMP_NOTE_LAUNCH();
+    if (estimate_ext)
+        k_residual<12><<<s.res_blocks, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
+    else
+        k_residual<6><<<s.res_blocks, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
+}
+void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st) {
+    VMP_NOTE_LAUNCH();
+    k_update_end<<<1, 256, 0, st>>>(f, estimate_ext ? 12 : 6);
+}
+
+}  // namespace vmp

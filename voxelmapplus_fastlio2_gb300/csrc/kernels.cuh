@@ -39,7 +39,7 @@ struct DScan {
     DPose* poses;          // [max_imu + 2]
     DStep* steps;          // [max_imu + 2] per-step terms of the predict chain
     // reduction partials
-    double* partials;      // [res_blocks * 80]
+    double* partials;      // [res_blocks * 160]
     unsigned int* done_ctr;
     int max_pts;
     int max_imu;
@@ -49,7 +49,6 @@ struct DScan {
 // ---- k_filter.cu
 void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& cfg, double t_end,
                      cudaStream_t st);
-void launch_predict_chain(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st);
 void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st);
 // ---- k_predict.cu
 void launch_predict_chain2(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st);
@@ -57,7 +56,7 @@ void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro
 void launch_update_begin(DFilter* f, cudaStream_t st);
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step = 1);
-void launch_update_end(DFilter* f, cudaStream_t st);
+void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st);
 
 // ---- k_points.cu
 void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st);

@@ -798,7 +798,7 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
         s->pend(VMP_PROF_RESIDUAL, 1);
     }
     s->pbeg();
-    launch_update_end(s->f, st);
+    launch_update_end(s->f, cfg.estimate_ext, st);
     s->pend(VMP_PROF_UPDATE_OTHER, -1);
     s->pbeg();
     launch_map_batch(s->f, s->s, n, false, cfg.ranging_cov, s->sin_deg, st);
@@ -1026,7 +1026,7 @@ vmp_status vmp_ieskf_update(vmp_stream_t s, const float* pts_l, int n, int* iter
     launch_update_begin(s->f, s->st);
     for (int it = 0; it < s->cfg.ieskf_max_iter; ++it)
         launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 1);
-    launch_update_end(s->f, s->st);
+    launch_update_end(s->f, s->cfg.estimate_ext, s->st);
     vmp_status v = finish_result(s, n, nullptr);
     if (v != VMP_OK) return v;
     if (iters) *iters = s->h_res->iters;
