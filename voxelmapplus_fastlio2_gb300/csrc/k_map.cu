@@ -254,10 +254,6 @@ __global__ void k_rollback_counters(DMap m) {
 }
 
 // ---------------------------------------------------------------- segments
-struct SegShared {
-    double stage[kSegThreads / 32][32][36];
-};
-
 __device__ inline double* slab_pt(const DMap& m, const int* chunks, int j) {
     return m.slab + ((size_t)chunks[j / kChunkPts] * kChunkPts + (j % kChunkPts)) * kSlabStride;
 }
@@ -338,96 +334,66 @@ __device__ void plane_cov_term(const double* p, const double* cov, const double*
     mm<6, 3, 6>(T1, JT, out36);
 }
 
-// Warp-cooperative updatePlane.  State lives in lane 0's registers (passed by
-// reference; only lane 0's copies are authoritative); cov lives in `cov`
-// (shared memory of the warp).  Points: from the slab (chunks) or from the
-// batch segment (sv/bpts/bcov) when from_batch.
-__device__ void warp_update_plane(const DMap& m, uint32_t& flags, int n, const double* mean, const double* ppt,
-                                  double* norm, double* center, double* cov, const int* chunks, int npts,
-                                  bool from_batch, const uint32_t* sv, int seg_b, const double* bpts,
-                                  const double* bcov, double (*stage)[36]) {
-    const int lane = threadIdx.x & 31;
-    int go = 0;
-    double ev[3], evecs[9], mn[3];
-    if (lane == 0) {
-        if (n >= m.update_thresh) {
-            flags |= F_INIT;
-            double C[9];
-            for (int k = 0; k < 3; ++k)
-                for (int l = 0; l < 3; ++l) C[k * 3 + l] = ppt[k * 3 + l] / (double)n - mean[k] * mean[l];
-            eig_sym3(C, ev, evecs);
-            if (ev[0] > m.plane_thresh) {
-                flags &= ~F_PLANE;
-            } else {
-                flags |= F_PLANE;
-                go = 1;
-            }
-        }
-        for (int k = 0; k < 3; ++k) mn[k] = mean[k];
-    }
-    go = __shfl_sync(0xffffffffu, go, 0);
-    if (!go) return;
-    for (int k = 0; k < 3; ++k) {
-        ev[k] = __shfl_sync(0xffffffffu, ev[k], 0);
-        mn[k] = __shfl_sync(0xffffffffu, mn[k], 0);
-    }
-    for (int k = 0; k < 9; ++k) evecs[k] = __shfl_sync(0xffffffffu, evecs[k], 0);
-    n = __shfl_sync(0xffffffffu, n, 0);
-    for (int base = 0; base < npts; base += 32) {
-        int j = base + lane;
-        if (j < npts) {
-            const double* src;
-            double pc[12];
-            if (from_batch) {
-                uint32_t i = sv[seg_b + j];
-                for (int k = 0; k < 3; ++k) pc[k] = bpts[i * 3 + k];
-                for (int k = 0; k < 9; ++k) pc[3 + k] = bcov[i * 9 + k];
-                src = pc;
-            } else {
-                src = slab_pt(m, chunks, j);
-            }
-            plane_cov_term(src, src + 3, mn, n, ev, evecs, stage[lane]);
-        }
-        __syncwarp();
-        const int cnt = min(32, npts - base);
-        for (int e = lane; e < 36; e += 32) {
-            double s = cov[e];
-            for (int q = 0; q < cnt; ++q) s = s + stage[q][e];
-            cov[e] = s;
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        double pn[3] = {evecs[0], evecs[3], evecs[6]};
-        double axis_distance = -dot3(mean, pn);
-        if (axis_distance < 0.0) { pn[0] = -pn[0]; pn[1] = -pn[1]; pn[2] = -pn[2]; }
-        for (int k = 0; k < 3; ++k) { norm[k] = pn[k]; center[k] = mean[k]; }
-    }
-    __syncwarp();
-}
+// ---------------------------------------------------------------- voxel state machine
+// VoxelGrid::pushPoint / addPoint / updatePlane (voxel_map.cpp:29-136) for
+// every touched voxel of a batch, in three kernels:
+//   k_seg_chain  one warp per voxel: the points in order -- addToPlane with
+//                the three coordinates of the mean and the nine of ppt on
+//                separate lanes, slab appends, the integer state machine --
+//                recording a snapshot (n, mean, ppt, slab length) at every
+//                updatePlane call that reaches the eigen decomposition;
+//   k_refit_eig  one thread per snapshot: the 3x3 eigen decomposition and the
+//                plane test, all refits of the batch at once;
+//   k_seg_cov    one warp per voxel with snapshots: the plane covariance
+//                terms of each plane refit (lanes over points) summed in
+//                point order onto the voxel's cov, the normal and centre of
+//                the last plane refit, and the merge calls of the points that
+//                reached the voxel after it froze.
+// Nothing in the state machine reads a refit's plane decision before the
+// voxel freezes (the branches test is_init and update_enable only, and
+// is_init follows from the count), so splitting the refits out keeps the
+// reference's sequence exactly.
+struct RefitSnap {
+    int n;           // point count at the refit
+    int npts;        // points the covariance terms run over
+    int from_batch;  // build: the batch segment's points, else the slab prefix
+    int plane;       // eigen test result
+    double mean[3];
+    double ppt[9];
+    double ev[3];
+    double evecs[9];
+};
+struct CovSeg {
+    uint32_t seg;
+    int nref;    // snapshots at seg_start[seg] .. + nref
+    int mstart;  // first point index of the merge calls (seg_end: none)
+    int pad;
+    int32_t chunks[kMaxChunks];  // the slab before a freeze released it
+};
 
-__device__ inline void add_to_plane(double* mean, double* ppt, int& n, const double* p) {
-    for (int k = 0; k < 3; ++k) mean[k] = mean[k] + (p[k] - mean[k]) / ((double)n + 1.0);
-    for (int k = 0; k < 3; ++k)
-        for (int l = 0; l < 3; ++l) ppt[k * 3 + l] = ppt[k * 3 + l] + p[k] * p[l];
-    n += 1;
-}
-
-__device__ inline bool slab_append(const DMap& m, int* chunks, int& nslab, const double* p, const double* c) {
-    int ci = nslab / kChunkPts;
+__device__ inline bool warp_slab_append(const DMap& m, int* chunks, int& nslab, const double* p, const double* c,
+                                        int lane) {
+    const int ci = nslab / kChunkPts;
     if (ci >= kMaxChunks) return false;
     if (nslab % kChunkPts == 0) {
-        int top = atomicSub(&m.cnt->chunk_free_top, 1);
-        if (top <= 0) {
-            atomicAdd(&m.cnt->chunk_free_top, 1);
-            set_error(m.cnt, E_CHUNKS);
-            return false;
+        int id = -1;
+        if (lane == 0) {
+            const int top = atomicSub(&m.cnt->chunk_free_top, 1);
+            if (top <= 0) {
+                atomicAdd(&m.cnt->chunk_free_top, 1);
+                set_error(m.cnt, E_CHUNKS);
+            } else {
+                id = m.chunk_free[top - 1];
+                chunks[ci] = id;
+            }
         }
-        chunks[ci] = m.chunk_free[top - 1];
+        id = __shfl_sync(0xffffffffu, id, 0);
+        if (id < 0) return false;
     }
+    __syncwarp();
     double* d = slab_pt(m, chunks, nslab);
-    for (int k = 0; k < 3; ++k) d[k] = p[k];
-    for (int k = 0; k < 9; ++k) d[3 + k] = c[k];
+    if (lane < 3) d[lane] = p[lane];
+    else if (lane < 12) d[lane] = c[lane - 3];
     nslab++;
     return true;
 }
@@ -444,111 +410,246 @@ __device__ inline void slab_release(const DMap& m, int* chunks, int& nslab) {
     nslab = 0;
 }
 
-__global__ void __launch_bounds__(kSegThreads) k_segments(DMap m, const uint32_t* __restrict__ seg_start,
-                                                          const uint32_t* __restrict__ seg_end,
-                                                          const uint32_t* __restrict__ seg_rec, const int* d_n_seg,
-                                                          const uint32_t* __restrict__ sv,
-                                                          const double* __restrict__ bpts,
-                                                          const double* __restrict__ bcov, uint32_t* ev_rec,
-                                                          int build) {
-    __shared__ SegShared sh;
-    __shared__ double s_cov[kSegThreads / 32][36];
+struct SegScratch {
+    RefitSnap* snaps;     // [max_batch], indexed like the sorted batch
+    uint32_t* refit_list; // [max_batch] snapshot indices
+    CovSeg* covsegs;      // [max_batch]
+    int* d_n_refit;
+    int* d_n_covseg;
+};
+
+__global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_t* __restrict__ seg_start,
+                                                           const uint32_t* __restrict__ seg_end,
+                                                           const uint32_t* __restrict__ seg_rec, const int* d_n_seg,
+                                                           const uint32_t* __restrict__ sv,
+                                                           const double* __restrict__ bpts,
+                                                           const double* __restrict__ bcov, uint32_t* ev_rec,
+                                                           SegScratch ss, int build) {
     __shared__ int s_chunks[kSegThreads / 32][kMaxChunks];
+    __shared__ int s_saved[kSegThreads / 32][kMaxChunks];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int nseg = *d_n_seg;
     const unsigned long long base = m.cnt->batch_base;
-    double* cov = s_cov[wib];
     int* chunks = s_chunks[wib];
+    int* saved = s_saved[wib];
     for (int sidx = gw; sidx < nseg; sidx += nw) {
         const uint32_t rec = seg_rec[sidx];
         const int b = (int)seg_start[sidx], e = (int)seg_end[sidx];
         RecHot& H = m.hot[rec];
         RecCold& Cc = m.cold[rec];
-        // lane 0 state
-        uint32_t flags = 0;
-        int n = 0, newly = 0, nslab = 0;
-        double mean[3] = {0, 0, 0}, ppt[9], norm[3] = {0, 0, 0}, center[3] = {0, 0, 0};
-        for (int k = 0; k < 9; ++k) ppt[k] = 0.0;
-        if (lane == 0) {
-            flags = H.flags; n = H.n; newly = Cc.newly; nslab = Cc.nslab;
-            for (int k = 0; k < 3; ++k) { mean[k] = H.mean[k]; norm[k] = H.norm[k]; center[k] = Cc.center[k]; }
-            for (int k = 0; k < 9; ++k) ppt[k] = Cc.ppt[k];
-        }
-        for (int k = lane; k < 36; k += 32) cov[k] = Cc.cov[k];
+        // integer state on every lane; mean[lane] (lane < 3), ppt[lane] (lane < 9)
+        uint32_t flags = H.flags;
+        int n = H.n, newly = Cc.newly, nslab = Cc.nslab;
+        double mean_l = lane < 3 ? H.mean[lane] : 0.0;
+        double ppt_l = lane < 9 ? Cc.ppt[lane] : 0.0;
         if (lane < kMaxChunks) chunks[lane] = Cc.chunks[lane];
         __syncwarp();
+        int nref = 0, mstart = e;
+        bool have_saved = false;
+        // updatePlane call: a snapshot when it reaches the eigen decomposition
+        auto refit = [&](int npts, int from_batch) {
+            if (n < m.update_thresh) return;
+            flags |= F_INIT;
+            RefitSnap& sn = ss.snaps[b + nref];
+            if (lane < 3) sn.mean[lane] = mean_l;
+            if (lane < 9) sn.ppt[lane] = ppt_l;
+            if (lane == 0) {
+                sn.n = n;
+                sn.npts = npts;
+                sn.from_batch = from_batch;
+                const int k = atomicAdd(ss.d_n_refit, 1);
+                ss.refit_list[k] = (uint32_t)(b + nref);
+            }
+            ++nref;
+        };
+        auto add_point = [&](const double* p) {
+            if (lane < 3) mean_l = mean_l + (p[lane] - mean_l) / ((double)n + 1.0);
+            if (lane < 9) ppt_l = ppt_l + p[lane / 3] * p[lane % 3];
+            n += 1;
+        };
         if (build) {
             // VoxelMap::build: addPoint for every point, one updatePlane at the end.
             const int cnt = e - b;
-            bool store = false;
-            if (lane == 0) {
-                store = (nslab + cnt) < m.max_thresh && !(flags & F_DROPPED);
-                for (int j = b; j < e; ++j) {
-                    uint32_t i = sv[j];
-                    const double* p = bpts + (size_t)i * 3;
-                    add_to_plane(mean, ppt, n, p);
-                    if (store) slab_append(m, chunks, nslab, p, bcov + (size_t)i * 9);
-                }
-                if (!store) flags |= F_DROPPED;
-            }
-            __syncwarp();
-            const int n_b = __shfl_sync(0xffffffffu, n, 0);
-            warp_update_plane(m, flags, n_b, mean, ppt, norm, center, cov, chunks, cnt, true, sv, b, bpts, bcov,
-                              sh.stage[wib]);
-            if (lane == 0 && (flags & F_DROPPED)) slab_release(m, chunks, nslab);
-        } else {
+            const bool store = (nslab + cnt) < m.max_thresh && !(flags & F_DROPPED);
             for (int j = b; j < e; ++j) {
                 const uint32_t i = sv[j];
-                const double* p = bpts + (size_t)i * 3;
-                const double* c = bcov + (size_t)i * 9;
-                int act = 0;  // bit0 refit, bit1 freeze, bit2 reset newly_add_point after the refit
-                if (lane == 0) {
-                    if (!(flags & F_INIT)) {
-                        add_to_plane(mean, ppt, n, p);
-                        if (!(flags & F_DROPPED)) slab_append(m, chunks, nslab, p, c);
-                        act = 1;
-                    } else if (flags & F_UPDATE) {
-                        add_to_plane(mean, ppt, n, p);
-                        if (!(flags & F_DROPPED)) slab_append(m, chunks, nslab, p, c);
-                        newly++;
-                        if (newly >= m.update_thresh) act |= 1 | 4;
-                        int size_after = (flags & F_DROPPED) ? n : nslab;
-                        if (size_after >= m.max_thresh) act |= 2;
-                    } else if (flags & F_PLANE) {
-                        ev_rec[i] = rec;  // merge() call at this point
-                    }
-                }
-                act = __shfl_sync(0xffffffffu, act, 0);
-                if (act & 1) {
-                    const int n_b = __shfl_sync(0xffffffffu, n, 0);
-                    const int np_b = __shfl_sync(0xffffffffu, nslab, 0);
-                    __syncwarp();
-                    warp_update_plane(m, flags, n_b, mean, ppt, norm, center, cov, chunks, np_b, false, sv, b, bpts,
-                                      bcov, sh.stage[wib]);
-                    if (lane == 0 && (act & 4)) newly = 0;
-                }
-                if ((act & 2) && lane == 0) {
-                    flags &= ~F_UPDATE;
-                    flags &= ~F_DROPPED;
-                    slab_release(m, chunks, nslab);
-                    Cc.freeze_g = base + i;
-                }
+                const double p[3] = {bpts[(size_t)i * 3], bpts[(size_t)i * 3 + 1], bpts[(size_t)i * 3 + 2]};
+                add_point(p);
+                if (store) warp_slab_append(m, chunks, nslab, p, bcov + (size_t)i * 9, lane);
+            }
+            if (!store) flags |= F_DROPPED;
+            refit(cnt, 1);
+            if (flags & F_DROPPED) {
+                if (lane == 0) slab_release(m, chunks, nslab);
+                nslab = 0;
                 __syncwarp();
             }
+        } else {
+            for (int j = b; j < e; ++j) {
+                const bool init = (flags & F_INIT) != 0;
+                if (init && !(flags & F_UPDATE)) {
+                    // frozen: the remaining points only call merge() (if plane)
+                    mstart = j;
+                    break;
+                }
+                const uint32_t i = sv[j];
+                const double p[3] = {bpts[(size_t)i * 3], bpts[(size_t)i * 3 + 1], bpts[(size_t)i * 3 + 2]};
+                const double* c = bcov + (size_t)i * 9;
+                add_point(p);
+                if (!(flags & F_DROPPED)) warp_slab_append(m, chunks, nslab, p, c, lane);
+                if (!init) {
+                    refit(nslab, 0);
+                } else {
+                    newly++;
+                    if (newly >= m.update_thresh) {
+                        refit(nslab, 0);
+                        newly = 0;
+                    }
+                    const int size_after = (flags & F_DROPPED) ? n : nslab;
+                    if (size_after >= m.max_thresh) {
+                        flags &= ~F_UPDATE;
+                        flags &= ~F_DROPPED;
+                        if (nref > 0 && !have_saved) {
+                            if (lane < kMaxChunks) saved[lane] = chunks[lane];
+                            have_saved = true;
+                        }
+                        __syncwarp();
+                        if (lane == 0) {
+                            slab_release(m, chunks, nslab);
+                            Cc.freeze_g = base + i;
+                        }
+                        nslab = 0;
+                        __syncwarp();
+                    }
+                }
+            }
         }
-        __syncwarp();
+        if (nref > 0) {
+            int k = 0;
+            if (lane == 0) k = atomicAdd(ss.d_n_covseg, 1);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            CovSeg& cs = ss.covsegs[k];
+            if (lane == 0) { cs.seg = (uint32_t)sidx; cs.nref = nref; cs.mstart = mstart; }
+            if (lane < kMaxChunks) cs.chunks[lane] = have_saved ? saved[lane] : chunks[lane];
+        } else if (flags & F_PLANE) {
+            for (int j = mstart + lane; j < e; j += 32) ev_rec[sv[j]] = rec;  // merge() calls
+        }
         if (lane == 0) {
-            H.flags = flags; H.n = n;
-            for (int k = 0; k < 3; ++k) { H.mean[k] = mean[k]; H.norm[k] = norm[k]; Cc.center[k] = center[k]; }
-            for (int k = 0; k < 9; ++k) Cc.ppt[k] = ppt[k];
+            H.flags = flags;
+            H.n = n;
             Cc.newly = newly;
             Cc.nslab = nslab;
             Cc.stamp = base + sv[e - 1];
         }
-        for (int k = lane; k < 36; k += 32) Cc.cov[k] = cov[k];
+        if (lane < 3) H.mean[lane] = mean_l;
+        if (lane < 9) Cc.ppt[lane] = ppt_l;
         if (lane < kMaxChunks) Cc.chunks[lane] = chunks[lane];
+        __syncwarp();
+    }
+}
+
+// Eigen decomposition of every refit snapshot (updatePlane, voxel_map.cpp:97-113).
+__global__ void k_refit_eig(DMap m, SegScratch ss) {
+    const int nr = *ss.d_n_refit;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nr; t += gridDim.x * blockDim.x) {
+        RefitSnap& sn = ss.snaps[ss.refit_list[t]];
+        const double dn = (double)sn.n;
+        double C[9], ev[3], evecs[9];
+        for (int k = 0; k < 3; ++k)
+            for (int l = 0; l < 3; ++l) C[k * 3 + l] = sn.ppt[k * 3 + l] / dn - sn.mean[k] * sn.mean[l];
+        eig_sym3(C, ev, evecs);
+        for (int k = 0; k < 3; ++k) sn.ev[k] = ev[k];
+        for (int k = 0; k < 9; ++k) sn.evecs[k] = evecs[k];
+        sn.plane = ev[0] > m.plane_thresh ? 0 : 1;
+    }
+}
+
+struct CovShared {
+    double stage[kSegThreads / 32][32][36];
+    double cov[kSegThreads / 32][36];
+    int chunks[kSegThreads / 32][kMaxChunks];
+};
+
+// Plane covariance accumulation, normal and centre, merge calls.
+__global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t* __restrict__ seg_start,
+                                                         const uint32_t* __restrict__ seg_end,
+                                                         const uint32_t* __restrict__ seg_rec,
+                                                         const uint32_t* __restrict__ sv,
+                                                         const double* __restrict__ bpts,
+                                                         const double* __restrict__ bcov, uint32_t* ev_rec,
+                                                         SegScratch ss) {
+    __shared__ CovShared sh;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int nc = *ss.d_n_covseg;
+    double* cov = sh.cov[wib];
+    int* chunks = sh.chunks[wib];
+    double (*stage)[36] = sh.stage[wib];
+    for (int li = gw; li < nc; li += nw) {
+        const CovSeg& cs = ss.covsegs[li];
+        const uint32_t sidx = cs.seg;
+        const int nref = cs.nref, mstart = cs.mstart;
+        const uint32_t rec = seg_rec[sidx];
+        const int b = (int)seg_start[sidx], e = (int)seg_end[sidx];
+        RecHot& H = m.hot[rec];
+        RecCold& Cc = m.cold[rec];
+        uint32_t flags = H.flags;
+        double norm[3] = {H.norm[0], H.norm[1], H.norm[2]};
+        double center[3] = {Cc.center[0], Cc.center[1], Cc.center[2]};
+        for (int k = lane; k < 36; k += 32) cov[k] = Cc.cov[k];
+        if (lane < kMaxChunks) chunks[lane] = cs.chunks[lane];
+        __syncwarp();
+        for (int r = 0; r < nref; ++r) {
+            const RefitSnap& sn = ss.snaps[b + r];
+            if (!sn.plane) {
+                flags &= ~F_PLANE;
+                continue;
+            }
+            flags |= F_PLANE;
+            const int n = sn.n, npts = sn.npts;
+            const bool from_batch = sn.from_batch != 0;
+            double mn[3], ev[3], evecs[9];
+            for (int k = 0; k < 3; ++k) { mn[k] = sn.mean[k]; ev[k] = sn.ev[k]; }
+            for (int k = 0; k < 9; ++k) evecs[k] = sn.evecs[k];
+            for (int base = 0; base < npts; base += 32) {
+                const int j = base + lane;
+                if (j < npts) {
+                    const double* src;
+                    double pc[12];
+                    if (from_batch) {
+                        const uint32_t i = sv[b + j];
+                        for (int k = 0; k < 3; ++k) pc[k] = bpts[(size_t)i * 3 + k];
+                        for (int k = 0; k < 9; ++k) pc[3 + k] = bcov[(size_t)i * 9 + k];
+                        src = pc;
+                    } else {
+                        src = slab_pt(m, chunks, j);
+                    }
+                    plane_cov_term(src, src + 3, mn, n, ev, evecs, stage[lane]);
+                }
+                __syncwarp();
+                const int cnt = min(32, npts - base);
+                for (int q = lane; q < 36; q += 32) {
+                    double acc = cov[q];
+                    for (int u = 0; u < cnt; ++u) acc = acc + stage[u][q];
+                    cov[q] = acc;
+                }
+                __syncwarp();
+            }
+            double pn[3] = {evecs[0], evecs[3], evecs[6]};
+            const double axis_distance = -dot3(mn, pn);
+            if (axis_distance < 0.0) { pn[0] = -pn[0]; pn[1] = -pn[1]; pn[2] = -pn[2]; }
+            for (int k = 0; k < 3; ++k) { norm[k] = pn[k]; center[k] = mn[k]; }
+        }
+        if (flags & F_PLANE)
+            for (int j = mstart + lane; j < e; j += 32) ev_rec[sv[j]] = rec;  // merge() calls
+        if (lane == 0) {
+            H.flags = flags;
+            for (int k = 0; k < 3; ++k) { H.norm[k] = norm[k]; Cc.center[k] = center[k]; }
+        }
+        for (int k = lane; k < 36; k += 32) Cc.cov[k] = cov[k];
         __syncwarp();
     }
 }
@@ -665,8 +766,17 @@ void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double*
     int sg = (n_max + (kSegThreads / 32) - 1) / (kSegThreads / 32);
     if (sg > 152 * 16) sg = 152 * 16;
     if (sg < 1) sg = 1;
-    VMP_NOTE_LAUNCH(); k_segments<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg,
-                                                              ms.sv, bpts, bcov, ms.ev_rec, build ? 1 : 0);
+    SegScratch ss{static_cast<RefitSnap*>(ms.seg_snaps), ms.refit_list, static_cast<CovSeg*>(ms.covsegs),
+                  ms.d_scratch_int + 5, ms.d_scratch_int + 6};
+    cudaMemsetAsync(ms.d_scratch_int + 5, 0, 2 * sizeof(int), st);
+    VMP_NOTE_LAUNCH();
+    k_seg_chain<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg, ms.sv, bpts, bcov,
+                                            ms.ev_rec, ss, build ? 1 : 0);
+    // one warp per block so that the refits spread over all SMs
+    VMP_NOTE_LAUNCH();
+    k_refit_eig<<<152 * 8, 32, 0, st>>>(m, ss);
+    VMP_NOTE_LAUNCH();
+    k_seg_cov<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.sv, bpts, bcov, ms.ev_rec, ss);
 }
 // Phase B2: merges, LRU queue, evictions, counters.
 void launch_map_finish(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st) {
@@ -809,6 +919,9 @@ cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
     for (auto pp : u32s)
         if ((e = cudaMalloc(pp, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
     if ((e = merge_scratch_alloc(&ms.merge, max_batch, rec_pool)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&ms.seg_snaps, sizeof(RefitSnap) * nb)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&ms.covsegs, sizeof(CovSeg) * nb)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&ms.refit_list, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
     ms.merge_mode = 0;
     ms.merge_rounds = 0;
     ms.merge_d2h = 0;
@@ -827,6 +940,9 @@ void map_scratch_free(MapScratch& ms) {
                         ms.ev_rec, ms.ev_list, ms.last_touch, ms.victims, ms.new_pos};
     for (auto p : u32s) cudaFree(p);
     merge_scratch_free(ms.merge);
+    cudaFree(ms.seg_snaps);
+    cudaFree(ms.covsegs);
+    cudaFree(ms.refit_list);
     cudaFree(ms.d_scratch_int);
     sort_scratch_free(ms.sort);
     scan_scratch_free(ms.scan);

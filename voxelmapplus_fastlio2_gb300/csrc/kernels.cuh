@@ -87,6 +87,9 @@ struct MapScratch {
     uint32_t* victims;    // [max_batch]
     uint32_t* new_pos;    // [max_batch] point index of the j-th creation
     void* merge;          // MergeScratch (k_merge.cu)
+    void* seg_snaps;      // [max_batch] refit snapshots (k_map.cu)
+    void* covsegs;        // [max_batch] voxels with refits (k_map.cu)
+    uint32_t* refit_list; // [max_batch]
     int merge_mode;
     int merge_rounds;
     long long merge_d2h;  // bytes read back by the merge rounds (cumulative)
@@ -95,7 +98,7 @@ struct MapScratch {
     int* d_n_seg;
     int* d_n_ev;
     int* d_n_touch;
-    int* d_scratch_int;   // [16]
+    int* d_scratch_int;   // [32]: batch counters; [5], [6] refit / voxel list lengths
     int max_batch;
     SortScratch sort;
     ScanScratch scan;
