@@ -752,7 +752,9 @@ void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
 void launch_map_segments(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
     const int g = grid_for_map(n_max);
     VMP_NOTE_LAUNCH(); k_resolve<<<g, kMapThreads, 0, st>>>(m, ms.slot, ms.d_n, ms.rec, ms.sk, ms.sv);
-    radix_sort_pairs(ms.sk, ms.sv, ms.d_n, 32, ms.sort, st);
+    int rec_bits = 1;
+    while (rec_bits < 32 && (1ll << rec_bits) < (long long)m.rec_pool) ++rec_bits;
+    radix_sort_pairs(ms.sk, ms.sv, ms.d_n, rec_bits, ms.sort, st);
     VMP_NOTE_LAUNCH(); k_seg_heads<<<g, kMapThreads, 0, st>>>(ms.sk, ms.d_n, ms.flag2);
     exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_seg, ms.scan, st);
     VMP_NOTE_LAUNCH(); k_fill_u32<<<g, kMapThreads, 0, st>>>(ms.last_touch, ms.d_n, 0u);

@@ -1,7 +1,9 @@
 // Stable LSD radix sort (8-bit digits) and exclusive scan.
 //
-// Sort pass = histogram per 2048-element tile -> scan of the digit-major
-// histogram -> stable scatter.  The scatter ranks equal digits inside a tile
+// Sort pass = histogram per 2048-element tile -> per-digit exclusive scan of
+// the tile counts (one warp per digit) -> stable scatter, which adds the
+// digit's base (an exclusive scan of the 256 digit totals, redone in every
+// scatter CTA).  The scatter ranks equal digits inside a tile
 // with __match_any_sync: warp w owns tile elements [256w, 256w + 256) and
 // walks them 32 at a time in order, so the rank of an element is
 // (earlier warps' count of its digit) + (its warp's running count) + (its
@@ -28,49 +30,45 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __res
     hist[threadIdx.x * blocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// Exclusive scan of the whole histogram (256 * blocks entries), one CTA.
-__global__ void k_radix_scan_hist(uint32_t* hist, int total) {
-    __shared__ uint32_t warp_tot[32];
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int base = 0; base < total; base += blockDim.x) {
-        int i = base + threadIdx.x;
-        uint32_t v = i < total ? hist[i] : 0u;
+// Exclusive scan of each digit's tile counts, one warp per digit, in place;
+// the digit totals go to row_total.
+__global__ void k_radix_scan_rows(uint32_t* hist, int blocks, uint32_t* row_total) {
+    const int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (d >= 256) return;
+    uint32_t* row = hist + (size_t)d * blocks;
+    uint32_t carry = 0;
+    for (int base = 0; base < blocks; base += 32) {
+        const int i = base + lane;
+        const uint32_t v = i < blocks ? row[i] : 0u;
         uint32_t x = v;
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
-        if (lane == 31) warp_tot[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0u;
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            warp_tot[lane] = w;
-        }
-        __syncthreads();
-        uint32_t prefix = carry + (warp > 0 ? warp_tot[warp - 1] : 0u) + x - v;
-        if (i < total) hist[i] = prefix;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = prefix + v;
-        __syncthreads();
+        if (i < blocks) row[i] = carry + x - v;
+        carry += __shfl_sync(0xffffffffu, x, 31);
     }
+    if (lane == 0) row_total[d] = carry;
 }
+
+__device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot, uint32_t& total);
 
 __global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                 const int* __restrict__ d_n, int shift, const uint32_t* __restrict__ hist,
-                                int blocks) {
+                                const uint32_t* __restrict__ row_total, int blocks) {
     constexpr int W = kSortThreads / 32;
+    static_assert(kSortThreads == 256, "one thread per digit");
     __shared__ uint32_t wcnt[W][256];
+    __shared__ uint32_t dbase[256];
+    __shared__ uint32_t warp_tot[32];
     const int n = *d_n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < W * 256; i += kSortThreads) (&wcnt[0][0])[i] = 0;
+    {
+        uint32_t total;
+        dbase[threadIdx.x] = block_exclusive_scan(row_total[threadIdx.x], warp_tot, total);
+    }
     __syncthreads();
     const int base = blockIdx.x * kSortTile + warp * (32 * kSortItems);
     uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
@@ -93,7 +91,7 @@ __global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t
     __syncthreads();
     // exclusive prefix over warps, per digit
     for (int d = threadIdx.x; d < 256; d += kSortThreads) {
-        uint32_t s = hist[d * blocks + blockIdx.x];
+        uint32_t s = dbase[d] + hist[d * blocks + blockIdx.x];
         for (int w = 0; w < W; ++w) {
             uint32_t c = wcnt[w][d];
             wcnt[w][d] = s;
@@ -121,26 +119,41 @@ cudaError_t sort_scratch_alloc(SortScratch& s, int n_max) {
     if ((e = cudaMalloc(&s.k_alt, sizeof(uint32_t) * (size_t)n_max + 16)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&s.v_alt, sizeof(uint32_t) * (size_t)n_max + 16)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * 256 * (size_t)s.blocks)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s.row_total, sizeof(uint32_t) * 256)) != cudaSuccess) return e;
     return cudaSuccess;
 }
 void sort_scratch_free(SortScratch& s) {
-    cudaFree(s.k_alt); cudaFree(s.v_alt); cudaFree(s.hist);
-    s.k_alt = s.v_alt = s.hist = nullptr;
+    cudaFree(s.k_alt); cudaFree(s.v_alt); cudaFree(s.hist); cudaFree(s.row_total);
+    s.k_alt = s.v_alt = s.hist = s.row_total = nullptr;
+}
+
+__global__ void k_copy_pairs(const uint32_t* __restrict__ ks, const uint32_t* __restrict__ vs, uint32_t* kd,
+                             uint32_t* vd, const int* d_n) {
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        kd[i] = ks[i];
+        vd[i] = vs[i];
+    }
 }
 
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, SortScratch& s, cudaStream_t st) {
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
-    if (passes & 1) passes++;  // even pass count: result lands back in keys/vals
     if (passes > 4) passes = 4;
     uint32_t *ka = keys, *va = vals, *kb = s.k_alt, *vb = s.v_alt;
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
         VMP_NOTE_LAUNCH(); k_radix_hist<<<s.blocks, kSortThreads, 0, st>>>(ka, d_n, shift, s.hist, s.blocks);
-        VMP_NOTE_LAUNCH(); k_radix_scan_hist<<<1, 1024, 0, st>>>(s.hist, 256 * s.blocks);
-        VMP_NOTE_LAUNCH(); k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.blocks);
+        VMP_NOTE_LAUNCH(); k_radix_scan_rows<<<8, 1024, 0, st>>>(s.hist, s.blocks, s.row_total);
+        VMP_NOTE_LAUNCH();
+        k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.row_total, s.blocks);
         uint32_t* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
+    }
+    if (ka != keys) {  // odd pass count: the result is in the alternate buffers
+        int g = (s.n_max + 255) / 256;
+        if (g > 152 * 8) g = 152 * 8;
+        VMP_NOTE_LAUNCH(); k_copy_pairs<<<g, 256, 0, st>>>(ka, va, keys, vals, d_n);
     }
 }
 

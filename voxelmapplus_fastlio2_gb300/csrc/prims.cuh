@@ -18,7 +18,8 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 struct SortScratch {
     uint32_t* k_alt = nullptr;
     uint32_t* v_alt = nullptr;
-    uint32_t* hist = nullptr;  // [256][blocks]
+    uint32_t* hist = nullptr;       // [256][blocks]
+    uint32_t* row_total = nullptr;  // [256] per-digit totals
     int n_max = 0;
     int blocks = 0;
 };

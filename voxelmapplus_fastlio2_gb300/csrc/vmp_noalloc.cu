@@ -52,7 +52,8 @@ constexpr size_t kOffRunStart = align256(kOffScan + kU32N);
 constexpr size_t kOffKAlt = align256(kOffRunStart + kU32N);
 constexpr size_t kOffVAlt = align256(kOffKAlt + kU32N);
 constexpr size_t kOffHist = align256(kOffVAlt + kU32N);
-constexpr size_t kOffBlockSums = align256(kOffHist + sizeof(uint32_t) * 256 * kNaSortBlocks);
+constexpr size_t kOffRowTotal = align256(kOffHist + sizeof(uint32_t) * 256 * kNaSortBlocks);
+constexpr size_t kOffBlockSums = align256(kOffRowTotal + sizeof(uint32_t) * 256);
 constexpr size_t kOffEnd = align256(kOffBlockSums + sizeof(uint32_t) * (kNaScanBlocks + 16));
 static_assert(kOffEnd <= kNoAllocBytes, "no-alloc scratch layout exceeds the static array");
 
@@ -117,6 +118,7 @@ extern "C" vmp_status vmp_downsample_noalloc(const vmp_point* d_in, int n, doubl
     ss.k_alt = reinterpret_cast<uint32_t*>(base + kOffKAlt);
     ss.v_alt = reinterpret_cast<uint32_t*>(base + kOffVAlt);
     ss.hist = reinterpret_cast<uint32_t*>(base + kOffHist);
+    ss.row_total = reinterpret_cast<uint32_t*>(base + kOffRowTotal);
     ss.n_max = kNoAllocMaxPoints;
     ss.blocks = kNaSortBlocks;
     ScanScratch sc{};
