@@ -273,7 +273,9 @@ vmp_status vmp_io_bytes(vmp_stream_t s, long long* h2d, long long* d2h);
 /* Kernel launches issued by the library so far (all streams). */
 long long vmp_launch_count(void);
 /* Merge resolution: 0 parallel fixed point (default), 1 single-thread replay
- * in point order; both exact.  Rounds of the last parallel resolution. */
+ * in point order; both exact.  vmp_last_merge_rounds waits for the stream and
+ * returns the rounds of the last batch's fixed point (0 when the replay
+ * produced the result). */
 vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode);
 int vmp_last_merge_rounds(vmp_stream_t s);
 /* Test hooks: valid flags of the persistent residual records; the clouds of

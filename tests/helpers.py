@@ -47,6 +47,39 @@ def plane_points(rng, n_planes=40, pts_per=(5, 160), extent=20.0, noise=0.01, is
     return P[perm], Cv[perm]
 
 
+def merge_scene(rng, per_voxel=130, update_per_voxel=6, n_updates=3, noise=0.005):
+    """A floor and a wall sampled densely enough that their voxels freeze as
+    planes, then sparse re-observations of both: every re-observation of a
+    frozen plane voxel is a merge() call, and neighbouring voxels of one
+    surface start in different groups, so the calls merge in long chains.
+    Returns the build batch and the update batches (points, covariances)."""
+    def cov_for(m):
+        A = rng.normal(0, 0.02, (m, 3, 3))
+        return (A @ A.transpose(0, 2, 1) + np.eye(3) * 1e-4).reshape(m, 9)
+
+    def surface(count_per_voxel):
+        pts = []
+        for ix in range(-12, 12):
+            for iy in range(-12, 12):  # floor z = -1.73
+                a = rng.uniform(0, 0.5, (count_per_voxel, 2))
+                z = -1.73 + rng.normal(0, noise, count_per_voxel)
+                pts.append(np.c_[ix * 0.5 + a[:, 0], iy * 0.5 + a[:, 1], z])
+            for iz in range(-3, 5):  # wall x = 3.21
+                a = rng.uniform(0, 0.5, (count_per_voxel, 2))
+                x = 3.21 + rng.normal(0, noise, count_per_voxel)
+                pts.append(np.c_[x, ix * 0.5 + a[:, 0], iz * 0.5 + a[:, 1]])
+        p = np.concatenate(pts).astype(np.float32).astype(np.float64)
+        return p[rng.permutation(len(p))]
+
+    P = surface(per_voxel)
+    build = (P, cov_for(len(P)))
+    updates = []
+    for _ in range(n_updates):
+        P = surface(update_per_voxel)
+        updates.append((P, cov_for(len(P))))
+    return build, updates
+
+
 def export_oracle_map(olib, h):
     info = abi.vmp_map_info()
     olib.orc_map_info(h, C.byref(info))

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from voxelmapplus_fastlio2_gb300 import abi, synth
-from tests.helpers import compare_maps, export_oracle_map, plane_points, rot_angle
+from tests.helpers import compare_maps, export_oracle_map, merge_scene, plane_points, rot_angle
 
 pytestmark = pytest.mark.gpu
 
@@ -65,6 +65,37 @@ def test_map_build_update_bit_exact(lio_mod, oracle_lib, merge_mode):
             vg, ng = g.map.export()
             problems = compare_maps(vo, no, vg, ng, exact=True)
             assert not problems, f"step {step}: " + "; ".join(problems[:8])
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
+@pytest.mark.parametrize("merge_mode", [0, 1])
+def test_map_merges_bit_exact(lio_mod, oracle_lib, merge_mode):
+    """VoxelGrid::merge chains: frozen floor and wall voxels re-observed in
+    random order.  The whole map (group ids, merged flags, merged planes and
+    covariances included) must equal the oracle's after every batch; the
+    parallel fixed point must have needed several rounds."""
+    rng = np.random.default_rng(21)
+    (P, Cv), updates = merge_scene(rng)
+    cfg = abi.default_config(map_capacity=200000, max_scan_points=120000)
+    g = lio_mod.LIOBuilder(cfg)
+    g.set_merge_mode(merge_mode)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        oracle_lib.orc_map_build(o, _dp(P), _dp(Cv), len(P))
+        g.map.build(P, Cv)
+        for step, (P2, C2) in enumerate(updates):
+            oracle_lib.orc_map_update(o, _dp(P2), _dp(C2), len(P2))
+            g.map.update(P2, C2)
+            rounds = g.last_merge_rounds()
+            vo, no, info, _, _ = export_oracle_map(oracle_lib, o)
+            vg, ng = g.map.export()
+            problems = compare_maps(vo, no, vg, ng, exact=True)
+            assert not problems, f"step {step}: " + "; ".join(problems[:8])
+            if step == 0:
+                assert sum(1 for i in range(no) if vo[i].merged) > 100
+                if merge_mode == 0:
+                    assert rounds >= 3, rounds
     finally:
         oracle_lib.orc_destroy(o)
 

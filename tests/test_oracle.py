@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from voxelmapplus_fastlio2_gb300 import abi, synth
-from tests.helpers import plane_points
+from tests.helpers import export_oracle_map, merge_scene, plane_points
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -159,6 +159,30 @@ def test_map_semantics_small(oracle_lib):
         oracle_lib.orc_map_update(h, _dp(pts[100:].copy()), _dp(cov[100:].copy()), 30)
         oracle_lib.orc_map_export(h, arr, 1)
         assert arr[0].n == 100  # frozen: points dropped
+    finally:
+        oracle_lib.orc_destroy(h)
+
+
+def test_merge_scene_merges(oracle_lib):
+    """The merge fixture does what the GPU merge test relies on: the first
+    re-observation batch merges most voxels of the floor and the wall (one
+    group per surface is not reached in one batch: merge() gives a
+    neighbour the caller's group, so later callers regroup it) and every
+    voxel is a plane."""
+    rng = np.random.default_rng(21)
+    (P, Cv), updates = merge_scene(rng)
+    cfg = abi.default_config(map_capacity=200000, max_scan_points=120000)
+    h = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        oracle_lib.orc_map_build(h, _dp(P), _dp(Cv), len(P))
+        vo, no, _, _, _ = export_oracle_map(oracle_lib, h)
+        assert no == 768 and all(vo[i].is_plane and not vo[i].merged for i in range(no))
+        P2, C2 = updates[0]
+        oracle_lib.orc_map_update(h, _dp(P2), _dp(C2), len(P2))
+        vo, no, _, _, _ = export_oracle_map(oracle_lib, h)
+        merged = [vo[i] for i in range(no) if vo[i].merged]
+        assert len(merged) > 600
+        assert len(set(vo[i].group_id for i in range(no))) < no
     finally:
         oracle_lib.orc_destroy(h)
 

@@ -37,7 +37,7 @@ constexpr uint32_t F_INIT = 1u, F_PLANE = 2u, F_UPDATE = 4u, F_MERGED = 8u, F_AL
 
 // device error word bits
 constexpr uint32_t E_KEY_RANGE = 1u, E_HASH_FULL = 2u, E_RECORDS = 4u, E_CHUNKS = 8u, E_CAPACITY = 16u,
-                   E_NONFINITE = 32u, E_MERGE_ITER = 64u;
+                   E_NONFINITE = 32u, E_MERGE_ITER = 64u, E_MERGE_WAIT = 128u;
 
 // --------------------------------------------------------------- data layout
 // kf::State; identical layout to vmp_state.

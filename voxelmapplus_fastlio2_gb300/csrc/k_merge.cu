@@ -13,10 +13,21 @@
 //     the next log; a 64-bit signature per call detects change;
 //   * when no call's outcome changes, the log equals the sequential
 //     replay's: the earliest call always sees exact inputs, and by induction
-//     every later one does once the calls before it have settled.
-// If the fixed point is not reached in kMaxRounds rounds (long causal chains)
-// or the log pool overflows, a single-thread replay in point order runs
-// instead.  Both paths do the reference's arithmetic in its order.
+//     every later one does once the calls before it have settled (a fixed
+//     point is therefore unique).
+// All rounds run in one cooperative kernel (its CTAs are co-resident; rounds
+// are separated by a grid barrier whose waits are bounded), so the host never
+// waits on a round.  Per round, one thread per call tests whether the call
+// merges anything (most do not: in the reference sequence the first call on a
+// pair of voxels gives them one group id, and later calls see equal groups);
+// the calls that merge are then re-run by one warp each, with the 36
+// covariance entries and the 6 mean / normal components of the merge
+// arithmetic on separate lanes.  Which neighbours can be merged at all (in
+// the map at the call's point, frozen, plane) does not change during the
+// merges, so it is decided once, in the first round.
+// If the fixed point is not reached in kMaxRounds rounds, the log pool
+// overflows or a barrier wait runs out, a single-thread replay in point order
+// runs instead.  Both paths do the reference's arithmetic in its order.
 #include <cstring>
 #include "kernels.cuh"
 
@@ -24,7 +35,10 @@ namespace vmp {
 
 constexpr int kMergeThreads = 256;
 constexpr int kMaxRounds = 24;
+constexpr int kLogs = 3;  // round r writes log r % 3, reads log (r - 1) % 3, clears log (r + 1) % 3
 constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint64_t kSigNone = 0x1234567ull;
+constexpr long long kBarrierSpinLimit = 20000000;  // x >= 64 ns sleeps: about a second or more
 
 struct MState {
     double mean[3];
@@ -44,19 +58,28 @@ struct MEntry {
 };
 
 struct MergeCtl {
-    int n_ent[2];
-    int changed;
+    int n_ent[kLogs];
     int overflow;
+    int changed[kMaxRounds];
+    int n_queue[kMaxRounds];
+    int rounds;     // rounds run by the last batch
+    int converged;  // 1: the final log is the sequential result
+    int wait_error; // a grid barrier gave up waiting
+    int pad;
+    unsigned int bar_count;
+    unsigned int bar_gen;
 };
 
 struct MergeScratch {
-    MEntry* ent[2];
-    uint32_t* head[2];   // [rec_pool]
-    uint64_t* sig;       // [max_batch] per call signature
+    MEntry* ent[kLogs];
+    uint32_t* head[kLogs];  // [rec_pool]
+    uint64_t* sig;          // [max_batch] per call signature
+    uint32_t* cand;         // [max_batch * 6] mergeable neighbours per call (kNone: none)
+    uint32_t* queue;        // [max_batch] calls that merge in the current round
     MergeCtl* ctl;
-    MergeCtl* h_ctl;     // pinned host mirror
     int pool;
     int rec_pool;
+    int coop_grid;
 };
 
 __device__ inline void base_state(const DMap& m, uint32_t r, MState& s) {
@@ -68,16 +91,22 @@ __device__ inline void base_state(const DMap& m, uint32_t r, MState& s) {
     s.merged = (h.flags & F_MERGED) ? 1u : 0u;
 }
 
-// State of record r as of batch point t (entries with a smaller t).
-__device__ inline void state_at(const DMap& m, uint32_t r, uint32_t t, const MEntry* ent, const uint32_t* head,
-                                MState& s) {
+// Latest log entry of record r written before batch point t (kNone: none).
+__device__ inline uint32_t find_entry(uint32_t r, uint32_t t, const MEntry* ent, const uint32_t* head) {
     uint32_t best = kNone, best_t = 0;
     if (head) {
         for (uint32_t e = head[r]; e != kNone; e = ent[e].next) {
-            uint32_t et = ent[e].t;
+            const uint32_t et = ent[e].t;
             if (et < t && (best == kNone || et > best_t)) { best = e; best_t = et; }
         }
     }
+    return best;
+}
+
+// State of record r as of batch point t.
+__device__ inline void state_at(const DMap& m, uint32_t r, uint32_t t, const MEntry* ent, const uint32_t* head,
+                                MState& s) {
+    const uint32_t best = find_entry(r, t, ent, head);
     if (best == kNone) base_state(m, r, s);
     else s = ent[best].s;
 }
@@ -91,39 +120,40 @@ __device__ inline uint64_t mix64(uint64_t h, uint64_t v) {
     h *= 0xff51afd7ed558ccdull;
     return h ^ (h >> 29);
 }
-__device__ inline uint64_t sig_state(uint64_t h, uint32_t rec, const MState& s) {
-    h = mix64(h, rec);
-    for (int k = 0; k < 3; ++k) { h = mix64(h, __double_as_longlong(s.mean[k])); h = mix64(h, __double_as_longlong(s.norm[k])); }
-    for (int k = 0; k < 36; ++k) h = mix64(h, __double_as_longlong(s.cov[k]));
-    h = mix64(h, s.group);
-    return mix64(h, s.merged);
+
+// The static part of merge()'s neighbour test: neighbour k of the caller is
+// in the map at point T, frozen and a plane (voxel_map.cpp:146-152).
+__device__ inline uint32_t merge_candidate(const DMap& m, int64_t x, int64_t y, int64_t z, int k,
+                                           unsigned long long T) {
+    const int64_t nb[6][3] = {{x - 1, y, z}, {x, y - 1, z}, {x, y, z - 1}, {x + 1, y, z}, {x, y + 1, z}, {x, y, z + 1}};
+    if (!key_in_range(nb[k][0]) || !key_in_range(nb[k][1]) || !key_in_range(nb[k][2])) return kNone;
+    const uint32_t b_rec = map_find(m, pack_key(nb[k][0], nb[k][1], nb[k][2]));
+    if (b_rec == kNoRec || b_rec >= (uint32_t)m.rec_pool) return kNone;
+    const RecCold& bc = m.cold[b_rec];
+    if (!(m.hot[b_rec].flags & F_ALIVE) && bc.evict_g == kNever) return kNone;
+    if (!(bc.create_g < T && bc.evict_g > T)) return kNone;  // not in the map at this point
+    if (!(bc.freeze_g < T)) return kNone;
+    if (!(m.hot[b_rec].flags & F_PLANE)) return kNone;
+    return b_rec;
 }
 
-// One merge() call by record a_rec at batch point t.  Outputs the written
-// states (neighbours first, in probe order, then the caller) into out/out_rec;
-// returns how many.
-__device__ int merge_call(const DMap& m, uint32_t a_rec, uint32_t t, const MEntry* ent, const uint32_t* head,
-                          MState* out, uint32_t* out_rec) {
+// One merge() call by record a_rec at batch point t, one thread (the replay).
+// Outputs the written states (neighbours first, in probe order, then the
+// caller) into out/out_rec; returns how many.
+__device__ int merge_call(const DMap& m, uint32_t a_rec, uint32_t t, MState* out, uint32_t* out_rec) {
     const unsigned long long T = m.cnt->batch_base + t;
     MState a;
-    state_at(m, a_rec, t, ent, head, a);
+    base_state(m, a_rec, a);
     int64_t x, y, z;
     unpack_key(m.cold[a_rec].key, x, y, z);
-    const int64_t nb[6][3] = {{x - 1, y, z}, {x, y - 1, z}, {x, y, z - 1}, {x + 1, y, z}, {x, y + 1, z}, {x, y, z + 1}};
     int nout = 0;
     bool any = false;
     for (int k = 0; k < 6; ++k) {
-        if (!key_in_range(nb[k][0]) || !key_in_range(nb[k][1]) || !key_in_range(nb[k][2])) continue;
-        uint32_t b_rec = map_find(m, pack_key(nb[k][0], nb[k][1], nb[k][2]));
-        if (b_rec == kNoRec || b_rec >= (uint32_t)m.rec_pool) continue;
-        const RecCold& bc = m.cold[b_rec];
-        if (!(m.hot[b_rec].flags & F_ALIVE) && bc.evict_g == kNever) continue;
-        if (!(bc.create_g < T && bc.evict_g > T)) continue;  // not in the map at this point
-        const bool frozen = bc.freeze_g < T;
-        const bool plane = (m.hot[b_rec].flags & F_PLANE) != 0;
+        const uint32_t b_rec = merge_candidate(m, x, y, z, k, T);
+        if (b_rec == kNone) continue;
         MState b;
-        state_at(m, b_rec, t, ent, head, b);
-        if (b.group == a.group || !frozen || !plane) continue;
+        base_state(m, b_rec, b);
+        if (b.group == a.group) continue;
         double norm_distance = 1.0 - dot3(b.norm, a.norm);
         double axis_distance = fabs(dot3(b.norm, b.mean) - dot3(a.norm, a.mean));
         if (norm_distance > m.merge_angle || axis_distance > m.merge_dist) continue;
@@ -167,156 +197,397 @@ __device__ inline void write_state(const DMap& m, uint32_t r, const MState& s) {
 }
 
 // ------------------------------------------------------------ sequential replay
+// Every call in point order on one thread, writing the records in place
+// (mode 1, and the fallback when the fixed point did not settle: `only_if`
+// non-null makes it return when the fixed point converged).
 __global__ void k_merge_sequential(DMap m, const uint32_t* __restrict__ ev_list, const uint32_t* __restrict__ ev_rec,
-                                   const int* d_n_ev) {
+                                   const int* d_n_ev, const MergeCtl* only_if) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (only_if && only_if->converged) return;
+    if (only_if) m.cnt->changed = 1;  // informational: the replay path ran
     const int ne = *d_n_ev;
     MState out[7];
     uint32_t out_rec[7];
     for (int e = 0; e < ne; ++e) {
-        uint32_t t = ev_list[e];
-        int no = merge_call(m, ev_rec[t], t, nullptr, nullptr, out, out_rec);
+        const uint32_t t = ev_list[e];
+        const int no = merge_call(m, ev_rec[t], t, out, out_rec);
         for (int k = 0; k < no; ++k) write_state(m, out_rec[k], out[k]);
     }
 }
 
 // ------------------------------------------------------------ fixed point
-__global__ void k_merge_clear(MergeScratch ms, int cur) {
-    const int n = ms.ctl->n_ent[cur];
-    const int lim = n < ms.pool ? n : ms.pool;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < lim; e += gridDim.x * blockDim.x)
-        ms.head[cur][ms.ent[cur][e].rec] = kNone;
+// Grid barrier for the cooperative kernel (all CTAs co-resident).  A wait
+// gives up after kBarrierSpinLimit polls, records the failure and lets every
+// later barrier pass at once, so the kernel always ends; the replay then
+// produces the result.
+__device__ void grid_barrier(MergeCtl* c) {
     __syncthreads();
-    if (blockIdx.x == 0 && threadIdx.x == 0) { ms.ctl->changed = 0; }
-}
-__global__ void k_merge_reset_count(MergeScratch ms, int cur) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) ms.ctl->n_ent[cur] = 0;
-}
-__global__ void k_merge_begin(MergeScratch ms) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) { ms.ctl->overflow = 0; ms.ctl->changed = 0; }
-}
-
-__global__ void __launch_bounds__(kMergeThreads) k_merge_round(DMap m, MergeScratch ms, const uint32_t* __restrict__ ev_list,
-                                                               const uint32_t* __restrict__ ev_rec,
-                                                               const int* d_n_ev, int cur, int first) {
-    const int ne = *d_n_ev;
-    const int prev = cur ^ 1;
-    const MEntry* pent = ms.ent[prev];
-    const uint32_t* phead = first ? nullptr : ms.head[prev];
-    MState out[7];
-    uint32_t out_rec[7];
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
-        const uint32_t t = ev_list[e];
-        int no = merge_call(m, ev_rec[t], t, pent, phead, out, out_rec);
-        uint64_t sg = 0x1234567ull + (uint64_t)no;
-        for (int k = 0; k < no; ++k) sg = sig_state(sg, out_rec[k], out[k]);
-        if (first || ms.sig[e] != sg) atomicAdd(&ms.ctl->changed, 1);
-        ms.sig[e] = sg;
-        if (no == 0) continue;
-        int pos = atomicAdd(&ms.ctl->n_ent[cur], no);
-        if (pos + no > ms.pool) { ms.ctl->overflow = 1; continue; }
-        for (int k = 0; k < no; ++k) {
-            MEntry& en = ms.ent[cur][pos + k];
-            en.rec = out_rec[k];
-            en.t = t;
-            en.s = out[k];
-            en.next = atomicExch(&ms.head[cur][out_rec[k]], (uint32_t)(pos + k));
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &c->bar_gen;
+        volatile int* verr = &c->wait_error;
+        if (!*verr) {
+            const unsigned int g = *vgen;
+            __threadfence();
+            if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+                c->bar_count = 0;
+                __threadfence();
+                atomicAdd(&c->bar_gen, 1u);
+            } else {
+                long long spins = 0;
+                while (*vgen == g) {
+                    if (*verr) break;
+                    __nanosleep(64);
+                    if (++spins > kBarrierSpinLimit) {
+                        atomicExch(&c->wait_error, 1);
+                        break;
+                    }
+                }
+            }
         }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+struct PlaneRef {
+    double mean[3], norm[3];
+    uint64_t group;
+};
+__device__ inline void plane_at(const DMap& m, uint32_t r, uint32_t t, const MEntry* ent, const uint32_t* head,
+                                PlaneRef& p) {
+    const uint32_t e = find_entry(r, t, ent, head);
+    if (e == kNone) {
+        const RecHot& h = m.hot[r];
+        for (int k = 0; k < 3; ++k) { p.mean[k] = h.mean[k]; p.norm[k] = h.norm[k]; }
+        p.group = h.group;
+    } else {
+        const MState& s = ent[e].s;
+        for (int k = 0; k < 3; ++k) { p.mean[k] = s.mean[k]; p.norm[k] = s.norm[k]; }
+        p.group = s.group;
     }
 }
 
-// Final states: the latest entry of each written record.
-__global__ void k_merge_apply(DMap m, MergeScratch ms, int cur) {
-    const int n = ms.ctl->n_ent[cur];
-    const MEntry* ent = ms.ent[cur];
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const uint32_t r = ent[e].rec;
-        // the entry is the record's latest if no other entry of r has a larger t
-        bool latest = true;
-        for (uint32_t o = ms.head[cur][r]; o != kNone; o = ent[o].next)
-            if (ent[o].t > ent[e].t) { latest = false; break; }
-        if (latest) write_state(m, r, ent[e].s);
+// Does the call merge anything?  merge()'s tests up to its first merge, with
+// the caller's state as of the call (one thread).
+__device__ bool call_merges(const DMap& m, uint32_t a_rec, uint32_t t, const uint32_t* cand, const MEntry* ent,
+                            const uint32_t* head) {
+    PlaneRef a;
+    plane_at(m, a_rec, t, ent, head, a);
+    for (int k = 0; k < 6; ++k) {
+        const uint32_t b_rec = cand[k];
+        if (b_rec == kNone) continue;
+        PlaneRef b;
+        plane_at(m, b_rec, t, ent, head, b);
+        if (b.group == a.group) continue;
+        double norm_distance = 1.0 - dot3(b.norm, a.norm);
+        double axis_distance = fabs(dot3(b.norm, b.mean) - dot3(a.norm, a.mean));
+        if (norm_distance > m.merge_angle || axis_distance > m.merge_dist) continue;
+        return true;
+    }
+    return false;
+}
+
+// A voxel state spread over a warp: mean / normal / group on every lane,
+// covariance entry `lane` in c0 and entry 32 + lane (lane < 4) in c1.
+struct WState {
+    double mean[3], norm[3];
+    double c0, c1;
+    uint64_t group;
+    uint32_t merged;
+};
+__device__ inline void wstate_load(const DMap& m, uint32_t r, uint32_t e, const MEntry* ent, int lane, WState& s) {
+    if (e == kNone) {
+        const RecHot& h = m.hot[r];
+        const RecCold& c = m.cold[r];
+        for (int k = 0; k < 3; ++k) { s.mean[k] = h.mean[k]; s.norm[k] = h.norm[k]; }
+        s.c0 = c.cov[lane];
+        s.c1 = lane < 4 ? c.cov[32 + lane] : 0.0;
+        s.group = h.group;
+        s.merged = (h.flags & F_MERGED) ? 1u : 0u;
+    } else {
+        const MState& x = ent[e].s;
+        for (int k = 0; k < 3; ++k) { s.mean[k] = x.mean[k]; s.norm[k] = x.norm[k]; }
+        s.c0 = x.cov[lane];
+        s.c1 = lane < 4 ? x.cov[32 + lane] : 0.0;
+        s.group = x.group;
+        s.merged = x.merged;
     }
 }
-
-__global__ void k_flag_merge_fallback(DMap m) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) m.cnt->changed = 1;  // informational: the replay path ran
+// trace3(cov, 0) and trace3(cov, 3) of a warp-spread covariance
+__device__ inline void wtraces(const WState& s, double& tn, double& tm) {
+    const double d0 = __shfl_sync(0xffffffffu, s.c0, 0), d7 = __shfl_sync(0xffffffffu, s.c0, 7),
+                 d14 = __shfl_sync(0xffffffffu, s.c0, 14), d21 = __shfl_sync(0xffffffffu, s.c0, 21),
+                 d28 = __shfl_sync(0xffffffffu, s.c0, 28), d35 = __shfl_sync(0xffffffffu, s.c1, 3);
+    tn = (d0 + d7) + d14;
+    tm = (d21 + d28) + d35;
 }
-static void set_error_host_flag(DMap& m, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_flag_merge_fallback<<<1, 32, 0, st>>>(m); }
+// Appends one output state to the log; returns its contribution to the
+// call's signature (the same on every lane).
+__device__ inline uint64_t wstate_emit(MergeScratch& g, int cur, uint32_t rec, uint32_t t, const WState& s, int lane,
+                                       bool& overflow) {
+    uint64_t h = mix64(0x51ull + lane, __double_as_longlong(s.c0));
+    if (lane < 4) h = mix64(h, __double_as_longlong(s.c1));
+    if (lane == 0) {
+        h = mix64(h, rec);
+        for (int k = 0; k < 3; ++k) { h = mix64(h, __double_as_longlong(s.mean[k])); h = mix64(h, __double_as_longlong(s.norm[k])); }
+        h = mix64(h, s.group);
+        h = mix64(h, s.merged);
+    }
+    for (int o = 16; o > 0; o >>= 1) h ^= __shfl_xor_sync(0xffffffffu, h, o);
+    int pos = 0;
+    if (lane == 0) pos = atomicAdd(&g.ctl->n_ent[cur], 1);
+    pos = __shfl_sync(0xffffffffu, pos, 0);
+    if (pos >= g.pool) {
+        overflow = true;
+        return h;
+    }
+    MEntry& en = g.ent[cur][pos];
+    en.s.cov[lane] = s.c0;
+    if (lane < 4) en.s.cov[32 + lane] = s.c1;
+    if (lane == 0) {
+        en.rec = rec;
+        en.t = t;
+        for (int k = 0; k < 3; ++k) { en.s.mean[k] = s.mean[k]; en.s.norm[k] = s.norm[k]; }
+        en.s.group = s.group;
+        en.s.merged = s.merged;
+        __threadfence();
+        en.next = atomicExch(&g.head[cur][rec], (uint32_t)pos);
+    }
+    return h;
+}
 
-static MergeScratch* g_unused = nullptr;
+// One merge() call on one warp, against the previous round's log; writes its
+// outputs to log `cur` and returns the call's signature.
+__device__ uint64_t warp_merge_call(const DMap& m, MergeScratch& g, uint32_t a_rec, uint32_t t, const uint32_t* cand,
+                                    const MEntry* pent, const uint32_t* phead, int cur, bool& overflow) {
+    const int lane = threadIdx.x & 31;
+    uint32_t ea = 0;
+    if (lane == 0) ea = find_entry(a_rec, t, pent, phead);
+    ea = __shfl_sync(0xffffffffu, ea, 0);
+    WState a;
+    wstate_load(m, a_rec, ea, pent, lane, a);
+    uint64_t sig = kSigNone;
+    int nout = 0;
+    for (int k = 0; k < 6; ++k) {
+        const uint32_t b_rec = cand[k];
+        if (b_rec == kNone) continue;
+        uint32_t eb = 0;
+        if (lane == 0) eb = find_entry(b_rec, t, pent, phead);
+        eb = __shfl_sync(0xffffffffu, eb, 0);
+        WState b;
+        wstate_load(m, b_rec, eb, pent, lane, b);
+        if (b.group == a.group) continue;
+        double norm_distance = 1.0 - dot3(b.norm, a.norm);
+        double axis_distance = fabs(dot3(b.norm, b.mean) - dot3(a.norm, a.mean));
+        if (norm_distance > m.merge_angle || axis_distance > m.merge_dist) continue;
+        double tn0, tm0, tn1, tm1;
+        wtraces(a, tn0, tm0);
+        wtraces(b, tn1, tm1);
+        const double tc0 = tn0 + tm0, tc1 = tn1 + tm1;
+        // mean on lanes 0-2, normal on lanes 3-5 (the reference's precedence:
+        // only the second product is divided)
+        const int q = lane < 3 ? lane : (lane < 6 ? lane - 3 : 0);
+        const bool is_mean = lane < 3;
+        const double bv = is_mean ? (q == 0 ? b.mean[0] : q == 1 ? b.mean[1] : b.mean[2])
+                                  : (q == 0 ? b.norm[0] : q == 1 ? b.norm[1] : b.norm[2]);
+        const double av = is_mean ? (q == 0 ? a.mean[0] : q == 1 ? a.mean[1] : a.mean[2])
+                                  : (q == 0 ? a.norm[0] : q == 1 ? a.norm[1] : a.norm[2]);
+        const double wb = is_mean ? tm0 : tn0, wa = is_mean ? tm1 : tn1;
+        const double v = wb * bv + wa * av / (wb + wa);
+        double nmean[3], nnorm[3];
+        for (int r = 0; r < 3; ++r) {
+            nmean[r] = __shfl_sync(0xffffffffu, v, r);
+            nnorm[r] = __shfl_sync(0xffffffffu, v, 3 + r);
+        }
+        const double w0 = tc0 * tc0, w1 = tc1 * tc1, den = (tc0 + tc1) * (tc0 + tc1);
+        const double nc0 = (w0 * b.c0 + w1 * a.c0) / den;
+        const double nc1 = lane < 4 ? (w0 * b.c1 + w1 * a.c1) / den : 0.0;
+        if (-dot3(nmean, nnorm) < 0.0) {
+            for (int r = 0; r < 3; ++r) nnorm[r] = -nnorm[r];
+        }
+        b.group = a.group;
+        a.merged = 1;
+        b.merged = 1;
+        for (int r = 0; r < 3; ++r) { a.mean[r] = nmean[r]; a.norm[r] = nnorm[r]; b.mean[r] = nmean[r]; b.norm[r] = nnorm[r]; }
+        a.c0 = nc0; a.c1 = nc1; b.c0 = nc0; b.c1 = nc1;
+        sig = mix64(sig, wstate_emit(g, cur, b_rec, t, b, lane, overflow));
+        ++nout;
+    }
+    if (nout > 0) sig = mix64(sig, wstate_emit(g, cur, a_rec, t, a, lane, overflow));
+    return mix64(sig, (uint64_t)nout);
+}
+
+// All rounds of the fixed point and the final write-back, one cooperative
+// launch.
+__global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeScratch g,
+                                                                  const uint32_t* __restrict__ ev_list,
+                                                                  const uint32_t* __restrict__ ev_rec,
+                                                                  const int* d_n_ev) {
+    MergeCtl* c = g.ctl;
+    const int ne = *d_n_ev;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31, gw = tid >> 5, nw = nth >> 5;
+    const uint64_t noop_sig = mix64(kSigNone, 0);
+    // the three logs still hold the previous batch's entries: unlink them
+    int old_n[kLogs];
+    for (int b = 0; b < kLogs; ++b) old_n[b] = min(c->n_ent[b], g.pool);
+    grid_barrier(c);
+    if (tid == 0) {
+        for (int b = 0; b < kLogs; ++b) c->n_ent[b] = 0;
+        c->overflow = 0;
+        c->rounds = 0;
+        for (int r = 0; r < kMaxRounds; ++r) { c->changed[r] = 0; c->n_queue[r] = 0; }
+    }
+    for (int b = 0; b < kLogs; ++b)
+        for (int e = tid; e < old_n[b]; e += nth) g.head[b][g.ent[b][e].rec] = kNone;
+    grid_barrier(c);
+
+    int final_log = -1;
+    for (int r = 0; r < kMaxRounds; ++r) {
+        const int cur = r % kLogs, prev = (r + kLogs - 1) % kLogs, nxt = (r + 1) % kLogs;
+        const bool first = r == 0;
+        const MEntry* pent = g.ent[prev];
+        const uint32_t* phead = first ? nullptr : g.head[prev];
+        if (r >= 2) {  // the log the next round writes still holds round r - 2's entries
+            const int nn = min(c->n_ent[nxt], g.pool);
+            for (int e = tid; e < nn; e += nth) g.head[nxt][g.ent[nxt][e].rec] = kNone;
+        }
+        // one thread per call: does it merge anything?
+        for (int e = tid; e < ne; e += nth) {
+            const uint32_t t = ev_list[e];
+            const uint32_t a_rec = ev_rec[t];
+            uint32_t cl[6];
+            if (first) {
+                const unsigned long long T = m.cnt->batch_base + t;
+                int64_t x, y, z;
+                unpack_key(m.cold[a_rec].key, x, y, z);
+                for (int k = 0; k < 6; ++k) {
+                    cl[k] = merge_candidate(m, x, y, z, k, T);
+                    g.cand[(size_t)e * 6 + k] = cl[k];
+                }
+            } else {
+                for (int k = 0; k < 6; ++k) cl[k] = g.cand[(size_t)e * 6 + k];
+            }
+            if (call_merges(m, a_rec, t, cl, pent, phead)) {
+                const int q = atomicAdd(&c->n_queue[r], 1);
+                g.queue[q] = (uint32_t)e;
+            } else {
+                if (first || g.sig[e] != noop_sig) atomicAdd(&c->changed[r], 1);
+                g.sig[e] = noop_sig;
+            }
+        }
+        grid_barrier(c);
+        if (tid == 0) c->n_ent[nxt] = 0;  // its unlinking above is done
+        // one warp per call that merges: the whole call, lane-parallel
+        const int nq = c->n_queue[r];
+        bool ovf = false;
+        for (int qi = gw; qi < nq; qi += nw) {
+            const int e = (int)g.queue[qi];
+            const uint32_t t = ev_list[e];
+            const uint32_t a_rec = ev_rec[t];
+            uint32_t cl[6];
+            for (int k = 0; k < 6; ++k) cl[k] = g.cand[(size_t)e * 6 + k];
+            const uint64_t sg = warp_merge_call(m, g, a_rec, t, cl, pent, phead, cur, ovf);
+            if (lane == 0) {
+                if (first || g.sig[e] != sg) atomicAdd(&c->changed[r], 1);
+                g.sig[e] = sg;
+            }
+        }
+        if (ovf && lane == 0) c->overflow = 1;
+        grid_barrier(c);
+        if (tid == 0) c->rounds = r + 1;
+        if (c->wait_error || c->overflow) break;
+        if (first && nq == 0) { final_log = cur; break; }  // no call merges anything
+        if (!first && c->changed[r] == 0) { final_log = cur; break; }
+    }
+    if (final_log >= 0 && !c->wait_error) {
+        const MEntry* fe = g.ent[final_log];
+        const uint32_t* fh = g.head[final_log];
+        const int nf = min(c->n_ent[final_log], g.pool);
+        for (int e = tid; e < nf; e += nth) {
+            const MEntry& en = fe[e];
+            bool latest = true;
+            for (uint32_t o = fh[en.rec]; o != kNone; o = fe[o].next)
+                if (fe[o].t > en.t) { latest = false; break; }
+            if (latest) write_state(m, en.rec, en.s);
+        }
+        if (tid == 0) c->converged = 1;
+    }
+    if (tid == 0 && c->wait_error) set_error(m.cnt, E_MERGE_WAIT);
+}
 
 cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool) {
     MergeScratch* ms = new MergeScratch();
     std::memset(ms, 0, sizeof(*ms));
+    *out = ms;
     ms->pool = max_batch / 2 + 1024;
     ms->rec_pool = rec_pool;
     cudaError_t e;
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kLogs; ++b) {
         if ((e = cudaMalloc(&ms->ent[b], sizeof(MEntry) * (size_t)ms->pool)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&ms->head[b], sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
         if ((e = cudaMemset(ms->head[b], 0xFF, sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
     }
-    if ((e = cudaMalloc(&ms->sig, sizeof(uint64_t) * ((size_t)max_batch + 16))) != cudaSuccess) return e;
+    const size_t nb = (size_t)max_batch + 16;
+    if ((e = cudaMalloc(&ms->sig, sizeof(uint64_t) * nb)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&ms->cand, sizeof(uint32_t) * 6 * nb)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&ms->queue, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&ms->ctl, sizeof(MergeCtl))) != cudaSuccess) return e;
     if ((e = cudaMemset(ms->ctl, 0, sizeof(MergeCtl))) != cudaSuccess) return e;
-    if ((e = cudaMallocHost(&ms->h_ctl, sizeof(MergeCtl))) != cudaSuccess) return e;
-    *out = ms;
-    (void)g_unused;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge_fixpoint, kMergeThreads, 0)) != cudaSuccess)
+        return e;
+    if (per_sm > 4) per_sm = 4;
+    ms->coop_grid = sms * per_sm;
     return cudaSuccess;
 }
 void merge_scratch_free(void* p) {
     MergeScratch* ms = (MergeScratch*)p;
     if (!ms) return;
-    for (int b = 0; b < 2; ++b) { cudaFree(ms->ent[b]); cudaFree(ms->head[b]); }
+    for (int b = 0; b < kLogs; ++b) { cudaFree(ms->ent[b]); cudaFree(ms->head[b]); }
     cudaFree(ms->sig);
+    cudaFree(ms->cand);
+    cudaFree(ms->queue);
     cudaFree(ms->ctl);
-    cudaFreeHost(ms->h_ctl);
     delete ms;
 }
 
-// Host loop: rounds until no call changes (one small device->host read per
-// round), then applies the log; sequential replay as the fallback.
+// The merge calls of one batch: the cooperative fixed point, then the replay
+// if it did not settle (the replay kernel returns at once when it did).
+// Nothing waits on the host.
 cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, int mode, int* rounds_out,
                              cudaStream_t st) {
+    (void)n_max;
     MergeScratch& g = *(MergeScratch*)scratch;
-    int grid = (n_max + kMergeThreads - 1) / kMergeThreads;
-    if (grid > 152 * 4) grid = 152 * 4;
-    if (grid < 1) grid = 1;
-    if (rounds_out) *rounds_out = 0;
+    if (rounds_out) *rounds_out = -1;
     if (mode == 1) {  // sequential replay only
-        VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev);
+        VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev, nullptr);
         return cudaGetLastError();
     }
     cudaError_t e;
-    VMP_NOTE_LAUNCH(); k_merge_begin<<<1, 32, 0, st>>>(g);
-    // clear both logs (left over from the previous batch)
-    for (int b = 0; b < 2; ++b) {
-        VMP_NOTE_LAUNCH(); k_merge_clear<<<grid, kMergeThreads, 0, st>>>(g, b);
-        VMP_NOTE_LAUNCH(); k_merge_reset_count<<<1, 32, 0, st>>>(g, b);
+    // converged = 0; wait_error, pad, bar_count = 0 (bar_gen keeps counting)
+    if ((e = cudaMemsetAsync(&g.ctl->converged, 0, sizeof(int) * 3 + sizeof(unsigned int), st)) != cudaSuccess) return e;
+    if (g.coop_grid > 0) {
+        void* args[] = {(void*)&m, (void*)&g, (void*)&ms.ev_list, (void*)&ms.ev_rec, (void*)&ms.d_n_ev};
+        VMP_NOTE_LAUNCH();
+        e = cudaLaunchCooperativeKernel((const void*)k_merge_fixpoint, dim3(g.coop_grid), dim3(kMergeThreads), args, 0,
+                                        st);
+        if (e != cudaSuccess) cudaGetLastError();  // the replay below produces the result
     }
-    int cur = 0;
-    bool converged = false;
-    for (int r = 0; r < kMaxRounds; ++r) {
-        VMP_NOTE_LAUNCH(); k_merge_clear<<<grid, kMergeThreads, 0, st>>>(g, cur);
-        VMP_NOTE_LAUNCH(); k_merge_reset_count<<<1, 32, 0, st>>>(g, cur);
-        VMP_NOTE_LAUNCH(); k_merge_round<<<grid, kMergeThreads, 0, st>>>(m, g, ms.ev_list, ms.ev_rec, ms.d_n_ev, cur, r == 0 ? 1 : 0);
-        if ((e = cudaMemcpyAsync(g.h_ctl, g.ctl, sizeof(MergeCtl), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-        ms.merge_d2h += (long long)sizeof(MergeCtl);
-        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-        if (rounds_out) *rounds_out = r + 1;
-        if (g.h_ctl->overflow) break;
-        if (g.h_ctl->n_ent[cur] == 0 && r == 0) { converged = true; break; }  // no call merges anything
-        if (r > 0 && g.h_ctl->changed == 0) { converged = true; break; }
-        cur ^= 1;
-    }
-    if (converged) {
-        VMP_NOTE_LAUNCH(); k_merge_apply<<<grid, kMergeThreads, 0, st>>>(m, g, cur);
-    } else {
-        VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev);
-        set_error_host_flag(m, st);
-    }
+    VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev, g.ctl);
     return cudaGetLastError();
+}
+
+// Rounds the last batch's fixed point ran (0 when the replay ran alone);
+// waits for the stream.
+int merge_rounds_read(void* scratch, cudaStream_t st) {
+    MergeScratch& g = *(MergeScratch*)scratch;
+    MergeCtl h;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    if (cudaMemcpy(&h, g.ctl, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return h.converged ? h.rounds : 0;
 }
 
 }  // namespace vmp

@@ -129,5 +129,6 @@ void merge_scratch_free(void* p);
 // mode 0: parallel fixed point (sequential replay as fallback); 1: replay only
 cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, int mode, int* rounds_out,
                              cudaStream_t st);
+int merge_rounds_read(void* scratch, cudaStream_t st);
 
 }  // namespace vmp

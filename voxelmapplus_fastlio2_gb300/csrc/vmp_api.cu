@@ -716,6 +716,8 @@ static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
         cudaStreamSynchronize(s->st);
         if (e & E_KEY_RANGE) return fail(s, VMP_ERR_KEY_RANGE, "a voxel index left the packed range [-2^20, 2^20)");
         if (e & E_HASH_FULL) return fail(s, VMP_ERR_HASH_FULL, "voxel hash table full");
+        if (e & E_MERGE_WAIT)
+            return fail(s, VMP_ERR_TIMEOUT, "merge fixed point: a grid barrier wait ran out (map state unreliable)");
         if (e & (E_RECORDS | E_CHUNKS | E_CAPACITY))
             return fail(s, VMP_ERR_CAPACITY, "voxel record / slab pool exhausted (error bits " + std::to_string(e) + ")");
     }
@@ -1157,6 +1159,6 @@ vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode) {
     s->ms.merge_mode = mode;
     return VMP_OK;
 }
-int vmp_last_merge_rounds(vmp_stream_t s) { return s ? s->ms.merge_rounds : -1; }
+int vmp_last_merge_rounds(vmp_stream_t s) { return s ? merge_rounds_read(s->ms.merge, s->st) : -1; }
 
 }  // extern "C"
