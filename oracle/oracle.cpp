@@ -411,19 +411,40 @@ void VoxelGrid::updatePlane() {  // voxel_map.cpp:97-136
     eigSym3(cov, evals, evecs);
     if (evals[0] > plane_thresh) { is_plane = false; return; }
     is_plane = true;
-    M3 J_Q = M3::Identity() / static_cast<double>(plane.n);
+    // J = [evecs * F; I / n] (voxel_map.cpp:115-130).  The per-refit factors
+    // are formed once, and the products with J's known zeros (row 0 of F, the
+    // off-diagonal of I / n) are left out: the same sums without their +-0
+    // terms.
+    const double inv_n = 1.0 / static_cast<double>(plane.n);
     V3 pn = v3(evecs(0, 0), evecs(1, 0), evecs(2, 0));
+    M3 Mm[3];
+    double den[3] = {0.0, 0.0, 0.0};
+    for (int m = 1; m < 3; m++) {
+        V3 vm = v3(evecs(0, m), evecs(1, m), evecs(2, m));
+        Mm[m] = vm * T(pn) + pn * T(vm);
+        den[m] = (plane.n) * (evals[0] - evals[m]);
+    }
     for (PointWithCov& pv : temp_points) {
-        Mat<6, 3> J;
+        const V3 d = pv.point - plane.mean;
         M3 F = M3::Zero();
         for (int m = 1; m < 3; m++) {
-            V3 vm = v3(evecs(0, m), evecs(1, m), evecs(2, m));
-            Mat<1, 3> Fm = (T(pv.point - plane.mean) / ((plane.n) * (evals[0] - evals[m]))) * (vm * T(pn) + pn * T(vm));
+            Mat<1, 3> Fm = (T(d) / den[m]) * Mm[m];
             F(m, 0) = Fm(0, 0); F(m, 1) = Fm(0, 1); F(m, 2) = Fm(0, 2);
         }
-        J.setBlock(0, 0, evecs * F);
-        J.setBlock(3, 0, J_Q);
-        plane.cov += J * pv.cov * T(J);
+        M3 top;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) top(i, j) = evecs(i, 1) * F(1, j) + evecs(i, 2) * F(2, j);
+        const M3 A = top * pv.cov;  // rows 0-2 of J * cov
+        M3 B;                       // rows 3-5
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) B(i, j) = inv_n * pv.cov(i, j);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                plane.cov(i, j) += (A(i, 0) * top(j, 0) + A(i, 1) * top(j, 1)) + A(i, 2) * top(j, 2);
+                plane.cov(i, 3 + j) += A(i, j) * inv_n;
+                plane.cov(3 + i, j) += (B(i, 0) * top(j, 0) + B(i, 1) * top(j, 1)) + B(i, 2) * top(j, 2);
+                plane.cov(3 + i, 3 + j) += B(i, j) * inv_n;
+            }
     }
     double axis_distance = -dot(plane.mean, pn);
     if (axis_distance < 0.0) pn = -pn;

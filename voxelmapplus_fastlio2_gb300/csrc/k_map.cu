@@ -303,35 +303,59 @@ __device__ void eig_sym3(const double* A, double* evals, double* evecs) {
     }
 }
 
-// Per-point term J * cov * J^T of VoxelGrid::updatePlane (voxel_map.cpp:115-130).
-__device__ void plane_cov_term(const double* p, const double* cov, const double* mean, int n, const double* ev,
-                               const double* evecs, double* out36) {
-    double pn[3] = {evecs[0], evecs[3], evecs[6]};
-    double F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    double d[3] = {p[0] - mean[0], p[1] - mean[1], p[2] - mean[2]};
-    for (int mm_ = 1; mm_ < 3; ++mm_) {
-        double vm[3] = {evecs[mm_], evecs[3 + mm_], evecs[6 + mm_]};
-        double den = (double)n * (ev[0] - ev[mm_]);
-        double dd[3] = {d[0] / den, d[1] / den, d[2] / den};
-        double M1[9], M2[9], M[9], Fm[3];
-        mm<3, 1, 3>(vm, pn, M1);
-        mm<3, 1, 3>(pn, vm, M2);
-        for (int k = 0; k < 9; ++k) M[k] = M1[k] + M2[k];
-        mm<1, 3, 3>(dd, M, Fm);
-        F[mm_ * 3] = Fm[0]; F[mm_ * 3 + 1] = Fm[1]; F[mm_ * 3 + 2] = Fm[2];
+// Per-refit factors of VoxelGrid::updatePlane's J (voxel_map.cpp:115-130):
+// J = [evecs * F; I / n], F row m = ((p - mean) / (n (l0 - lm)))^T (vm pn^T + pn vm^T).
+struct RefitConst {
+    double mean[3];
+    double evecs[9];
+    double M1[9], M2[9];
+    double den1, den2, inv_n;
+};
+__device__ inline void refit_const(const double* mean, int n, const double* ev, const double* evecs, RefitConst& k) {
+    const double pn[3] = {evecs[0], evecs[3], evecs[6]};
+    for (int q = 0; q < 3; ++q) k.mean[q] = mean[q];
+    for (int q = 0; q < 9; ++q) k.evecs[q] = evecs[q];
+    for (int m = 1; m < 3; ++m) {
+        const double vm[3] = {evecs[m], evecs[3 + m], evecs[6 + m]};
+        double* M = m == 1 ? k.M1 : k.M2;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) M[i * 3 + j] = vm[i] * pn[j] + pn[i] * vm[j];
     }
-    double J[18], top[9];
-    mm<3, 3, 3>(evecs, F, top);
-    const double inv_n = 1.0 / (double)n, zero_n = 0.0 / (double)n;
+    k.den1 = (double)n * (ev[0] - ev[1]);
+    k.den2 = (double)n * (ev[0] - ev[2]);
+    k.inv_n = 1.0 / (double)n;
+}
+
+// Per-point term J * cov * J^T, without the products with J's known zeros
+// (row 0 of F, the off-diagonal of I / n): the same sums without their +-0
+// terms, as the oracle forms them.
+__device__ inline void plane_cov_term(const double* p, const double* cov, const RefitConst& k, double* out36) {
+    const double d[3] = {p[0] - k.mean[0], p[1] - k.mean[1], p[2] - k.mean[2]};
+    double F1[3], F2[3];
+    {
+        const double a[3] = {d[0] / k.den1, d[1] / k.den1, d[2] / k.den1};
+        const double b[3] = {d[0] / k.den2, d[1] / k.den2, d[2] / k.den2};
+        for (int j = 0; j < 3; ++j) {
+            F1[j] = (a[0] * k.M1[j] + a[1] * k.M1[3 + j]) + a[2] * k.M1[6 + j];
+            F2[j] = (b[0] * k.M2[j] + b[1] * k.M2[3 + j]) + b[2] * k.M2[6 + j];
+        }
+    }
+    double top[9], A[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) top[i * 3 + j] = k.evecs[i * 3 + 1] * F1[j] + k.evecs[i * 3 + 2] * F2[j];
+    mm<3, 3, 3>(top, cov, A);
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
-            J[i * 3 + j] = top[i * 3 + j];
-            J[(3 + i) * 3 + j] = (i == j) ? inv_n : zero_n;
+            const double B_ij = k.inv_n * cov[i * 3 + j];
+            out36[i * 6 + j] = (A[i * 3] * top[j * 3] + A[i * 3 + 1] * top[j * 3 + 1]) + A[i * 3 + 2] * top[j * 3 + 2];
+            out36[i * 6 + 3 + j] = A[i * 3 + j] * k.inv_n;
+            out36[(3 + i) * 6 + 3 + j] = B_ij * k.inv_n;
         }
-    double T1[18], JT[18];
-    mm<6, 3, 3>(J, cov, T1);
-    tr<6, 3>(J, JT);
-    mm<6, 3, 6>(T1, JT, out36);
+    for (int i = 0; i < 3; ++i) {
+        const double B0 = k.inv_n * cov[i * 3], B1 = k.inv_n * cov[i * 3 + 1], B2 = k.inv_n * cov[i * 3 + 2];
+        for (int j = 0; j < 3; ++j)
+            out36[(3 + i) * 6 + j] = (B0 * top[j * 3] + B1 * top[j * 3 + 1]) + B2 * top[j * 3 + 2];
+    }
 }
 
 // ---------------------------------------------------------------- voxel state machine
@@ -614,6 +638,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
             double mn[3], ev[3], evecs[9];
             for (int k = 0; k < 3; ++k) { mn[k] = sn.mean[k]; ev[k] = sn.ev[k]; }
             for (int k = 0; k < 9; ++k) evecs[k] = sn.evecs[k];
+            RefitConst kc;
+            refit_const(mn, n, ev, evecs, kc);
             for (int base = 0; base < npts; base += 32) {
                 const int j = base + lane;
                 if (j < npts) {
@@ -627,7 +653,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
                     } else {
                         src = slab_pt(m, chunks, j);
                     }
-                    plane_cov_term(src, src + 3, mn, n, ev, evecs, stage[lane]);
+                    plane_cov_term(src, src + 3, kc, stage[lane]);
                 }
                 __syncwarp();
                 const int cnt = min(32, npts - base);
