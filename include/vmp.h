@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define VMP_ABI_VERSION 1
+#define VMP_ABI_VERSION 2
 
 typedef enum vmp_status {
     VMP_OK = 0,
@@ -282,6 +282,69 @@ int vmp_last_merge_rounds(vmp_stream_t s);
  * the last scan (kind 0 undistorted time-sorted cloud, 1 downsampled). */
 vmp_status vmp_residual_valid(vmp_stream_t s, unsigned char* valid, int n);
 vmp_status vmp_last_cloud(vmp_stream_t s, int kind, vmp_point* out, int max, int* n_out);
+/* Device memory a stream holds (all of it is allocated by vmp_create). */
+long long vmp_device_bytes(vmp_stream_t s);
+/* How vmp_process waits for its result: 0 (default) polls, lowest latency;
+ * 1 the calling thread sleeps until the GPU is done, for many streams driven
+ * by more threads than host cores (the server's workers use 1). */
+vmp_status vmp_set_wait_mode(vmp_stream_t s, int blocking);
+
+/* ------------------------------------------------------------------ serving
+ * Many independent sensor streams on one GPU.  No reference counterpart: the
+ * reference runs one LIOBuilder per ROS node (lio_node.cpp:263) and
+ * processes its packages one at a time on the timer thread
+ * (lio_node.cpp:167-182); a server runs many such streams at once.
+ *
+ * A server owns its streams (each a vmp_stream_t with its own map, filter
+ * and CUDA stream).  vmp_server_open_stream admits a stream while the sum of
+ * the admitted streams' device memory stays within the HBM budget and a slot
+ * is free, else returns VMP_ERR_ADMISSION_DENIED.  vmp_submit copies a
+ * package and returns at once.  Worker threads run each stream's packages in
+ * submission order and many streams at once, each on its own CUDA stream,
+ * so their kernels overlap on the GPU; a package submitted while others run
+ * starts as soon as a worker and its stream are free (continuous batching,
+ * not a queue drained batch by batch).  Results come back through vmp_poll.
+ * A stream's results do not depend on what else runs: the same packages give
+ * the same bits alone and in the mix.
+ *
+ * Threading: vmp_submit and vmp_poll may be called from any threads. */
+typedef struct vmp_server_s* vmp_server_t;
+
+typedef struct vmp_server_config {
+    long long hbm_budget_bytes; /* admission limit on the streams' device memory (default 150e9) */
+    int max_streams;            /* stream slots (default 64) */
+    int workers;                /* host threads driving streams concurrently (default 32) */
+    int queue_depth;            /* queued packages per stream before vmp_submit answers VMP_ERR_CAPACITY (default 64) */
+    int reserved[7];
+} vmp_server_config;
+
+typedef struct vmp_server_result {
+    long long cookie;  /* as given to vmp_submit */
+    int stream_id;
+    int status;        /* vmp_status of the package */
+    double submit_ms;  /* server clock (ms since vmp_server_create) at vmp_submit */
+    double start_ms;   /* when a worker started the package */
+    double end_ms;     /* when its result was on the host */
+    vmp_result result;
+} vmp_server_result;
+
+void vmp_server_config_default(vmp_server_config* c);
+vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out);
+/* Waits for the packages that are running; queued ones are dropped. */
+vmp_status vmp_server_destroy(vmp_server_t sv);
+vmp_status vmp_server_open_stream(vmp_server_t sv, const vmp_config* cfg, int* stream_id);
+/* Waits until the stream's queued packages are done, then frees it. */
+vmp_status vmp_server_close_stream(vmp_server_t sv, int stream_id);
+vmp_status vmp_submit(vmp_server_t sv, int stream_id, const vmp_scan* scan, const vmp_imu* imus, int n_imu,
+                      long long cookie);
+/* Moves up to max finished results to out (completion order), waiting up to
+ * timeout_ms for the first one; returns how many, or -1 on a bad argument. */
+int vmp_poll(vmp_server_t sv, vmp_server_result* out, int max, int timeout_ms);
+/* Waits until the stream is idle and returns its handle (map export, state
+ * reads); the handle stays owned by the server. */
+vmp_status vmp_server_stream(vmp_server_t sv, int stream_id, vmp_stream_t* out);
+vmp_status vmp_server_info(vmp_server_t sv, long long* budget_used, int* streams_open, int* queued, int* running);
+const char* vmp_server_last_error(vmp_server_t sv);
 
 #ifdef __cplusplus
 }

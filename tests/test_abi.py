@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol():
     lib = C.CDLL(_lib.LIB_PATH)
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.vmp_abi_version() == 1
+    assert lib.vmp_abi_version() == 2
 
 
 def test_config_default_matches_lioconfig():
@@ -60,13 +60,14 @@ def test_config_default_matches_lioconfig():
 
 def test_struct_layouts_match_c():
     structs = ["vmp_config", "vmp_point", "vmp_imu", "vmp_scan", "vmp_state", "vmp_result", "vmp_map_info",
-               "vmp_voxel"]
+               "vmp_voxel", "vmp_server_config", "vmp_server_result"]
     src = '#include <stdio.h>\n#include <stddef.h>\n#include "vmp.h"\nint main(void){\n'
     for s in structs:
         src += f'printf("{s} %zu\\n", sizeof({s}));\n'
     src += 'printf("off_result_x %zu\\n", offsetof(vmp_result, x));\n'
     src += 'printf("off_voxel_mean %zu\\n", offsetof(vmp_voxel, mean));\n'
-    src += 'printf("off_config_map_capacity %zu\\n", offsetof(vmp_config, map_capacity));\nreturn 0;}\n'
+    src += 'printf("off_config_map_capacity %zu\\n", offsetof(vmp_config, map_capacity));\n'
+    src += 'printf("off_sres_result %zu\\n", offsetof(vmp_server_result, result));\nreturn 0;}\n'
     with tempfile.TemporaryDirectory() as d:
         cfile = os.path.join(d, "t.c")
         exe = os.path.join(d, "t")
@@ -79,6 +80,7 @@ def test_struct_layouts_match_c():
     assert int(sizes["off_result_x"]) == abi.vmp_result.x.offset
     assert int(sizes["off_voxel_mean"]) == abi.vmp_voxel.mean.offset
     assert int(sizes["off_config_map_capacity"]) == abi.vmp_config.map_capacity.offset
+    assert int(sizes["off_sres_result"]) == abi.vmp_server_result.result.offset
 
 
 def test_no_gpu_path_fails_loudly():

@@ -1,0 +1,113 @@
+"""Serving (many streams on one GPU) through libvmp's server API.
+
+The reference has no serving layer; these tests pin the server's contract:
+each stream's results are bit-identical alone and in the mix (their work
+overlaps on the device), per-stream order is kept, admission follows the HBM
+budget, and a closed stream frees its budget.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from voxelmapplus_fastlio2_gb300 import abi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _packages(kind, seed, pts, count):
+    seq = synth.Sequence(kind, seed=seed, points_per_scan=pts)
+    return [seq.next() for _ in range(count)]
+
+
+def _cfg(kind):
+    if kind == synth.KIND_URBAN:
+        return abi.default_config(scan_resolution=0.1, map_capacity=300000, max_scan_points=40064, ieskf_max_iter=4)
+    return abi.default_config(scan_resolution=0.2, map_capacity=100000, max_scan_points=16384)
+
+
+def _key(res):
+    """The bits of a result that must not depend on the other streams."""
+    return (res.lio_status, res.iters, res.effect_num, res.n_raw, res.n_down, res.map_size, bytes(res.x),
+            bytes(res.P))
+
+
+def _run_server(streams, workers, concurrent):
+    """streams: list of (kind, packages).  concurrent=False submits one
+    stream's next package only after the previous stream's finished."""
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    srv = Server(hbm_budget_bytes=150e9, max_streams=len(streams), workers=workers)
+    try:
+        sids = [srv.open_stream(_cfg(kind)) for kind, _ in streams]
+        out = {sid: [] for sid in sids}
+        if concurrent:
+            total = 0
+            for k in range(max(len(p) for _, p in streams)):
+                for sid, (_, pk) in zip(sids, streams):
+                    if k < len(pk):
+                        srv.submit(sid, pk[k], cookie=k)
+                        total += 1
+            got = 0
+            while got < total:
+                for r in srv.poll(timeout_ms=1000):
+                    assert r.status == abi.VMP_OK, r.status
+                    out[r.stream_id].append((r.cookie, _key(r.result)))
+                    got += 1
+        else:
+            for sid, (_, pk) in zip(sids, streams):
+                for k, p in enumerate(pk):
+                    srv.submit(sid, p, cookie=k)
+                    rs = []
+                    while not rs:
+                        rs = srv.poll(timeout_ms=1000)
+                    assert len(rs) == 1 and rs[0].status == abi.VMP_OK
+                    out[sid].append((rs[0].cookie, _key(rs[0].result)))
+        maps = {}
+        for sid in sids:
+            v, n = srv.stream(sid).map.export()
+            maps[sid] = C.string_at(v, n * C.sizeof(abi.vmp_voxel))
+        return [out[s] for s in sids], [maps[s] for s in sids]
+    finally:
+        srv.close()
+
+
+def test_alone_equals_mix():
+    """Eight streams (rooms and urban blocks, own seeds and scan sizes):
+    every per-scan result and every final map is the same bits whether the
+    streams run one at a time or all at once on 8 workers."""
+    streams = []
+    for i in range(8):
+        kind = synth.KIND_ROOM if i % 2 == 0 else synth.KIND_URBAN
+        pts = [3000, 20000, 8000, 40000, 12000, 30000, 5000, 25000][i]
+        streams.append((kind, _packages(kind, 0x5EED0000 + 100 + i, pts, 8)))
+    alone, maps_alone = _run_server(streams, workers=1, concurrent=False)
+    mix, maps_mix = _run_server(streams, workers=8, concurrent=True)
+    for i, (a, b) in enumerate(zip(alone, mix)):
+        assert [c for c, _ in b] == list(range(len(streams[i][1])))  # per-stream order kept
+        assert [k for _, k in a] == [k for _, k in b], f"stream {i} differs between alone and mix"
+        assert maps_alone[i] == maps_mix[i], f"stream {i} map differs"
+
+
+def test_admission_by_budget_and_release():
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    from voxelmapplus_fastlio2_gb300._lib import VmpError
+    srv = Server(hbm_budget_bytes=150e9, max_streams=8, workers=2)
+    try:
+        a = srv.open_stream(_cfg(synth.KIND_ROOM))
+        one = srv.info()["budget_used"]
+        assert one > 0
+    finally:
+        srv.close()
+    srv = Server(hbm_budget_bytes=int(2.5 * one), max_streams=8, workers=2)
+    try:
+        a = srv.open_stream(_cfg(synth.KIND_ROOM))
+        b = srv.open_stream(_cfg(synth.KIND_ROOM))
+        with pytest.raises(VmpError) as e:
+            srv.open_stream(_cfg(synth.KIND_ROOM))
+        assert e.value.code == abi.VMP_ERR_ADMISSION_DENIED
+        assert srv.info()["streams_open"] == 2
+        srv.close_stream(a)
+        c = srv.open_stream(_cfg(synth.KIND_ROOM))  # the freed budget admits a new stream
+        assert srv.info()["streams_open"] == 2 and c != b
+    finally:
+        srv.close()

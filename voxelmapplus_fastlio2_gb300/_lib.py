@@ -56,6 +56,18 @@ def _declare(lib):
         "vmp_launch_count": ([], C.c_longlong),
         "vmp_io_bytes": ([vp, P(C.c_longlong), P(C.c_longlong)], st),
         "vmp_last_merge_rounds": ([vp], C.c_int),
+        "vmp_device_bytes": ([vp], C.c_longlong),
+        "vmp_set_wait_mode": ([vp, C.c_int], st),
+        "vmp_server_config_default": ([P(abi.vmp_server_config)], None),
+        "vmp_server_create": ([P(abi.vmp_server_config), P(vp)], st),
+        "vmp_server_destroy": ([vp], st),
+        "vmp_server_open_stream": ([vp, P(abi.vmp_config), P(C.c_int)], st),
+        "vmp_server_close_stream": ([vp, C.c_int], st),
+        "vmp_submit": ([vp, C.c_int, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, C.c_longlong], st),
+        "vmp_poll": ([vp, P(abi.vmp_server_result), C.c_int, C.c_int], C.c_int),
+        "vmp_server_stream": ([vp, C.c_int, P(vp)], st),
+        "vmp_server_info": ([vp, P(C.c_longlong), P(C.c_int), P(C.c_int), P(C.c_int)], st),
+        "vmp_server_last_error": ([vp], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -11,6 +11,7 @@ STATUS_NAMES = {
     4: "VMP_ERR_HASH_FULL", 5: "VMP_ERR_TIMEOUT", 6: "VMP_ERR_CUDA", 7: "VMP_ERR_KEY_RANGE",
     8: "VMP_ERR_STATE", 9: "VMP_ERR_CAPACITY",
 }
+VMP_ERR_INVALID_ARG, VMP_ERR_ADMISSION_DENIED, VMP_ERR_CAPACITY = 1, 3, 9
 IMU_INIT, MAP_INIT, LIO_MAPPING = 0, 1, 2
 
 
@@ -115,6 +116,17 @@ def default_config(**kw):
         else:
             setattr(c, k, v)
     return c
+
+
+class vmp_server_config(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_longlong), ("max_streams", C.c_int), ("workers", C.c_int),
+                ("queue_depth", C.c_int), ("reserved", C.c_int * 7)]
+
+
+class vmp_server_result(C.Structure):
+    _fields_ = [("cookie", C.c_longlong), ("stream_id", C.c_int), ("status", C.c_int),
+                ("submit_ms", C.c_double), ("start_ms", C.c_double), ("end_ms", C.c_double),
+                ("result", vmp_result)]
 
 
 def state_to_dict(x):

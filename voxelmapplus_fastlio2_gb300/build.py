@@ -34,6 +34,7 @@ CU_SOURCES = [
     "k_map.cu",
     "k_merge.cu",
     "vmp_noalloc.cu",
+    "vmp_server.cu",
 ]
 
 
@@ -84,7 +85,7 @@ def build_vmp(verbose=False, extra=()):
             sys.stdout.write(o)
     so = os.path.join(OUT, "libvmp.so")
     if _stale(so, objs):
-        _run([NVCC] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
+        _run([NVCC] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart", "-lpthread"])
     return so
 
 

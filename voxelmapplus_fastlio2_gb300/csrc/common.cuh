@@ -464,6 +464,18 @@ __device__ inline void state_minus(const DState& x, const DState& o, double* d) 
     s2_minus(x.g, o.g, d + 21);
 }
 
+// ----- device allocations
+// Bytes of device memory allocated through dev_malloc by the calling thread;
+// vmp_create reads it around a stream's allocations (its footprint, which the
+// server's HBM admission adds up).
+long long& dev_bytes_counter();
+template <class T>
+inline cudaError_t dev_malloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n);
+    if (e == cudaSuccess) dev_bytes_counter() += (long long)n;
+    return e;
+}
+
 // ----- error reporting
 __device__ inline void set_error(Counters* c, uint32_t bit) { atomicOr(&c->error, bit); }
 

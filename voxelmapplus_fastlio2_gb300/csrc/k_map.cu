@@ -945,15 +945,15 @@ cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
     uint32_t** u32s[] = {&ms.slot, &ms.rec, &ms.flag, &ms.rank, &ms.flag2, &ms.rank2, &ms.sk, &ms.sv, &ms.seg_start, &ms.seg_end,
                          &ms.seg_rec, &ms.ev_rec, &ms.ev_list, &ms.last_touch, &ms.victims, &ms.new_pos};
     for (auto pp : u32s)
-        if ((e = cudaMalloc(pp, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
+        if ((e = dev_malloc(pp, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
     if ((e = merge_scratch_alloc(&ms.merge, max_batch, rec_pool)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&ms.seg_snaps, sizeof(RefitSnap) * nb)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&ms.covsegs, sizeof(CovSeg) * nb)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&ms.refit_list, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.seg_snaps, sizeof(RefitSnap) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.covsegs, sizeof(CovSeg) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.refit_list, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
     ms.merge_mode = 0;
     ms.merge_rounds = 0;
     ms.merge_d2h = 0;
-    if ((e = cudaMalloc(&ms.d_scratch_int, sizeof(int) * 32)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.d_scratch_int, sizeof(int) * 32)) != cudaSuccess) return e;
     ms.d_n = ms.d_scratch_int;
     ms.d_n_new = ms.d_scratch_int + 1;
     ms.d_n_seg = ms.d_scratch_int + 2;

@@ -29,6 +29,7 @@
 // overflows or a barrier wait runs out, a single-thread replay in point order
 // runs instead.  Both paths do the reference's arithmetic in its order.
 #include <cstring>
+#include <mutex>
 #include "kernels.cuh"
 
 namespace vmp {
@@ -524,15 +525,15 @@ cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool) {
     ms->rec_pool = rec_pool;
     cudaError_t e;
     for (int b = 0; b < kLogs; ++b) {
-        if ((e = cudaMalloc(&ms->ent[b], sizeof(MEntry) * (size_t)ms->pool)) != cudaSuccess) return e;
-        if ((e = cudaMalloc(&ms->head[b], sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
+        if ((e = dev_malloc(&ms->ent[b], sizeof(MEntry) * (size_t)ms->pool)) != cudaSuccess) return e;
+        if ((e = dev_malloc(&ms->head[b], sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
         if ((e = cudaMemset(ms->head[b], 0xFF, sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
     }
     const size_t nb = (size_t)max_batch + 16;
-    if ((e = cudaMalloc(&ms->sig, sizeof(uint64_t) * nb)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&ms->cand, sizeof(uint32_t) * 6 * nb)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&ms->queue, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&ms->ctl, sizeof(MergeCtl))) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms->sig, sizeof(uint64_t) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms->cand, sizeof(uint32_t) * 6 * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms->queue, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms->ctl, sizeof(MergeCtl))) != cudaSuccess) return e;
     if ((e = cudaMemset(ms->ctl, 0, sizeof(MergeCtl))) != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -570,11 +571,24 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     // converged = 0; wait_error, pad, bar_count = 0 (bar_gen keeps counting)
     if ((e = cudaMemsetAsync(&g.ctl->converged, 0, sizeof(int) * 3 + sizeof(unsigned int), st)) != cudaSuccess) return e;
     if (g.coop_grid > 0) {
+        // One cooperative kernel on the device at a time: two of them, each
+        // holding part of the SMs while waiting for its remaining CTAs, could
+        // wait on each other.  Every launch (from any stream of the process)
+        // waits for the previous one.
+        static std::mutex mu;
+        static cudaEvent_t last_done = nullptr;
+        std::lock_guard<std::mutex> lk(mu);
+        if (!last_done && cudaEventCreateWithFlags(&last_done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            last_done = nullptr;
+        }
+        if (last_done) cudaStreamWaitEvent(st, last_done, 0);
         void* args[] = {(void*)&m, (void*)&g, (void*)&ms.ev_list, (void*)&ms.ev_rec, (void*)&ms.d_n_ev};
         VMP_NOTE_LAUNCH();
         e = cudaLaunchCooperativeKernel((const void*)k_merge_fixpoint, dim3(g.coop_grid), dim3(kMergeThreads), args, 0,
                                         st);
         if (e != cudaSuccess) cudaGetLastError();  // the replay below produces the result
+        if (last_done) cudaEventRecord(last_done, st);
     }
     VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev, g.ctl);
     return cudaGetLastError();

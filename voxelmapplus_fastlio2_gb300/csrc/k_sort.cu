@@ -15,6 +15,11 @@ namespace vmp {
 
 std::atomic<long long> g_launch_count{0};
 
+long long& dev_bytes_counter() {
+    static thread_local long long bytes = 0;
+    return bytes;
+}
+
 __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __restrict__ d_n, int shift,
                              uint32_t* __restrict__ hist, int blocks) {
     __shared__ uint32_t cnt[256];
@@ -116,10 +121,10 @@ cudaError_t sort_scratch_alloc(SortScratch& s, int n_max) {
     s.blocks = (n_max + kSortTile - 1) / kSortTile;
     if (s.blocks < 1) s.blocks = 1;
     cudaError_t e;
-    if ((e = cudaMalloc(&s.k_alt, sizeof(uint32_t) * (size_t)n_max + 16)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&s.v_alt, sizeof(uint32_t) * (size_t)n_max + 16)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * 256 * (size_t)s.blocks)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&s.row_total, sizeof(uint32_t) * 256)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&s.k_alt, sizeof(uint32_t) * (size_t)n_max + 16)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&s.v_alt, sizeof(uint32_t) * (size_t)n_max + 16)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&s.hist, sizeof(uint32_t) * 256 * (size_t)s.blocks)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&s.row_total, sizeof(uint32_t) * 256)) != cudaSuccess) return e;
     return cudaSuccess;
 }
 void sort_scratch_free(SortScratch& s) {
@@ -241,7 +246,7 @@ cudaError_t scan_scratch_alloc(ScanScratch& s, int n_max) {
     s.n_max = n_max;
     s.blocks = (n_max + kScanTile - 1) / kScanTile;
     if (s.blocks < 1) s.blocks = 1;
-    return cudaMalloc(&s.block_sums, sizeof(uint32_t) * (size_t)s.blocks + 16);
+    return dev_malloc(&s.block_sums, sizeof(uint32_t) * (size_t)s.blocks + 16);
 }
 void scan_scratch_free(ScanScratch& s) {
     cudaFree(s.block_sums);

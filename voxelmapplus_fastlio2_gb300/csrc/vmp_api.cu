@@ -251,6 +251,9 @@ struct vmp_stream_s {
     std::vector<void*> allocs;
     bool broken = false;
     long long last_evicted_total = 0;
+    long long dev_bytes = 0;  // device memory allocated by vmp_create
+    bool blocking_wait = false;  // vmp_set_wait_mode
+    cudaEvent_t done_ev = nullptr;
     // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
     // the stream's own CUDA stream, resolved after the call's final sync
     struct ProfRec { int slot; int items_kind; cudaEvent_t a, b; };
@@ -331,7 +334,7 @@ static vmp_status cuda_fail(vmp_stream_t s, cudaError_t e, const char* where) {
 
 template <typename T>
 static cudaError_t dalloc(vmp_stream_t s, T** p, size_t count) {
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count < 1 ? 1 : count));
+    cudaError_t e = dev_malloc(p, sizeof(T) * (count < 1 ? 1 : count));
     if (e == cudaSuccess) s->allocs.push_back(*p);
     return e;
 }
@@ -405,6 +408,7 @@ vmp_status vmp_destroy(vmp_stream_t s) {
     cudaFreeHost(s->h_res);
     cudaFreeHost(s->h_cnt);
     cudaFreeHost(s->h_int);
+    if (s->done_ev) cudaEventDestroy(s->done_ev);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return VMP_OK;
@@ -430,6 +434,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     vmp_stream_t s = new (std::nothrow) vmp_stream_s();
     if (!s) return VMP_ERR_OUT_OF_MEMORY;
     s->cfg = cfg;
+    const long long bytes0 = dev_bytes_counter();
     cudaError_t e;
 #define CREATE_TRY(expr)                         \
     do {                                         \
@@ -441,6 +446,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
         }                                        \
     } while (0)
     CREATE_TRY(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    CREATE_TRY(cudaEventCreateWithFlags(&s->done_ev, cudaEventBlockingSync | cudaEventDisableTiming));
     const int max_pts = cfg.max_scan_points;
     const int max_imu = cfg.max_imu_per_scan;
     s->sin_deg = std::sin(cfg.angle_cov * 0.017453293);  // pcl_macros.h DEG2RAD
@@ -553,6 +559,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     CREATE_TRY(cudaGetLastError());
     CREATE_TRY(cudaStreamSynchronize(s->st));
 #undef CREATE_TRY
+    s->dev_bytes = dev_bytes_counter() - bytes0;
     *out = s;
     return VMP_OK;
 }
@@ -690,7 +697,12 @@ static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
     VMP_TRY(cudaMemcpyAsync(s->h_res, s->d_res, sizeof(DResult), cudaMemcpyDeviceToHost, s->st), "result copy");
     s->io_d2h += (long long)sizeof(DResult);
     s->pend(VMP_PROF_RESULT, -1);
-    VMP_TRY(cudaStreamSynchronize(s->st), "scan");
+    if (s->blocking_wait && s->done_ev) {
+        VMP_TRY(cudaEventRecord(s->done_ev, s->st), "scan");
+        VMP_TRY(cudaEventSynchronize(s->done_ev), "scan");
+    } else {
+        VMP_TRY(cudaStreamSynchronize(s->st), "scan");
+    }
     const DResult& r = *s->h_res;
     s->pflush(r.iters, n_raw, r.n_down, r.n_down);
     s->h_size = r.cnt.size;
@@ -739,17 +751,37 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
         size_t old = s->imu_cache.size();
         s->imu_cache.resize(old + n_imu);
         if (device_ptrs) {
-            VMP_TRY(cudaMemcpy(s->imu_cache.data() + old, imus, sizeof(vmp_imu) * n_imu, cudaMemcpyDeviceToHost), "imu read");
+            VMP_TRY(cudaMemcpyAsync(s->imu_cache.data() + old, imus, sizeof(vmp_imu) * n_imu, cudaMemcpyDeviceToHost, st),
+                    "imu read");
+            VMP_TRY(cudaStreamSynchronize(st), "imu read");
         } else {
             std::memcpy(s->imu_cache.data() + old, imus, sizeof(vmp_imu) * n_imu);
         }
         if ((int)s->imu_cache.size() >= cfg.imu_init_num) {
-            vmp_imu* d_all = nullptr;
-            VMP_TRY(cudaMalloc(&d_all, sizeof(vmp_imu) * s->imu_cache.size()), "imu init alloc");
-            cudaMemcpyAsync(d_all, s->imu_cache.data(), sizeof(vmp_imu) * s->imu_cache.size(), cudaMemcpyHostToDevice, st);
-            launch_imu_init(s->f, d_all, (int)s->imu_cache.size(), cfg, t_end, st);
+            // all samples go to the device in one copy through the package
+            // IMU buffers (max_imu_per_scan + 8 samples); a longer
+            // initialisation window takes a stream-ordered temporary.  No
+            // cudaMalloc / cudaFree: they would synchronise the whole device
+            // and stall the other streams of a server.
+            const size_t cnt = s->imu_cache.size();
+            const size_t cap = (size_t)cfg.max_imu_per_scan + 8;
+            vmp_imu* d_all = s->s.imus;
+            vmp_imu* d_tmp = nullptr;
+            VMP_TRY(cudaStreamSynchronize(st), "sync");
+            if (cnt > cap) {
+                VMP_TRY(cudaMallocAsync(&d_tmp, sizeof(vmp_imu) * cnt, st), "imu init alloc");
+                d_all = d_tmp;
+                VMP_TRY(cudaMemcpyAsync(d_all, s->imu_cache.data(), sizeof(vmp_imu) * cnt, cudaMemcpyHostToDevice, st),
+                        "imu init upload");
+                VMP_TRY(cudaStreamSynchronize(st), "sync");
+            } else {
+                std::memcpy(s->h_imus, s->imu_cache.data(), sizeof(vmp_imu) * cnt);
+                VMP_TRY(cudaMemcpyAsync(d_all, s->h_imus, sizeof(vmp_imu) * cnt, cudaMemcpyHostToDevice, st),
+                        "imu init upload");
+            }
+            launch_imu_init(s->f, d_all, (int)cnt, cfg, t_end, st);
+            if (d_tmp) cudaFreeAsync(d_tmp, st);
             cudaError_t e = cudaStreamSynchronize(st);
-            cudaFree(d_all);
             if (e != cudaSuccess) return cuda_fail(s, e, "imu init");
             s->imu_cache.clear();
             s->lio_status = VMP_MAP_INIT;
@@ -1157,6 +1189,12 @@ long long vmp_launch_count(void) { return g_launch_count.load(std::memory_order_
 vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode) {
     if (!s || mode < 0 || mode > 1) return VMP_ERR_INVALID_ARG;
     s->ms.merge_mode = mode;
+    return VMP_OK;
+}
+long long vmp_device_bytes(vmp_stream_t s) { return s ? s->dev_bytes : -1; }
+vmp_status vmp_set_wait_mode(vmp_stream_t s, int blocking) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    s->blocking_wait = blocking != 0;
     return VMP_OK;
 }
 int vmp_last_merge_rounds(vmp_stream_t s) { return s ? merge_rounds_read(s->ms.merge, s->st) : -1; }

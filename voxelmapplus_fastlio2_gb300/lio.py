@@ -121,10 +121,23 @@ class LIOBuilder:
         self.map = VoxelMapView(self)
         self.kf = IESKFView(self)
 
+    @classmethod
+    def view(cls, lib, handle, config):
+        """A LIOBuilder over a handle owned elsewhere (a server's stream):
+        the same calls, and close() leaves the handle alone."""
+        obj = cls.__new__(cls)
+        obj.lib = lib
+        obj.cfg = config
+        obj.h = handle
+        obj._borrowed = True
+        obj.map = VoxelMapView(obj)
+        obj.kf = IESKFView(obj)
+        return obj
+
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not getattr(self, "_borrowed", False):
             self.lib.vmp_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
