@@ -1,29 +1,40 @@
 #!/usr/bin/env python
-"""Odometry-step benchmark of the GB300 hot path (one JSON line on stdout).
+"""Benchmark of the GB300 odometry hot path (one JSON line on stdout).
 
-A step is LIOBuilder::process on one LiDAR package in the LIO_MAPPING state:
+Metric: scans/s and p99 per-scan latency of the 64-stream served form, next
+to the plain one-stream GPU path and the CPU reference restatement.  A step
+(scan) is LIOBuilder::process on one LiDAR package in the LIO_MAPPING state:
 time sort, IMU predict chain, undistortion, downsample, iterated EKF update
-(ieskf_max_iter residual launches) and the voxel-map update.
+and the voxel-map update.
 
-Workload (default, `--workload urban`): the seeded synthetic 100 x 100 x 20 m
-urban block -- ground, random facades, 5 % clutter points -- seen by a
-spinning 128-beam LiDAR, 200 000 rays per scan at 10 Hz (about 173 000 returns),
-float32 points, 3 cm range noise, 200 Hz IMU, 0.1 m scan downsample, 0.5 m
-voxels, LRU capacity 4 M voxels, 4 IEKF iterations per scan.
-
-Arms:
-  value  scans/s with every package already in HBM (vmp_process_device),
-         per-step CUDA events on the library's stream, L2 flushed (256 MB
-         write) before each step outside the timed events;
-  e2e    scans/s through vmp_process from pinned host buffers: each step's
-         host->device copy of the scan + IMU samples and the device->host
-         result copy are inside the (wall-clock) timing;
+Default workload (`--workload serve`): 64 independent sensor streams on one
+GPU, each with its own seeded scene and trajectory -- even streams the
+20 x 20 x 5 m room seen by a rosette LiDAR, odd ones the 100 x 100 x 20 m
+urban block seen by a spinning 128-beam LiDAR -- with rays per scan drawn
+uniformly from [2k, 200k], 200 Hz IMU, 0.5 m voxels, admitted under a 150 GB
+HBM budget, served by libvmp's server (vmp_submit / vmp_poll).
+  value     scans/s of all streams: `--steps` mapping scans per stream, the
+            packages already in HBM (vmp_submit_device), all submitted at
+            once, wall time until the last result is on the host;
+  e2e       the same from host memory (vmp_submit copies each package; the
+            host->device copies and the result reads are inside the timing);
+  latency   open loop: each stream a Poisson process at 10 Hz, p50 / p99 of
+            (result on host - submission);
+  plain_1stream  the same streams and packages with one package on the GPU
+            at a time (one worker), and the one-stream urban block (200k
+            rays, 4 M voxel capacity) with its per-phase CUDA-event profile,
+            which gives the kernel roofline;
   cpu_baseline  the CPU oracle (restated reference, one thread as the
-         reference's MP_PROC_NUM=1) on a bounded sample of the same scans.
-`--impl reference` times that CPU restatement with all host threads instead.
+            reference's MP_PROC_NUM=1) on a bounded sample of the streams.
+`--impl reference` runs the CPU restatement on all streams of the served
+workload, one single-threaded oracle per stream, all host cores.
 
-Multi-GPU: streams shard by GPU (one independent sensor stream per rank,
-seed 0x5EED0000 + rank), no collective on the data path; "scaling": "weak".
+`--workload urban|room` runs the plain one-stream path alone (value: HBM
+resident with per-step CUDA events and an L2 flush between steps; e2e: from
+pinned host buffers).
+
+Multi-GPU: streams shard by GPU (each rank serves its own streams), no
+collective on the data path; "scaling": "weak".
 """
 import argparse
 import ctypes as C
@@ -58,21 +69,33 @@ PROF_NAMES = ["upload", "time_sort", "predict", "undistort", "downsample", "body
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed scans (per stream for the served workload; default 8 there, 60 otherwise)")
+    ap.add_argument("--warmup", type=int, default=None, help="warm-up scans (default 3 served, 5 otherwise)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="urban", choices=["urban", "room"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room"])
+    ap.add_argument("--streams", type=int, default=64, help="served workload: concurrent sensor streams")
+    ap.add_argument("--workers", type=int, default=0, help="served workload: server worker threads (0: streams, <= 64)")
+    ap.add_argument("--open-loop-scans", type=int, default=15, help="served workload: 10 Hz scans per stream")
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
+    ap.add_argument("--plain-steps", type=int, default=30, help="served workload: steps of the plain urban run")
     ap.add_argument("--points", type=int, default=None, help="rays per scan (default: workload's)")
+    ap.add_argument("--map-capacity", type=int, default=None, help="plain workloads: LRU voxel capacity")
     ap.add_argument("--cpu-sample", type=int, default=None, help="CPU-baseline scans (default: bounded)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--flush-mb", type=int, default=256)
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.steps is None:
+        a.steps = 8 if a.workload == "serve" else 60
+    if a.warmup is None:
+        a.warmup = 3 if a.workload == "serve" else 5
+    return a
 
 
-def workload(args, rank):
+def workload(args, rank, name=None):
     from voxelmapplus_fastlio2_gb300 import abi, synth
-    if args.workload == "urban":
+    if (name or args.workload) == "urban":
         kind, pts, leaf, cap, iters = synth.KIND_URBAN, 200000, 0.1, 4000000, 4
         name = "urban block 100x100x20 m, spinning 128-beam, 200k rays/scan"
     else:
@@ -80,6 +103,8 @@ def workload(args, rank):
         name = "room 20x20x5 m, rosette, 20k rays/scan"
     if args.points:
         pts = args.points
+    if getattr(args, "map_capacity", None):
+        cap = args.map_capacity
     cfg = abi.default_config(scan_resolution=leaf, map_capacity=cap, ieskf_max_iter=iters,
                              max_scan_points=max(1024, pts + 64))
     seed = 0x5EED0000 + rank
@@ -284,6 +309,163 @@ def run_cpu(pkgs, cfg, n_init, warmup, sample, threads):
     return t
 
 
+# ------------------------------------------------------------------ served
+def serve_streams(args, rank):
+    """The served workload: per stream (kind, rays per scan, config, seed).
+    Even streams are rooms, odd ones urban blocks, each with its own seeded
+    scene and trajectory; rays per scan uniform in [2k, 200k]."""
+    from voxelmapplus_fastlio2_gb300 import abi, synth
+    rng = np.random.default_rng(0x5EED + rank)
+    out = []
+    for s in range(args.streams):
+        kind = synth.KIND_ROOM if s % 2 == 0 else synth.KIND_URBAN
+        rays = int(rng.integers(2000, 200001))
+        if kind == synth.KIND_URBAN:
+            cfg = abi.default_config(scan_resolution=0.1, map_capacity=400000, ieskf_max_iter=4,
+                                     max_scan_points=rays + 64)
+        else:
+            cfg = abi.default_config(scan_resolution=0.2, map_capacity=100000, max_scan_points=rays + 64)
+        out.append((kind, rays, cfg, 0x5EED0000 + 1000 * rank + 16 + s))
+    return out
+
+
+def make_serve_packages(streams, count):
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        return list(ex.map(lambda st: make_packages(st[0], st[1], st[3], count), streams))
+
+
+def _drain(srv, total, timeout_s=600.0):
+    res, t_end = [], time.perf_counter() + timeout_s
+    while len(res) < total:
+        if time.perf_counter() > t_end:
+            raise RuntimeError(f"served run timed out with {len(res)} of {total} results")
+        for r in srv.poll(max_results=1024, timeout_ms=200):
+            if r.status != 0:
+                raise RuntimeError(f"stream {r.stream_id} package {r.cookie}: status {r.status}")
+            res.append(r)
+    return res
+
+
+def _stage_device(pk):
+    import torch
+    pts, imu = pkg_arrays(pk)
+    return torch.from_numpy(pts).cuda(), torch.from_numpy(imu).cuda()
+
+
+def run_served(args, streams, pkgs, workers, phases, barrier):
+    """One server, all streams.  Per stream the packages run in order:
+    IMU_INIT + MAP_INIT + warm-up, then the phases:
+      "device": K packages per stream, already in HBM, all submitted at once;
+      "host":   K packages per stream from host memory (vmp_submit copies);
+      "open":   open loop, each stream a Poisson process at 10 Hz for L
+                packages, host memory.
+    Returns per phase: scans/s, latencies, launches, clocks."""
+    import torch
+    from voxelmapplus_fastlio2_gb300 import lio as vlio
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    W, K, L = args.warmup, args.steps, args.open_loop_scans
+    srv = Server(hbm_budget_bytes=args.hbm_budget_gb * 1e9, max_streams=len(streams), workers=workers,
+                 queue_depth=max(64, K + L + 8))
+    out = {}
+    try:
+        sids = [srv.open_stream(cfg) for (_, _, cfg, _) in streams]
+        out["budget_used_gb"] = srv.info()["budget_used"] / 1e9
+        n0 = 2 + W
+        for k in range(n0):
+            for sid, pk in zip(sids, pkgs):
+                srv.submit(sid, pk[k], cookie=k)
+        _drain(srv, n0 * len(sids))
+        nxt = n0
+        lib = vlio.load()
+        for ph in phases:
+            if ph == "device":
+                dev = [[_stage_device(pk[nxt + k]) for k in range(K)] for pk in pkgs]
+                torch.cuda.synchronize()
+            barrier()
+            clocks = ClockSampler(torch.cuda.current_device())
+            clocks.start()
+            time.sleep(0.3)
+            l0 = lib.vmp_launch_count()
+            t0 = time.perf_counter()
+            if ph in ("device", "host"):
+                for k in range(K):
+                    for i, (sid, pk) in enumerate(zip(sids, pkgs)):
+                        p = pk[nxt + k]
+                        if ph == "device":
+                            d_pts, d_imu = dev[i][k]
+                            srv.submit_device(sid, d_pts.data_ptr(), p.n, p.t_start, p.t_end, d_imu.data_ptr(),
+                                              p.n_imu, cookie=nxt + k)
+                        else:
+                            srv.submit(sid, p, cookie=nxt + k)
+                res = _drain(srv, K * len(sids))
+                nxt += K
+            else:
+                rng = np.random.default_rng(7)
+                events = []
+                for i in range(len(sids)):
+                    t = float(rng.uniform(0.0, 0.1))
+                    for k in range(L):
+                        events.append((t, i, nxt + k))
+                        t += float(rng.exponential(0.1))
+                events.sort()
+                got = []
+                th = threading.Thread(target=lambda: got.extend(_drain(srv, len(events))))
+                th.start()
+                for t, i, k in events:
+                    dt = t0 + t - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    srv.submit(sids[i], pkgs[i][k], cookie=k)
+                th.join()
+                res = got
+                nxt += L
+            wall = time.perf_counter() - t0
+            launches = lib.vmp_launch_count() - l0
+            clk = clocks.stop()
+            barrier()
+            lat = [r.end_ms - r.submit_ms for r in res]
+            svc = [r.end_ms - r.start_ms for r in res]
+            out[ph] = {"scans": len(res), "wall_s": wall, "scans_per_s": len(res) / wall,
+                       "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                       "service_ms": {"p50": float(np.percentile(svc, 50)), "p99": float(np.percentile(svc, 99))},
+                       "launches": launches, "clocks": clk,
+                       "n_down_mean": float(np.mean([r.result.n_down for r in res]))}
+            if ph == "device":
+                del dev
+    finally:
+        srv.close()
+    return out
+
+
+def run_cpu_served(streams, pkgs, warmup, steps, threads, stream_ids):
+    """The CPU oracle on the served workload: the listed streams' packages,
+    streams in parallel on `threads` host threads (one oracle per stream, as
+    the reference runs one single-threaded node per sensor)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+
+    def one(i):
+        o = oracle.Oracle(streams[i][2], threads=1)
+        for p in pkgs[i][:2 + warmup]:
+            o.process(p)
+        return o
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        ors = list(ex.map(one, stream_ids))
+
+    def timed(j):
+        i = stream_ids[j]
+        for p in pkgs[i][2 + warmup:2 + warmup + steps]:
+            ors[j].process(p)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(timed, range(len(stream_ids))))
+    wall = time.perf_counter() - t0
+    return len(stream_ids) * steps / wall, wall
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -305,10 +487,120 @@ def dist_setup(args):
     return rank, ws, barrier, allmax, dist
 
 
+def roofline_of(prof):
+    """Roofline of the dominant profiled phase with an algorithmic byte count."""
+    dom = max(ALGO_BYTES, key=lambda k: prof[k]["ms"])
+    per_unit, unit_name = ALGO_BYTES[dom]
+    launches = max(1, prof[dom]["launches"])
+    avg_ms = prof[dom]["ms"] / launches
+    bytes_per_launch = per_unit * prof[dom]["items"] / launches
+    peak, peak_src = load_peaks()
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": load_traffic(dom),
+            "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
+            "bytes_per_unit": per_unit, "unit_of_work": unit_name, "peak_source": peak_src}
+
+
+SERVE_NAME = ("64 independent streams, each its own seeded scene and trajectory (even: 20x20x5 m room, "
+              "rosette; odd: 100x100x20 m urban block, 128-beam), rays/scan uniform 2k-200k, 10 Hz, "
+              "HBM admission budget 150 GB")
+
+
+def main_serve(args, rank, ws, barrier, allmax, dist):
+    from voxelmapplus_fastlio2_gb300 import abi
+    from voxelmapplus_fastlio2_gb300 import build as vbuild
+    streams = serve_streams(args, rank)
+    W, K, L = args.warmup, args.steps, args.open_loop_scans
+    if args.workload == "serve" and args.streams != 64:
+        name = SERVE_NAME.replace("64 independent", f"{args.streams} independent")
+    else:
+        name = SERVE_NAME
+    cfg_line = {"workload": name, "streams_per_gpu": args.streams, "rays_per_scan": [s[1] for s in streams],
+                "ieskf_max_iter": {"room": 5, "urban": 4}, "scan_resolution": {"room": 0.2, "urban": 0.1},
+                "voxel_size": 0.5, "map_capacity": {"room": 100000, "urban": 400000},
+                "parallelism": f"stream-sharded x{ws}, {args.streams} streams per GPU"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle
+        oracle.build() if not os.path.exists(oracle.ORACLE_SO) else None
+        vbuild.build_synth()
+        threads = os.cpu_count() or 1
+        pkgs = make_serve_packages(streams, 2 + W + K)
+        v, wall = run_cpu_served(streams, pkgs, W, K, threads, list(range(len(streams))))
+        line = {"metric": METRIC, "value": v, "unit": "scans/s", "impl": "reference", "n_gpus": args.gpus,
+                "steps": K, "warmup": W, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "config": cfg_line,
+                "cpu_baseline": {"value": v, "unit": "scans/s", "cores": threads, "kind": "port",
+                                 "sample": f"{K} mapping scans per stream of all {len(streams)} streams after "
+                                           f"{W} warm-up scans; CPU restatement of the reference, one "
+                                           f"single-threaded oracle per stream, {threads} streams at a time"},
+                "e2e": {"value": v, "unit": "scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    vbuild.build_all()
+    pkgs = make_serve_packages(streams, 2 + W + 2 * K + L)
+    workers = args.workers or min(64, len(streams))
+    served = run_served(args, streams, pkgs, workers, ["device", "host", "open"], barrier)
+    plain_mix = run_served(args, streams, pkgs, 1, ["device"], barrier)
+    # plain one-stream urban block (per-phase profile: the kernel roofline)
+    kind, pts, ucfg, seed, uname = workload(args, rank, "urban")
+    upk = make_packages(kind, pts, seed, 2 + W + args.plain_steps)
+    uargs = argparse.Namespace(**vars(args))
+    uargs.steps = args.plain_steps
+    uval = run_value(uargs, upk, ucfg, 2, barrier)
+    uval_s = sum(uval["step_ms"]) / 1e3
+    dv = served["device"]
+    value = ws * dv["scans"] / allmax(dv["wall_s"])
+    hv = served["host"]
+    h2d = float(np.mean([p.n * C.sizeof(abi.vmp_point) + p.n_imu * C.sizeof(abi.vmp_imu)
+                         for pk in pkgs for p in pk[2 + W + K:2 + W + 2 * K]]))
+    line = {"metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * allmax(dv["wall_s"]) / dv["scans"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": dict(cfg_line, steps_meaning=f"{K} mapping scans per stream, all submitted at once; "
+                                                   "value = scans of all streams / wall time"),
+            "latency_ms": served["open"]["latency_ms"],
+            "e2e": {"value": ws * hv["scans"] / allmax(hv["wall_s"]), "unit": "scans/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(C.sizeof(abi.vmp_result)),
+                    "latency_ms": hv["latency_ms"]},
+            "served": {"streams": args.streams, "workers": workers, "hbm_budget_gb": args.hbm_budget_gb,
+                       "budget_used_gb": served["budget_used_gb"],
+                       "device_resident": dv, "host_buffers": hv,
+                       "open_loop_10hz": served["open"]},
+            "plain_1stream": {
+                "same_mix_scans_per_s": plain_mix["device"]["scans_per_s"],
+                "same_mix_note": "the same streams and packages with one package on the GPU at a time",
+                "urban200k": {"scans_per_s": len(uval["step_ms"]) / uval_s,
+                              "latency_ms": {"p50": float(np.percentile(uval["step_ms"], 50)),
+                                             "p99": float(np.percentile(uval["step_ms"], 99))},
+                              "workload": uname}},
+            "served_over_plain_same_mix": dv["scans_per_s"] / plain_mix["device"]["scans_per_s"],
+            "roofline": dict(roofline_of(uval["prof"]), measured_on="plain one-stream urban block run"),
+            "profile_ms_per_step_urban200k": {k: v["ms"] / args.plain_steps for k, v in uval["prof"].items()},
+            "clocks": dv["clocks"], "gpu_launches": dv["launches"]}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        ids = list(range(min(4, len(streams))))
+        cpk = [pkgs[i][:2 + W + K] if i in ids else [] for i in range(len(streams))]
+        v1, wall = run_cpu_served(streams, cpk, W, K, 1, ids)
+        line["cpu_baseline"] = {"value": v1, "unit": "scans/s", "cores": 1, "kind": "port",
+                                "sample": f"{K} mapping scans of each of streams {ids} (rays/scan "
+                                          f"{[streams[i][1] for i in ids]}) after {W} warm-up scans; CPU "
+                                          "restatement of the reference on 1 thread",
+                                "host_cores": os.cpu_count()}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     from voxelmapplus_fastlio2_gb300 import build as vbuild
     rank, ws, barrier, allmax, dist = dist_setup(args)
+    if args.workload == "serve":
+        return main_serve(args, rank, ws, barrier, allmax, dist)
     kind, pts, cfg, seed, wname = workload(args, rank)
     n_init = 2  # IMU_INIT + MAP_INIT packages
     if args.impl == "reference":
@@ -358,19 +650,8 @@ def main():
                        "d2h_bytes_per_step": int(e2e["d2h"]),
                        "latency_ms": {"p50": 1e3 * float(np.percentile(e2e["walls"], 50)),
                                       "p99": 1e3 * float(np.percentile(e2e["walls"], 99))}}
-    # roofline of the dominant profiled phase with an algorithmic byte count
     prof = val["prof"]
-    dom = max(ALGO_BYTES, key=lambda k: prof[k]["ms"])
-    per_unit, unit_name = ALGO_BYTES[dom]
-    launches = max(1, prof[dom]["launches"])
-    avg_ms = prof[dom]["ms"] / launches
-    bytes_per_launch = per_unit * prof[dom]["items"] / launches
-    peak, peak_src = load_peaks()
-    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
-    line["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": load_traffic(dom),
-                        "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
-                        "bytes_per_unit": per_unit, "unit_of_work": unit_name, "peak_source": peak_src}
+    line["roofline"] = roofline_of(prof)
     line["profile_ms_per_step"] = {k: v["ms"] / args.steps for k, v in prof.items()}
     line["clocks"] = val["clocks"]
     line["gpu_launches"] = val["launches"]

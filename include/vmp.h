@@ -337,6 +337,10 @@ vmp_status vmp_server_open_stream(vmp_server_t sv, const vmp_config* cfg, int* s
 vmp_status vmp_server_close_stream(vmp_server_t sv, int stream_id);
 vmp_status vmp_submit(vmp_server_t sv, int stream_id, const vmp_scan* scan, const vmp_imu* imus, int n_imu,
                       long long cookie);
+/* The same with the package already in device memory (as vmp_process_device);
+ * the buffers must stay valid until the package's result is polled. */
+vmp_status vmp_submit_device(vmp_server_t sv, int stream_id, const vmp_point* d_pts, int n, double t_start,
+                             double t_end, const vmp_imu* d_imus, int n_imu, long long cookie);
 /* Moves up to max finished results to out (completion order), waiting up to
  * timeout_ms for the first one; returns how many, or -1 on a bad argument. */
 int vmp_poll(vmp_server_t sv, vmp_server_result* out, int max, int timeout_ms);

@@ -30,6 +30,7 @@
 // runs instead.  Both paths do the reference's arithmetic in its order.
 #include <cstring>
 #include <mutex>
+#include <vector>
 #include "kernels.cuh"
 
 namespace vmp {
@@ -80,7 +81,8 @@ struct MergeScratch {
     MergeCtl* ctl;
     int pool;
     int rec_pool;
-    int coop_grid;
+    int coop_grid;   // CTAs of one fixed-point launch
+    int coop_slots;  // launches that may be on the device at once (their CTAs all fit co-resident)
 };
 
 __device__ inline void base_state(const DMap& m, uint32_t r, MState& s) {
@@ -540,8 +542,15 @@ cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool) {
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge_fixpoint, kMergeThreads, 0)) != cudaSuccess)
         return e;
-    if (per_sm > 4) per_sm = 4;
-    ms->coop_grid = sms * per_sm;
+    // half the SMs per launch: a few launches (from the streams of a server)
+    // can be resident together, and their grids together never exceed what
+    // the device holds at once
+    const int capacity = sms * per_sm;
+    ms->coop_grid = sms / 2 > 0 ? sms / 2 : 1;
+    if (ms->coop_grid > capacity) ms->coop_grid = capacity;
+    ms->coop_slots = capacity / (ms->coop_grid > 0 ? ms->coop_grid : 1);
+    if (ms->coop_slots < 1) ms->coop_slots = 1;
+    if (ms->coop_slots > 8) ms->coop_slots = 8;
     return cudaSuccess;
 }
 void merge_scratch_free(void* p) {
@@ -571,24 +580,30 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     // converged = 0; wait_error, pad, bar_count = 0 (bar_gen keeps counting)
     if ((e = cudaMemsetAsync(&g.ctl->converged, 0, sizeof(int) * 3 + sizeof(unsigned int), st)) != cudaSuccess) return e;
     if (g.coop_grid > 0) {
-        // One cooperative kernel on the device at a time: two of them, each
-        // holding part of the SMs while waiting for its remaining CTAs, could
-        // wait on each other.  Every launch (from any stream of the process)
-        // waits for the previous one.
+        // At most coop_slots fixed-point launches on the device at once (from
+        // any stream of the process): launch i waits for launch i - slots.
+        // Their CTAs then always fit co-resident, so no launch can wait for
+        // CTAs that the others hold while they wait themselves.
         static std::mutex mu;
-        static cudaEvent_t last_done = nullptr;
+        static std::vector<cudaEvent_t> done;
+        static unsigned long long next = 0;
         std::lock_guard<std::mutex> lk(mu);
-        if (!last_done && cudaEventCreateWithFlags(&last_done, cudaEventDisableTiming) != cudaSuccess) {
-            cudaGetLastError();
-            last_done = nullptr;
+        if (done.empty()) {
+            done.assign(g.coop_slots, nullptr);
+            for (auto& ev : done)
+                if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+                    cudaGetLastError();
+                    ev = nullptr;
+                }
         }
-        if (last_done) cudaStreamWaitEvent(st, last_done, 0);
+        cudaEvent_t slot = done[next++ % done.size()];
+        if (slot) cudaStreamWaitEvent(st, slot, 0);
         void* args[] = {(void*)&m, (void*)&g, (void*)&ms.ev_list, (void*)&ms.ev_rec, (void*)&ms.d_n_ev};
         VMP_NOTE_LAUNCH();
         e = cudaLaunchCooperativeKernel((const void*)k_merge_fixpoint, dim3(g.coop_grid), dim3(kMergeThreads), args, 0,
                                         st);
         if (e != cudaSuccess) cudaGetLastError();  // the replay below produces the result
-        if (last_done) cudaEventRecord(last_done, st);
+        if (slot) cudaEventRecord(slot, st);
     }
     VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev, g.ctl);
     return cudaGetLastError();

@@ -28,6 +28,10 @@ struct Package {
     long long cookie = 0;
     std::vector<vmp_point> pts;
     std::vector<vmp_imu> imus;
+    // vmp_submit_device: the caller's device buffers
+    const vmp_point* d_pts = nullptr;
+    const vmp_imu* d_imus = nullptr;
+    int n = 0, n_imu = 0;
     double t_start = 0.0, t_end = 0.0;
     double submit_ms = 0.0;
 };
@@ -97,8 +101,12 @@ struct vmp_server_s {
             r.stream_id = id;
             r.submit_ms = p.submit_ms;
             r.start_ms = now_ms();
-            vmp_scan scan{p.pts.data(), (int)p.pts.size(), p.t_start, p.t_end};
-            r.status = vmp_process(h, &scan, p.imus.data(), (int)p.imus.size(), &r.result);
+            if (p.d_pts) {
+                r.status = vmp_process_device(h, p.d_pts, p.n, p.t_start, p.t_end, p.d_imus, p.n_imu, &r.result);
+            } else {
+                vmp_scan scan{p.pts.data(), (int)p.pts.size(), p.t_start, p.t_end};
+                r.status = vmp_process(h, &scan, p.imus.data(), (int)p.imus.size(), &r.result);
+            }
             r.end_ms = now_ms();
             lk.lock();
             sl.busy = false;
@@ -213,16 +221,7 @@ vmp_status vmp_server_close_stream(vmp_server_t sv, int id) {
     return VMP_OK;
 }
 
-vmp_status vmp_submit(vmp_server_t sv, int id, const vmp_scan* scan, const vmp_imu* imus, int n_imu,
-                      long long cookie) {
-    if (!sv || !scan || (scan->n > 0 && !scan->points) || n_imu < 0 || (n_imu > 0 && !imus))
-        return VMP_ERR_INVALID_ARG;
-    Package p;
-    p.cookie = cookie;
-    p.pts.assign(scan->points, scan->points + (scan->n > 0 ? scan->n : 0));
-    p.imus.assign(imus, imus + n_imu);
-    p.t_start = scan->t_start;
-    p.t_end = scan->t_end;
+static vmp_status enqueue(vmp_server_t sv, int id, Package&& p) {
     std::lock_guard<std::mutex> lk(sv->mu);
     if (id < 0 || id >= (int)sv->slots.size() || !sv->slots[id].open || sv->slots[id].closing) {
         sv->err = "submit to a stream that is not open";
@@ -238,6 +237,33 @@ vmp_status vmp_submit(vmp_server_t sv, int id, const vmp_scan* scan, const vmp_i
     ++sv->queued;
     sv->cv_work.notify_one();
     return VMP_OK;
+}
+
+vmp_status vmp_submit(vmp_server_t sv, int id, const vmp_scan* scan, const vmp_imu* imus, int n_imu,
+                      long long cookie) {
+    if (!sv || !scan || (scan->n > 0 && !scan->points) || n_imu < 0 || (n_imu > 0 && !imus))
+        return VMP_ERR_INVALID_ARG;
+    Package p;
+    p.cookie = cookie;
+    p.pts.assign(scan->points, scan->points + (scan->n > 0 ? scan->n : 0));
+    p.imus.assign(imus, imus + n_imu);
+    p.t_start = scan->t_start;
+    p.t_end = scan->t_end;
+    return enqueue(sv, id, std::move(p));
+}
+
+vmp_status vmp_submit_device(vmp_server_t sv, int id, const vmp_point* d_pts, int n, double t_start, double t_end,
+                             const vmp_imu* d_imus, int n_imu, long long cookie) {
+    if (!sv || !d_pts || n <= 0 || !d_imus || n_imu <= 0) return VMP_ERR_INVALID_ARG;
+    Package p;
+    p.cookie = cookie;
+    p.d_pts = d_pts;
+    p.d_imus = d_imus;
+    p.n = n;
+    p.n_imu = n_imu;
+    p.t_start = t_start;
+    p.t_end = t_end;
+    return enqueue(sv, id, std::move(p));
 }
 
 int vmp_poll(vmp_server_t sv, vmp_server_result* out, int max, int timeout_ms) {

@@ -49,6 +49,12 @@ class Server:
         scan = pkg.scan()
         self._check(self.lib.vmp_submit(self.h, int(sid), C.byref(scan), pkg.imus, pkg.n_imu, int(cookie)), "submit")
 
+    def submit_device(self, sid, d_pts, n, t_start, t_end, d_imus, n_imu, cookie=0):
+        """A package already in device memory (pointers stay valid until polled)."""
+        self._check(self.lib.vmp_submit_device(self.h, int(sid), C.c_void_p(d_pts), int(n), float(t_start),
+                                               float(t_end), C.c_void_p(d_imus), int(n_imu), int(cookie)),
+                    "submit_device")
+
     def poll(self, max_results=256, timeout_ms=100):
         buf = (abi.vmp_server_result * max_results)()
         n = self.lib.vmp_poll(self.h, buf, max_results, int(timeout_ms))
