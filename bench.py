@@ -40,6 +40,7 @@ import argparse
 import ctypes as C
 import json
 import os
+import resource
 import statistics
 import subprocess
 import sys
@@ -75,7 +76,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room"])
     ap.add_argument("--streams", type=int, default=64, help="served workload: concurrent sensor streams")
-    ap.add_argument("--workers", type=int, default=0, help="served workload: server worker threads (0: streams, <= 64)")
+    ap.add_argument("--workers", type=int, default=0, help="served workload: server worker threads (0: streams, <= 32)")
     ap.add_argument("--open-loop-scans", type=int, default=15, help="served workload: 10 Hz scans per stream")
     ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
     ap.add_argument("--plain-steps", type=int, default=30, help="served workload: steps of the plain urban run")
@@ -387,6 +388,7 @@ def run_served(args, streams, pkgs, workers, phases, barrier):
             clocks.start()
             time.sleep(0.3)
             l0 = lib.vmp_launch_count()
+            ru0 = resource.getrusage(resource.RUSAGE_SELF)
             t0 = time.perf_counter()
             if ph in ("device", "host"):
                 for k in range(K):
@@ -421,6 +423,8 @@ def run_served(args, streams, pkgs, workers, phases, barrier):
                 res = got
                 nxt += L
             wall = time.perf_counter() - t0
+            ru1 = resource.getrusage(resource.RUSAGE_SELF)
+            cpu_s = (ru1.ru_utime - ru0.ru_utime) + (ru1.ru_stime - ru0.ru_stime)
             launches = lib.vmp_launch_count() - l0
             clk = clocks.stop()
             barrier()
@@ -429,7 +433,7 @@ def run_served(args, streams, pkgs, workers, phases, barrier):
             out[ph] = {"scans": len(res), "wall_s": wall, "scans_per_s": len(res) / wall,
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
                        "service_ms": {"p50": float(np.percentile(svc, 50)), "p99": float(np.percentile(svc, 99))},
-                       "launches": launches, "clocks": clk,
+                       "launches": launches, "clocks": clk, "host_cpu_cores_busy": cpu_s / wall,
                        "n_down_mean": float(np.mean([r.result.n_down for r in res]))}
             if ph == "device":
                 del dev
@@ -541,7 +545,7 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
         return
     vbuild.build_all()
     pkgs = make_serve_packages(streams, 2 + W + 2 * K + L)
-    workers = args.workers or min(64, len(streams))
+    workers = args.workers or min(32, len(streams))
     served = run_served(args, streams, pkgs, workers, ["device", "host", "open"], barrier)
     plain_mix = run_served(args, streams, pkgs, 1, ["device"], barrier)
     # plain one-stream urban block (per-phase profile: the kernel roofline)
@@ -598,6 +602,10 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
 def main():
     args = parse()
     from voxelmapplus_fastlio2_gb300 import build as vbuild
+    if args.workload == "serve":
+        # 64 streams need more than the default 8 hardware work queues (set
+        # before the process creates its CUDA context)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     rank, ws, barrier, allmax, dist = dist_setup(args)
     if args.workload == "serve":
         return main_serve(args, rank, ws, barrier, allmax, dist)

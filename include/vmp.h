@@ -89,6 +89,9 @@ typedef struct vmp_config {
     /* device sizing; no reference counterpart */
     int max_scan_points;          /* raw points accepted per scan (default 262144) */
     int max_imu_per_scan;         /* IMU samples accepted per scan (default 1000, at most 1000) */
+    /* reserved[0]: point-slab chunks (0: 2 x records + 1024); reserved[1]:
+     * plane-covariance term buffer (0: 4 x max_scan_points + 65536; terms
+     * that do not fit are formed by the summation itself); the rest 0 */
     int reserved[6];
 } vmp_config;
 

@@ -69,6 +69,32 @@ def test_map_build_update_bit_exact(lio_mod, oracle_lib, merge_mode):
         oracle_lib.orc_destroy(o)
 
 
+@pytest.mark.parametrize("term_cap", [0, 300])
+def test_map_update_term_buffer_overflow(lio_mod, oracle_lib, term_cap):
+    """The plane-covariance terms of a batch go through a term buffer; with a
+    buffer far too small most refits form their terms in the summation kernel
+    instead.  Both ways the map must equal the oracle's bit for bit."""
+    rng = np.random.default_rng(31)
+    cfg = abi.default_config(map_capacity=200000, max_scan_points=60000)
+    cfg.reserved[1] = term_cap
+    g = lio_mod.LIOBuilder(cfg)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        P, Cv = plane_points(rng, n_planes=80, pts_per=(40, 160), iso_frac=0.0)
+        oracle_lib.orc_map_build(o, _dp(P), _dp(Cv), len(P))
+        g.map.build(P, Cv)
+        for step in range(4):
+            P2, C2 = plane_points(rng, n_planes=120, pts_per=(20, 120), iso_frac=0.0)
+            oracle_lib.orc_map_update(o, _dp(P2), _dp(C2), len(P2))
+            g.map.update(P2, C2)
+            vo, no, info, _, _ = export_oracle_map(oracle_lib, o)
+            vg, ng = g.map.export()
+            problems = compare_maps(vo, no, vg, ng, exact=True)
+            assert not problems, f"step {step}: " + "; ".join(problems[:8])
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
 @pytest.mark.parametrize("merge_mode", [0, 1])
 def test_map_merges_bit_exact(lio_mod, oracle_lib, merge_mode):
     """VoxelGrid::merge chains: frozen floor and wall voxels re-observed in

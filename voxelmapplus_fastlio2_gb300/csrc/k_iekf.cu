@@ -490,12 +490,17 @@ void launch_update_begin(DFilter* f, cudaStream_t st) {
 }
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step) {
-    (void)n_max;
+    // about two points per thread for the largest scans, fewer CTAs for small
+    // ones (n_max bounds the downsampled count); the fold and the reduction
+    // order follow the grid, which depends only on n_max
+    int grid = (n_max + 2 * kIekfThreads - 1) / (2 * kIekfThreads);
+    if (grid > s.res_blocks) grid = s.res_blocks;
+    if (grid < 1) grid = 1;
     VMP_NOTE_LAUNCH();
     if (estimate_ext)
-        k_residual<12><<<s.res_blocks, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
+        k_residual<12><<<grid, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
     else
-        k_residual<6><<<s.res_blocks, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
+        k_residual<6><<<grid, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
 }
 void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st) {
     VMP_NOTE_LAUNCH();

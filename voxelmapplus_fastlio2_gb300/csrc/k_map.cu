@@ -382,10 +382,14 @@ struct RefitSnap {
     int npts;        // points the covariance terms run over
     int from_batch;  // build: the batch segment's points, else the slab prefix
     int plane;       // eigen test result
+    int seg;         // segment index
+    int toff;        // first of its npts covariance terms in the term buffer (-1: computed in k_seg_cov)
     double mean[3];
     double ppt[9];
     double ev[3];
     double evecs[9];
+    double M1[9], M2[9];  // RefitConst of a plane refit
+    double den1, den2, inv_n;
 };
 struct CovSeg {
     uint32_t seg;
@@ -438,8 +442,14 @@ struct SegScratch {
     RefitSnap* snaps;     // [max_batch], indexed like the sorted batch
     uint32_t* refit_list; // [max_batch] snapshot indices
     CovSeg* covsegs;      // [max_batch]
+    int* seg_cov;         // [max_batch] covseg index of a segment with snapshots
+    uint32_t* term_snap;  // [term_cap] snapshot of each covariance term (kNoRec: unused slot)
+    double* terms;        // [term_cap][36]
+    int term_cap;
+    int snap_cap;         // snapshots (max_batch + 16)
     int* d_n_refit;
     int* d_n_covseg;
+    int* d_n_terms;
 };
 
 __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_t* __restrict__ seg_start,
@@ -483,6 +493,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
                 sn.n = n;
                 sn.npts = npts;
                 sn.from_batch = from_batch;
+                sn.seg = sidx;
                 const int k = atomicAdd(ss.d_n_refit, 1);
                 ss.refit_list[k] = (uint32_t)(b + nref);
             }
@@ -555,7 +566,12 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             if (lane == 0) k = atomicAdd(ss.d_n_covseg, 1);
             k = __shfl_sync(0xffffffffu, k, 0);
             CovSeg& cs = ss.covsegs[k];
-            if (lane == 0) { cs.seg = (uint32_t)sidx; cs.nref = nref; cs.mstart = mstart; }
+            if (lane == 0) {
+                cs.seg = (uint32_t)sidx;
+                cs.nref = nref;
+                cs.mstart = mstart;
+                ss.seg_cov[sidx] = k;
+            }
             if (lane < kMaxChunks) cs.chunks[lane] = have_saved ? saved[lane] : chunks[lane];
         } else if (flags & F_PLANE) {
             for (int j = mstart + lane; j < e; j += 32) ev_rec[sv[j]] = rec;  // merge() calls
@@ -574,11 +590,14 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
     }
 }
 
-// Eigen decomposition of every refit snapshot (updatePlane, voxel_map.cpp:97-113).
+// Eigen decomposition of every refit snapshot (updatePlane, voxel_map.cpp:97-113);
+// for a plane, the refit's J factors and a run of npts slots in the term
+// buffer (one covariance term per buffered point).
 __global__ void k_refit_eig(DMap m, SegScratch ss) {
     const int nr = *ss.d_n_refit;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nr; t += gridDim.x * blockDim.x) {
-        RefitSnap& sn = ss.snaps[ss.refit_list[t]];
+        const uint32_t si = ss.refit_list[t];
+        RefitSnap& sn = ss.snaps[si];
         const double dn = (double)sn.n;
         double C[9], ev[3], evecs[9];
         for (int k = 0; k < 3; ++k)
@@ -586,17 +605,88 @@ __global__ void k_refit_eig(DMap m, SegScratch ss) {
         eig_sym3(C, ev, evecs);
         for (int k = 0; k < 3; ++k) sn.ev[k] = ev[k];
         for (int k = 0; k < 9; ++k) sn.evecs[k] = evecs[k];
-        sn.plane = ev[0] > m.plane_thresh ? 0 : 1;
+        const int plane = ev[0] > m.plane_thresh ? 0 : 1;
+        sn.plane = plane;
+        sn.toff = -1;
+        if (!plane) continue;
+        RefitConst kc;
+        refit_const(sn.mean, sn.n, ev, evecs, kc);
+        for (int k = 0; k < 9; ++k) { sn.M1[k] = kc.M1[k]; sn.M2[k] = kc.M2[k]; }
+        sn.den1 = kc.den1;
+        sn.den2 = kc.den2;
+        sn.inv_n = kc.inv_n;
+        const int off = atomicAdd(ss.d_n_terms, sn.npts);
+        if (off + sn.npts <= ss.term_cap) {  // else k_seg_cov forms these terms itself
+            sn.toff = off;
+            for (int j = 0; j < sn.npts; ++j) ss.term_snap[off + j] = si;
+        }
+    }
+}
+
+__device__ inline void snap_const(const RefitSnap& sn, RefitConst& k) {
+    for (int q = 0; q < 3; ++q) k.mean[q] = sn.mean[q];
+    for (int q = 0; q < 9; ++q) { k.evecs[q] = sn.evecs[q]; k.M1[q] = sn.M1[q]; k.M2[q] = sn.M2[q]; }
+    k.den1 = sn.den1;
+    k.den2 = sn.den2;
+    k.inv_n = sn.inv_n;
+}
+
+// The point's source: batch segment (build) or slab prefix.
+__device__ inline const double* term_point(const DMap& m, const RefitSnap& sn, int j, const int* chunks,
+                                           const uint32_t* sv, const uint32_t* seg_start, const double* bpts,
+                                           const double* bcov, double* pc) {
+    if (sn.from_batch) {
+        const uint32_t i = sv[seg_start[sn.seg] + j];
+        for (int k = 0; k < 3; ++k) pc[k] = bpts[(size_t)i * 3 + k];
+        for (int k = 0; k < 9; ++k) pc[3 + k] = bcov[(size_t)i * 9 + k];
+        return pc;
+    }
+    return slab_pt(m, chunks, j);
+}
+
+constexpr int kTermThreads = 128;
+
+// Every covariance term of every plane refit, one per thread (the terms of
+// all refits of the batch packed densely over the lanes).
+__global__ void __launch_bounds__(kTermThreads) k_cov_terms(DMap m, const uint32_t* __restrict__ seg_start,
+                                                           const uint32_t* __restrict__ sv,
+                                                           const double* __restrict__ bpts,
+                                                           const double* __restrict__ bcov, SegScratch ss) {
+    __shared__ double stage[kTermThreads * 36];
+    int nt = *ss.d_n_terms;
+    if (nt > ss.term_cap) nt = ss.term_cap;
+    for (int t0 = blockIdx.x * kTermThreads; t0 < nt; t0 += gridDim.x * kTermThreads) {
+        const int t = t0 + threadIdx.x;
+        // a slot belongs to a refit only if that refit's whole run fitted;
+        // the others keep the fill value of this batch (kNoRec)
+        const uint32_t si = t < nt ? ss.term_snap[t] : kNoRec;
+        if (si < (uint32_t)ss.snap_cap) {
+            const RefitSnap& sn = ss.snaps[si];
+            const int j = t - sn.toff;
+            if (sn.toff >= 0 && j >= 0 && j < sn.npts) {
+                RefitConst kc;
+                snap_const(sn, kc);
+                double pc[12];
+                const int* chunks = ss.covsegs[ss.seg_cov[sn.seg]].chunks;
+                const double* src = term_point(m, sn, j, chunks, sv, seg_start, bpts, bcov, pc);
+                plane_cov_term(src, src + 3, kc, stage + threadIdx.x * 36);
+            }
+        }
+        __syncthreads();
+        const int cnt = min(kTermThreads, nt - t0);
+        for (int q = threadIdx.x; q < cnt * 36; q += kTermThreads) ss.terms[(size_t)t0 * 36 + q] = stage[q];
+        __syncthreads();
     }
 }
 
 struct CovShared {
     double stage[kSegThreads / 32][32][36];
-    double cov[kSegThreads / 32][36];
     int chunks[kSegThreads / 32][kMaxChunks];
 };
 
-// Plane covariance accumulation, normal and centre, merge calls.
+// Per voxel with refits: the plane covariance sums in point order (terms from
+// the term buffer, or formed here when they did not fit), normal and centre
+// of the last plane refit, merge calls.
 __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t* __restrict__ seg_start,
                                                          const uint32_t* __restrict__ seg_end,
                                                          const uint32_t* __restrict__ seg_rec,
@@ -609,7 +699,6 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int nc = *ss.d_n_covseg;
-    double* cov = sh.cov[wib];
     int* chunks = sh.chunks[wib];
     double (*stage)[36] = sh.stage[wib];
     for (int li = gw; li < nc; li += nw) {
@@ -623,7 +712,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
         uint32_t flags = H.flags;
         double norm[3] = {H.norm[0], H.norm[1], H.norm[2]};
         double center[3] = {Cc.center[0], Cc.center[1], Cc.center[2]};
-        for (int k = lane; k < 36; k += 32) cov[k] = Cc.cov[k];
+        // lane q accumulates entry q, lanes 0-3 also entry 32 + q
+        double c0 = Cc.cov[lane], c1 = lane < 4 ? Cc.cov[32 + lane] : 0.0;
         if (lane < kMaxChunks) chunks[lane] = cs.chunks[lane];
         __syncwarp();
         for (int r = 0; r < nref; ++r) {
@@ -633,41 +723,36 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
                 continue;
             }
             flags |= F_PLANE;
-            const int n = sn.n, npts = sn.npts;
-            const bool from_batch = sn.from_batch != 0;
-            double mn[3], ev[3], evecs[9];
-            for (int k = 0; k < 3; ++k) { mn[k] = sn.mean[k]; ev[k] = sn.ev[k]; }
-            for (int k = 0; k < 9; ++k) evecs[k] = sn.evecs[k];
-            RefitConst kc;
-            refit_const(mn, n, ev, evecs, kc);
-            for (int base = 0; base < npts; base += 32) {
-                const int j = base + lane;
-                if (j < npts) {
-                    const double* src;
-                    double pc[12];
-                    if (from_batch) {
-                        const uint32_t i = sv[b + j];
-                        for (int k = 0; k < 3; ++k) pc[k] = bpts[(size_t)i * 3 + k];
-                        for (int k = 0; k < 9; ++k) pc[3 + k] = bcov[(size_t)i * 9 + k];
-                        src = pc;
-                    } else {
-                        src = slab_pt(m, chunks, j);
+            const int npts = sn.npts;
+            if (sn.toff >= 0) {
+                const double* tp = ss.terms + (size_t)sn.toff * 36;
+                for (int j = 0; j < npts; ++j) {
+                    c0 = c0 + tp[j * 36 + lane];
+                    if (lane < 4) c1 = c1 + tp[j * 36 + 32 + lane];
+                }
+            } else {
+                RefitConst kc;
+                snap_const(sn, kc);
+                for (int base = 0; base < npts; base += 32) {
+                    const int j = base + lane;
+                    if (j < npts) {
+                        double pc[12];
+                        const double* src = term_point(m, sn, j, chunks, sv, seg_start, bpts, bcov, pc);
+                        plane_cov_term(src, src + 3, kc, stage[lane]);
                     }
-                    plane_cov_term(src, src + 3, kc, stage[lane]);
+                    __syncwarp();
+                    const int cnt = min(32, npts - base);
+                    for (int u = 0; u < cnt; ++u) {
+                        c0 = c0 + stage[u][lane];
+                        if (lane < 4) c1 = c1 + stage[u][32 + lane];
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
-                const int cnt = min(32, npts - base);
-                for (int q = lane; q < 36; q += 32) {
-                    double acc = cov[q];
-                    for (int u = 0; u < cnt; ++u) acc = acc + stage[u][q];
-                    cov[q] = acc;
-                }
-                __syncwarp();
             }
-            double pn[3] = {evecs[0], evecs[3], evecs[6]};
-            const double axis_distance = -dot3(mn, pn);
+            double pn[3] = {sn.evecs[0], sn.evecs[3], sn.evecs[6]};
+            const double axis_distance = -dot3(sn.mean, pn);
             if (axis_distance < 0.0) { pn[0] = -pn[0]; pn[1] = -pn[1]; pn[2] = -pn[2]; }
-            for (int k = 0; k < 3; ++k) { norm[k] = pn[k]; center[k] = mn[k]; }
+            for (int k = 0; k < 3; ++k) { norm[k] = pn[k]; center[k] = sn.mean[k]; }
         }
         if (flags & F_PLANE)
             for (int j = mstart + lane; j < e; j += 32) ev_rec[sv[j]] = rec;  // merge() calls
@@ -675,7 +760,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
             H.flags = flags;
             for (int k = 0; k < 3; ++k) { H.norm[k] = norm[k]; Cc.center[k] = center[k]; }
         }
-        for (int k = lane; k < 36; k += 32) Cc.cov[k] = cov[k];
+        Cc.cov[lane] = c0;
+        if (lane < 4) Cc.cov[32 + lane] = c1;
         __syncwarp();
     }
 }
@@ -795,14 +881,21 @@ void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double*
     if (sg > 152 * 16) sg = 152 * 16;
     if (sg < 1) sg = 1;
     SegScratch ss{static_cast<RefitSnap*>(ms.seg_snaps), ms.refit_list, static_cast<CovSeg*>(ms.covsegs),
-                  ms.d_scratch_int + 5, ms.d_scratch_int + 6};
-    cudaMemsetAsync(ms.d_scratch_int + 5, 0, 2 * sizeof(int), st);
+                  ms.seg_cov, ms.term_snap, ms.terms, ms.term_cap, ms.max_batch + 16, ms.d_scratch_int + 5,
+                  ms.d_scratch_int + 6, ms.d_scratch_int + 7};
+    cudaMemsetAsync(ms.d_scratch_int + 5, 0, 3 * sizeof(int), st);
+    cudaMemsetAsync(ms.term_snap, 0xFF, sizeof(uint32_t) * (size_t)ms.term_cap, st);
     VMP_NOTE_LAUNCH();
     k_seg_chain<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg, ms.sv, bpts, bcov,
                                             ms.ev_rec, ss, build ? 1 : 0);
     // one warp per block so that the refits spread over all SMs
     VMP_NOTE_LAUNCH();
     k_refit_eig<<<152 * 8, 32, 0, st>>>(m, ss);
+    int tg = (2 * n_max + kTermThreads - 1) / kTermThreads;
+    if (tg > 152 * 8) tg = 152 * 8;
+    if (tg < 1) tg = 1;
+    VMP_NOTE_LAUNCH();
+    k_cov_terms<<<tg, kTermThreads, 0, st>>>(m, ms.seg_start, ms.sv, bpts, bcov, ss);
     VMP_NOTE_LAUNCH();
     k_seg_cov<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.sv, bpts, bcov, ms.ev_rec, ss);
 }
@@ -938,7 +1031,7 @@ __global__ void k_map_reset(DMap m) {
 }
 void launch_map_reset(DMap& m, cudaStream_t st) { VMP_NOTE_LAUNCH(); k_map_reset<<<1216, 256, 0, st>>>(m); }
 
-cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
+cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool, int term_cap) {
     ms.max_batch = max_batch;
     size_t nb = (size_t)max_batch + 16;
     cudaError_t e;
@@ -950,6 +1043,12 @@ cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool) {
     if ((e = dev_malloc(&ms.seg_snaps, sizeof(RefitSnap) * nb)) != cudaSuccess) return e;
     if ((e = dev_malloc(&ms.covsegs, sizeof(CovSeg) * nb)) != cudaSuccess) return e;
     if ((e = dev_malloc(&ms.refit_list, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.seg_cov, sizeof(int) * nb)) != cudaSuccess) return e;
+    // refits re-read the slab, so a batch has more terms than points; terms
+    // that do not fit are formed by k_seg_cov itself
+    ms.term_cap = term_cap > 0 ? term_cap : 4 * max_batch + 65536;
+    if ((e = dev_malloc(&ms.term_snap, sizeof(uint32_t) * (size_t)ms.term_cap)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.terms, sizeof(double) * 36 * (size_t)ms.term_cap)) != cudaSuccess) return e;
     ms.merge_mode = 0;
     ms.merge_rounds = 0;
     ms.merge_d2h = 0;
@@ -971,6 +1070,9 @@ void map_scratch_free(MapScratch& ms) {
     cudaFree(ms.seg_snaps);
     cudaFree(ms.covsegs);
     cudaFree(ms.refit_list);
+    cudaFree(ms.seg_cov);
+    cudaFree(ms.term_snap);
+    cudaFree(ms.terms);
     cudaFree(ms.d_scratch_int);
     sort_scratch_free(ms.sort);
     scan_scratch_free(ms.scan);

@@ -90,6 +90,10 @@ struct MapScratch {
     void* seg_snaps;      // [max_batch] refit snapshots (k_map.cu)
     void* covsegs;        // [max_batch] voxels with refits (k_map.cu)
     uint32_t* refit_list; // [max_batch]
+    int* seg_cov;         // [max_batch] voxel-with-refits index of a segment
+    uint32_t* term_snap;  // [term_cap] refit of each plane covariance term
+    double* terms;        // [term_cap][36] plane covariance terms
+    int term_cap;
     int merge_mode;
     int merge_rounds;
     long long merge_d2h;  // bytes read back by the merge rounds (cumulative)
@@ -98,12 +102,12 @@ struct MapScratch {
     int* d_n_seg;
     int* d_n_ev;
     int* d_n_touch;
-    int* d_scratch_int;   // [32]: batch counters; [5], [6] refit / voxel list lengths
+    int* d_scratch_int;   // [32]: batch counters; [5], [6], [7] refit / voxel / term list lengths
     int max_batch;
     SortScratch sort;
     ScanScratch scan;
 };
-cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool);
+cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool, int term_cap);
 void map_scratch_free(MapScratch& ms);
 
 // Applies VoxelMap::update (build = false) or VoxelMap::build (build = true)

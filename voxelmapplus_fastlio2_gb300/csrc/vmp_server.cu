@@ -13,6 +13,7 @@
 // HBM budget and a slot is free.
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -137,6 +138,11 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
     if (cfg.max_streams <= 0 || cfg.max_streams > 4096 || cfg.workers <= 0 || cfg.workers > 1024 ||
         cfg.queue_depth <= 0 || cfg.hbm_budget_bytes <= 0)
         return VMP_ERR_INVALID_ARG;
+    // Many streams need more hardware work queues than the default 8, or
+    // kernels of unrelated streams queue behind each other.  Effective only
+    // if the process has not created its CUDA context yet; a caller's own
+    // setting wins.
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     vmp_server_t sv = new (std::nothrow) vmp_server_s();
     if (!sv) return VMP_ERR_OUT_OF_MEMORY;
     sv->cfg = cfg;
