@@ -285,6 +285,9 @@ int vmp_last_merge_rounds(vmp_stream_t s);
  * the last scan (kind 0 undistorted time-sorted cloud, 1 downsampled). */
 vmp_status vmp_residual_valid(vmp_stream_t s, unsigned char* valid, int n);
 vmp_status vmp_last_cloud(vmp_stream_t s, int kind, vmp_point* out, int max, int* n_out);
+/* Test hook: batches that the LRU eviction had to split (an evicted voxel
+ * touched again later in the same batch). */
+long long vmp_eviction_splits(vmp_stream_t s);
 /* Device memory a stream holds (all of it is allocated by vmp_create). */
 long long vmp_device_bytes(vmp_stream_t s);
 /* How vmp_process waits for its result: 0 (default) polls, lowest latency;

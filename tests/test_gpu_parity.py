@@ -126,6 +126,77 @@ def test_map_merges_bit_exact(lio_mod, oracle_lib, merge_mode):
         oracle_lib.orc_destroy(o)
 
 
+def test_map_eviction_bit_exact(lio_mod, oracle_lib):
+    """LRU eviction (VoxelMap::update's cache splice / pop_back,
+    voxel_map.cpp:232-256) with a map capacity far below the voxels the
+    batches create: evictions in most batches, batches whose evicted voxels
+    are touched again later in the same batch (the reference re-creates them;
+    the batch is split), LRU-queue compaction and hash rehash.  The whole map,
+    LRU order included, must equal the oracle's after every batch."""
+    rng = np.random.default_rng(41)
+    cap = 1500
+    cfg = abi.default_config(map_capacity=cap, max_scan_points=12000)
+    g = lio_mod.LIOBuilder(cfg)
+    o = oracle_lib.orc_create(C.byref(cfg))
+    try:
+        P0, C0 = plane_points(rng, n_planes=60, extent=30.0)
+        oracle_lib.orc_map_build(o, _dp(P0), _dp(C0), len(P0))
+        g.map.build(P0, C0)
+        seen = set(map(tuple, np.floor(P0 / cfg.voxel_size).astype(np.int64)))
+        Pp, Cp = P0, C0
+        for step in range(12):
+            P2, C2 = plane_points(rng, n_planes=70, pts_per=(5, 120), extent=30.0 + 4.0 * step)
+            Pn, Cn = P2, C2
+            if step % 3 == 2:
+                # at the end of the batch: voxels of the previous batch (still
+                # in the map when the batch starts, evicted by its creations,
+                # then touched again) and long-evicted ones
+                P2 = np.vstack([P2, Pp[:300], P0[:150]])
+                C2 = np.vstack([C2, Cp[:300], C0[:150]])
+            Pp, Cp = Pn, Cn
+            seen |= set(map(tuple, np.floor(P2 / cfg.voxel_size).astype(np.int64)))
+            oracle_lib.orc_map_update(o, _dp(P2), _dp(C2), len(P2))
+            g.map.update(P2, C2)
+            vo, no, info, _, _ = export_oracle_map(oracle_lib, o)
+            vg, ng = g.map.export()
+            assert no <= cap
+            problems = compare_maps(vo, no, vg, ng, exact=True)
+            assert not problems, f"step {step}: " + "; ".join(problems[:8])
+            order_o = [tuple(vo[i].key) for i in range(no)]
+            order_g = [tuple(vg[i].key) for i in range(ng)]
+            assert order_o == order_g, f"step {step}: LRU order differs"
+        assert len(seen) > 5 * cap  # most voxels were evicted along the way
+        assert g.lib.vmp_eviction_splits(g.h) > 0  # the split path ran
+    finally:
+        oracle_lib.orc_destroy(o)
+
+
+def test_process_sequence_with_eviction(lio_mod, oracle_lib):
+    """LIOBuilder::process on a corridor walk with a small map capacity: the
+    map stays at capacity while evicting; per-scan pose, counts and map size
+    as the oracle's."""
+    import oracle as orc
+    seq_g = synth.Sequence(synth.KIND_CORRIDOR, points_per_scan=8000)
+    seq_o = synth.Sequence(synth.KIND_CORRIDOR, points_per_scan=8000)
+    cfg = abi.default_config(scan_resolution=0.2, max_scan_points=16384, map_capacity=2500)
+    g = lio_mod.LIOBuilder(cfg)
+    o = orc.Oracle(cfg)
+    full = 0
+    for k in range(40):
+        rg = g.process(seq_g.next())
+        ro = o.process(seq_o.next())
+        assert rg.lio_status == ro.lio_status
+        if ro.lio_status != abi.LIO_MAPPING or k < 2:
+            continue
+        assert (rg.n_down, rg.effect_num, rg.iters, rg.map_size) == (ro.n_down, ro.effect_num, ro.iters, ro.map_size), k
+        assert rg.map_size <= 2500
+        full += rg.map_size == 2500
+        dp = np.max(np.abs(np.array(rg.x.pos[:]) - np.array(ro.x.pos[:])))
+        da = rot_angle(rg.x.rot[:], ro.x.rot[:])
+        assert dp < 1e-9 and da < 1e-9, (k, dp, da)
+    assert full > 10
+
+
 def test_map_index_matches_oracle(lio_mod, oracle_lib):
     rng = np.random.default_rng(3)
     cfg = abi.default_config()

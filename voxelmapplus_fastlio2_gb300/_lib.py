@@ -57,6 +57,7 @@ def _declare(lib):
         "vmp_io_bytes": ([vp, P(C.c_longlong), P(C.c_longlong)], st),
         "vmp_last_merge_rounds": ([vp], C.c_int),
         "vmp_device_bytes": ([vp], C.c_longlong),
+        "vmp_eviction_splits": ([vp], C.c_longlong),
         "vmp_set_wait_mode": ([vp, C.c_int], st),
         "vmp_server_config_default": ([P(abi.vmp_server_config)], None),
         "vmp_server_create": ([P(abi.vmp_server_config), P(vp)], st),

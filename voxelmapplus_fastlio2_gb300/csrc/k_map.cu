@@ -188,9 +188,10 @@ __global__ void k_fill_u32(uint32_t* p, const int* d_n, uint32_t v) {
 // A victim that a later point of the batch touches would be re-created by the
 // reference; the walk then reports the first such point (split_at) and the
 // host applies the batch in two parts.
-__global__ void k_evict_walk(DMap m, const uint32_t* __restrict__ new_pos, uint32_t* victims) {
+__global__ void k_evict_walk(DMap m, const uint32_t* __restrict__ new_pos, uint32_t* victims, const int* d_n) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Counters* c = m.cnt;
+    const unsigned long long batch_end = c->batch_base + (unsigned long long)*d_n;
     const int n_new = c->n_new;
     const long long size_before = c->size - n_new;
     const unsigned long long base = c->batch_base;
@@ -211,7 +212,9 @@ __global__ void k_evict_walk(DMap m, const uint32_t* __restrict__ new_pos, uint3
             ++q;
             if (!(m.hot[r].flags & F_ALIVE) || m.cold[r].stamp != st) continue;
             uint64_t tf = m.cold[r].touch_first_g;
-            bool touched_here = (tf != kNever) && tf >= base;
+            // a stamp past this batch's points is left by the rolled-back
+            // first pass of a batch that was split: not a touch of this batch
+            bool touched_here = (tf != kNever) && tf >= base && tf < batch_end;
             if (touched_here && tf < cg) continue;  // moved to the front before this creation
             victim = r;
             if (touched_here) split = (long long)(tf - base);  // re-created later by the reference
@@ -853,7 +856,7 @@ void launch_map_phase_a(DMap& m, MapScratch& ms, const double* bpts, int n_max, 
 }
 // Eviction walk (only when the batch can overflow the capacity).
 void launch_map_walk(DMap& m, MapScratch& ms, cudaStream_t st) {
-    VMP_NOTE_LAUNCH(); k_evict_walk<<<1, 32, 0, st>>>(m, ms.new_pos, ms.victims);
+    VMP_NOTE_LAUNCH(); k_evict_walk<<<1, 32, 0, st>>>(m, ms.new_pos, ms.victims, ms.d_n);
 }
 void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
     VMP_NOTE_LAUNCH(); k_rollback<<<grid_for_map(n_max), kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.d_n);

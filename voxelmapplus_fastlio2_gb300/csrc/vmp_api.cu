@@ -252,6 +252,7 @@ struct vmp_stream_s {
     bool broken = false;
     long long last_evicted_total = 0;
     long long dev_bytes = 0;  // device memory allocated by vmp_create
+    long long eviction_splits = 0;  // batches split by the eviction walk
     bool blocking_wait = false;  // vmp_set_wait_mode
     cudaEvent_t done_ev = nullptr;
     // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
@@ -651,6 +652,7 @@ static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bc
         VMP_TRY(cudaGetLastError(), "map update launch");
         return read_counters(s);
     }
+    ++s->eviction_splits;
     launch_map_rollback(m, ms, n, s->st);
     st = read_counters(s);
     if (st != VMP_OK) return st;
@@ -1192,6 +1194,7 @@ vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode) {
     return VMP_OK;
 }
 long long vmp_device_bytes(vmp_stream_t s) { return s ? s->dev_bytes : -1; }
+long long vmp_eviction_splits(vmp_stream_t s) { return s ? s->eviction_splits : -1; }
 vmp_status vmp_set_wait_mode(vmp_stream_t s, int blocking) {
     if (!s) return VMP_ERR_INVALID_ARG;
     s->blocking_wait = blocking != 0;
