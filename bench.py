@@ -178,12 +178,14 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic(phase):
-    """DRAM bytes per launch of the phase's main kernel from a committed ncu summary."""
+def load_traffic(phase, units_per_launch):
+    """DRAM bytes per launch of the phase from the committed ncu summary
+    (profiles/traffic.json holds bytes per unit of work)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(phase)
+            t = json.load(f).get(phase)
+        return None if t is None else float(t["bytes_per_unit"]) * units_per_launch
     except Exception:
         return None
 
@@ -501,7 +503,7 @@ def roofline_of(prof):
     peak, peak_src = load_peaks()
     achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": load_traffic(dom),
+            "frac": achieved / peak, "traffic": load_traffic(dom, prof[dom]["items"] / launches),
             "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
             "bytes_per_unit": per_unit, "unit_of_work": unit_name, "peak_source": peak_src}
 
