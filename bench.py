@@ -196,8 +196,14 @@ def pkg_arrays(p):
     return pts, imu
 
 
+PROFILE_STEPS = 10
+
+
 def run_value(args, pkgs, cfg, n_init, barrier):
-    """Inputs resident in HBM; per-step CUDA events on the library's stream."""
+    """Inputs resident in HBM; per-step CUDA events on the library's stream.
+    The timed steps run as in production (captured scan graphs); the
+    per-phase profile comes from PROFILE_STEPS further scans with the
+    library's CUDA-event profiler on (direct launches, same kernels)."""
     import torch
     from voxelmapplus_fastlio2_gb300 import lio
     g = lio.LIOBuilder(cfg)
@@ -210,12 +216,12 @@ def run_value(args, pkgs, cfg, n_init, barrier):
     stream = torch.cuda.ExternalStream(g.lib.vmp_cuda_stream(g.h))
     flush = torch.empty(args.flush_mb << 20, dtype=torch.uint8, device="cuda")
     W, K = args.warmup, args.steps
+    P = min(PROFILE_STEPS, len(dev) - W - K)
     for i in range(W):
         d_pts, d_imu, p = dev[i]
         g.process_device(d_pts.data_ptr(), p.n, p.t_start, p.t_end, d_imu.data_ptr(), p.n_imu)
     torch.cuda.synchronize()
     barrier()
-    g.lib.vmp_profile_enable(g.h, 1)
     launches0 = g.lib.vmp_launch_count()
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
@@ -242,6 +248,13 @@ def run_value(args, pkgs, cfg, n_init, barrier):
     clk = clocks.stop()
     launches = g.lib.vmp_launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
+    g.lib.vmp_profile_enable(g.h, 1)
+    for i in range(W + K, W + K + P):
+        d_pts, d_imu, p = dev[i]
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 255)
+        g.process_device(d_pts.data_ptr(), p.n, p.t_start, p.t_end, d_imu.data_ptr(), p.n_imu)
+    torch.cuda.synchronize()
     ms = (C.c_double * 16)()
     nl = (C.c_longlong * 16)()
     it = (C.c_longlong * 16)()
@@ -249,8 +262,8 @@ def run_value(args, pkgs, cfg, n_init, barrier):
     prof = {PROF_NAMES[k]: {"ms": ms[k], "launches": nl[k], "items": it[k]} for k in range(len(PROF_NAMES))}
     g.lib.vmp_profile_enable(g.h, 0)
     out = {"step_ms": step_ms, "wall_s": t_wall, "launches": launches, "clocks": clk, "prof": prof,
-           "n_raw": float(np.mean(n_raw)), "n_down": float(np.mean(n_down)), "map_size": int(res.map_size),
-           "iters_last": int(res.iters)}
+           "prof_steps": max(P, 1), "n_raw": float(np.mean(n_raw)), "n_down": float(np.mean(n_down)),
+           "map_size": int(res.map_size), "iters_last": int(res.iters)}
     g.close()
     return out
 
@@ -552,7 +565,7 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
     plain_mix = run_served(args, streams, pkgs, 1, ["device"], barrier)
     # plain one-stream urban block (per-phase profile: the kernel roofline)
     kind, pts, ucfg, seed, uname = workload(args, rank, "urban")
-    upk = make_packages(kind, pts, seed, 2 + W + args.plain_steps)
+    upk = make_packages(kind, pts, seed, 2 + W + args.plain_steps + PROFILE_STEPS)
     uargs = argparse.Namespace(**vars(args))
     uargs.steps = args.plain_steps
     uval = run_value(uargs, upk, ucfg, 2, barrier)
@@ -584,7 +597,7 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
                               "workload": uname}},
             "served_over_plain_same_mix": dv["scans_per_s"] / plain_mix["device"]["scans_per_s"],
             "roofline": dict(roofline_of(uval["prof"]), measured_on="plain one-stream urban block run"),
-            "profile_ms_per_step_urban200k": {k: v["ms"] / args.plain_steps for k, v in uval["prof"].items()},
+            "profile_ms_per_step_urban200k": {k: v["ms"] / uval["prof_steps"] for k, v in uval["prof"].items()},
             "clocks": dv["clocks"], "gpu_launches": dv["launches"]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         ids = list(range(min(4, len(streams))))
@@ -637,7 +650,7 @@ def main():
         return
     vbuild.build_all()
     import torch
-    pkgs = make_packages(kind, pts, seed, n_init + args.warmup + args.steps)
+    pkgs = make_packages(kind, pts, seed, n_init + args.warmup + args.steps + PROFILE_STEPS)
     val = run_value(args, pkgs, cfg, n_init, barrier)
     e2e = None if args.no_e2e else run_e2e(args, pkgs, cfg, n_init, barrier)
     step_s = sum(val["step_ms"]) / 1e3
@@ -662,7 +675,7 @@ def main():
                                       "p99": 1e3 * float(np.percentile(e2e["walls"], 99))}}
     prof = val["prof"]
     line["roofline"] = roofline_of(prof)
-    line["profile_ms_per_step"] = {k: v["ms"] / args.steps for k, v in prof.items()}
+    line["profile_ms_per_step"] = {k: v["ms"] / val["prof_steps"] for k, v in prof.items()}
     line["clocks"] = val["clocks"]
     line["gpu_launches"] = val["launches"]
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -285,6 +285,11 @@ int vmp_last_merge_rounds(vmp_stream_t s);
  * the last scan (kind 0 undistorted time-sorted cloud, 1 downsampled). */
 vmp_status vmp_residual_valid(vmp_stream_t s, unsigned char* valid, int n);
 vmp_status vmp_last_cloud(vmp_stream_t s, int kind, vmp_point* out, int max, int* n_out);
+/* Steady-state scans run as captured CUDA graphs (default 1): two graph
+ * launches around the merge resolution instead of ~90 kernel launches.  The
+ * direct launches (0; also used while profiling or when the batch may evict)
+ * launch the same kernels with the same grids and give the same results. */
+vmp_status vmp_set_graphs(vmp_stream_t s, int on);
 /* Test hook: batches that the LRU eviction had to split (an evicted voxel
  * touched again later in the same batch). */
 long long vmp_eviction_splits(vmp_stream_t s);

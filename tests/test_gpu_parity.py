@@ -335,6 +335,29 @@ def test_process_sequence_room(lio_mod, oracle_lib):
         assert np.max(np.abs(Pg - Po)) <= 1e-8 * np.max(np.abs(Po)), k
 
 
+def test_graph_and_direct_launches_agree(lio_mod):
+    """The steady-state scan as captured graphs and as direct launches: the
+    same kernels with the same grids, so the same bits -- every result, and
+    the map at the end (two urban streams of different scan sizes, so that
+    several size classes are captured)."""
+    from voxelmapplus_fastlio2_gb300 import abi as A
+    out = []
+    for graphs in (1, 0):
+        seq = synth.Sequence(synth.KIND_URBAN, points_per_scan=30000)
+        cfg = A.default_config(scan_resolution=0.1, map_capacity=300000, max_scan_points=40000, ieskf_max_iter=4)
+        g = lio_mod.LIOBuilder(cfg)
+        g.lib.vmp_set_graphs(g.h, graphs)
+        res = []
+        for k in range(12):
+            r = g.process(seq.next())
+            res.append((r.lio_status, r.iters, r.effect_num, r.n_down, r.map_size, bytes(r.x), bytes(r.P)))
+        v, n = g.map.export()
+        out.append((res, C.string_at(v, n * C.sizeof(A.vmp_voxel))))
+        g.close()
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
+
+
 def test_undistort_and_predict_chain_match_oracle(lio_mod, oracle_lib):
     """undistortCloud after IMU init + map init: the time-sorted compensated
     cloud and the filter state / covariance at the scan end."""

@@ -59,6 +59,7 @@ def _declare(lib):
         "vmp_device_bytes": ([vp], C.c_longlong),
         "vmp_eviction_splits": ([vp], C.c_longlong),
         "vmp_set_wait_mode": ([vp, C.c_int], st),
+        "vmp_set_graphs": ([vp, C.c_int], st),
         "vmp_server_config_default": ([P(abi.vmp_server_config)], None),
         "vmp_server_create": ([P(abi.vmp_server_config), P(vp)], st),
         "vmp_server_destroy": ([vp], st),

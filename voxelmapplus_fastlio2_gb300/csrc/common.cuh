@@ -17,7 +17,15 @@ namespace vmp {
 
 // Host-side count of kernel launches issued by the library (all streams).
 extern std::atomic<long long> g_launch_count;
-#define VMP_NOTE_LAUNCH() ::vmp::g_launch_count.fetch_add(1, std::memory_order_relaxed)
+// While this thread captures a CUDA graph its launches only record into the
+// graph: they are counted here and added to g_launch_count at every replay.
+long long* capture_launch_counter();
+inline void note_launch() {
+    long long* c = capture_launch_counter();
+    if (c) ++*c;
+    else g_launch_count.fetch_add(1, std::memory_order_relaxed);
+}
+#define VMP_NOTE_LAUNCH() ::vmp::note_launch()
 
 constexpr double kGravity = 9.81;          // kf::GRAVITY (ieskf.h:6)
 constexpr double kSophusEps = 1e-10;       // Sophus::Constants<double>::epsilon()

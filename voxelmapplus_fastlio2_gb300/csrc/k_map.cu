@@ -402,33 +402,6 @@ struct CovSeg {
     int32_t chunks[kMaxChunks];  // the slab before a freeze released it
 };
 
-__device__ inline bool warp_slab_append(const DMap& m, int* chunks, int& nslab, const double* p, const double* c,
-                                        int lane) {
-    const int ci = nslab / kChunkPts;
-    if (ci >= kMaxChunks) return false;
-    if (nslab % kChunkPts == 0) {
-        int id = -1;
-        if (lane == 0) {
-            const int top = atomicSub(&m.cnt->chunk_free_top, 1);
-            if (top <= 0) {
-                atomicAdd(&m.cnt->chunk_free_top, 1);
-                set_error(m.cnt, E_CHUNKS);
-            } else {
-                id = m.chunk_free[top - 1];
-                chunks[ci] = id;
-            }
-        }
-        id = __shfl_sync(0xffffffffu, id, 0);
-        if (id < 0) return false;
-    }
-    __syncwarp();
-    double* d = slab_pt(m, chunks, nslab);
-    if (lane < 3) d[lane] = p[lane];
-    else if (lane < 12) d[lane] = c[lane - 3];
-    nslab++;
-    return true;
-}
-
 __device__ inline void slab_release(const DMap& m, int* chunks, int& nslab) {
     int used = (nslab + kChunkPts - 1) / kChunkPts;
     for (int k = 0; k < used && k < kMaxChunks; ++k) {
@@ -453,7 +426,46 @@ struct SegScratch {
     int* d_n_refit;
     int* d_n_covseg;
     int* d_n_terms;
+    int* d_work_chain;  // next segment group for k_seg_chain
+    int* d_work_cov;    // next voxel-with-refits for k_seg_cov
 };
+
+// Three voxel chains per warp, ten lanes each: the nine ppt components on
+// lanes 0-8 of a group (the three mean components on lanes 0-2), the integer
+// state on every lane of the group.  A chain's steps stay lane-parallel (its
+// latency as with a whole warp), and every FP64 instruction serves three
+// voxels.  Collective steps (chunk allocation, the loop test) run on the
+// whole warp with per-group predicates.
+constexpr int kGroupLanes = 10;
+constexpr int kGroups = 3;
+
+// Slab append for the groups with `app` (all lanes call it).
+__device__ inline void group_slab_append(const DMap& m, bool app, int* chunks, int& nslab, const double* p,
+                                         const double* c, int q, int gbase) {
+    const int ci = nslab / kChunkPts;
+    const bool fits = app && ci < kMaxChunks;
+    const bool need = fits && (nslab % kChunkPts == 0);
+    int got = 1;
+    if (need && q == 0) {
+        const int top = atomicSub(&m.cnt->chunk_free_top, 1);
+        if (top <= 0) {
+            atomicAdd(&m.cnt->chunk_free_top, 1);
+            set_error(m.cnt, E_CHUNKS);
+            got = 0;
+        } else {
+            chunks[ci] = m.chunk_free[top - 1];
+        }
+    }
+    got = __shfl_sync(0xffffffffu, got, gbase);
+    __syncwarp();
+    if (fits && (!need || got)) {
+        double* d = slab_pt(m, chunks, nslab);
+        if (q < 3) d[q] = p[q];
+        else d[q] = c[q - 3];  // covariance entries 0-6 on lanes 3-9
+        if (q < 2) d[10 + q] = c[7 + q];
+        nslab++;
+    }
+}
 
 __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_t* __restrict__ seg_start,
                                                            const uint32_t* __restrict__ seg_end,
@@ -462,37 +474,58 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
                                                            const double* __restrict__ bpts,
                                                            const double* __restrict__ bcov, uint32_t* ev_rec,
                                                            SegScratch ss, int build) {
-    __shared__ int s_chunks[kSegThreads / 32][kMaxChunks];
-    __shared__ int s_saved[kSegThreads / 32][kMaxChunks];
+    __shared__ int s_chunks[kSegThreads / 32][kGroups][kMaxChunks];
+    __shared__ int s_saved[kSegThreads / 32][kGroups][kMaxChunks];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int g = lane / kGroupLanes, q = lane - g * kGroupLanes;  // lanes 30, 31: g == kGroups, idle
+    const int gi = g < kGroups ? g : 0;
+    const int gbase = gi * kGroupLanes;
+    const unsigned gmask = ((1u << kGroupLanes) - 1u) << gbase;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int nseg = *d_n_seg;
     const unsigned long long base = m.cnt->batch_base;
-    int* chunks = s_chunks[wib];
-    int* saved = s_saved[wib];
-    for (int sidx = gw; sidx < nseg; sidx += nw) {
-        const uint32_t rec = seg_rec[sidx];
-        const int b = (int)seg_start[sidx], e = (int)seg_end[sidx];
-        RecHot& H = m.hot[rec];
-        RecCold& Cc = m.cold[rec];
-        // integer state on every lane; mean[lane] (lane < 3), ppt[lane] (lane < 9)
-        uint32_t flags = H.flags;
-        int n = H.n, newly = Cc.newly, nslab = Cc.nslab;
-        double mean_l = lane < 3 ? H.mean[lane] : 0.0;
-        double ppt_l = lane < 9 ? Cc.ppt[lane] : 0.0;
-        if (lane < kMaxChunks) chunks[lane] = Cc.chunks[lane];
+    int* chunks = s_chunks[wib][gi];
+    int* saved = s_saved[wib][gi];
+    // segment groups are taken from a counter: a warp that finishes early
+    // takes the next group instead of idling in its block
+    (void)gw;
+    (void)nw;
+    for (;;) {
+        int s0 = 0;
+        if (lane == 0) s0 = atomicAdd(ss.d_work_chain, kGroups);
+        s0 = __shfl_sync(0xffffffffu, s0, 0);
+        if (s0 >= nseg) break;
+        const int sidx = s0 + g;
+        const bool mine = g < kGroups && sidx < nseg;
+        uint32_t rec = 0, flags = 0;
+        int b = 0, e = 0, n = 0, newly = 0, nslab = 0;
+        double mean_l = 0.0, ppt_l = 0.0;
+        if (mine) {
+            rec = seg_rec[sidx];
+            b = (int)seg_start[sidx];
+            e = (int)seg_end[sidx];
+            const RecHot& H = m.hot[rec];
+            const RecCold& Cc = m.cold[rec];
+            flags = H.flags;
+            n = H.n;
+            newly = Cc.newly;
+            nslab = Cc.nslab;
+            if (q < 3) mean_l = H.mean[q];
+            if (q < 9) ppt_l = Cc.ppt[q];
+            for (int k = q; k < kMaxChunks; k += kGroupLanes) chunks[k] = Cc.chunks[k];
+        }
         __syncwarp();
         int nref = 0, mstart = e;
-        bool have_saved = false;
-        // updatePlane call: a snapshot when it reaches the eigen decomposition
+        bool have_saved = false, done = !mine;
+        // updatePlane call (group-uniform): a snapshot when it reaches the eigen decomposition
         auto refit = [&](int npts, int from_batch) {
             if (n < m.update_thresh) return;
             flags |= F_INIT;
             RefitSnap& sn = ss.snaps[b + nref];
-            if (lane < 3) sn.mean[lane] = mean_l;
-            if (lane < 9) sn.ppt[lane] = ppt_l;
-            if (lane == 0) {
+            if (q < 3) sn.mean[q] = mean_l;
+            if (q < 9) sn.ppt[q] = ppt_l;
+            if (q == 0) {
                 sn.n = n;
                 sn.npts = npts;
                 sn.from_batch = from_batch;
@@ -503,92 +536,117 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             ++nref;
         };
         auto add_point = [&](const double* p) {
-            if (lane < 3) mean_l = mean_l + (p[lane] - mean_l) / ((double)n + 1.0);
-            if (lane < 9) ppt_l = ppt_l + p[lane / 3] * p[lane % 3];
+            if (q < 3) mean_l = mean_l + (p[q] - mean_l) / ((double)n + 1.0);
+            if (q < 9) ppt_l = ppt_l + p[q / 3] * p[q % 3];
             n += 1;
         };
         if (build) {
             // VoxelMap::build: addPoint for every point, one updatePlane at the end.
             const int cnt = e - b;
-            const bool store = (nslab + cnt) < m.max_thresh && !(flags & F_DROPPED);
-            for (int j = b; j < e; ++j) {
-                const uint32_t i = sv[j];
-                const double p[3] = {bpts[(size_t)i * 3], bpts[(size_t)i * 3 + 1], bpts[(size_t)i * 3 + 2]};
-                add_point(p);
-                if (store) warp_slab_append(m, chunks, nslab, p, bcov + (size_t)i * 9, lane);
+            const bool store = mine && (nslab + cnt) < m.max_thresh && !(flags & F_DROPPED);
+            for (int jj = 0;; ++jj) {
+                const bool act = mine && b + jj < e;
+                if (!__any_sync(0xffffffffu, act)) break;
+                double p[3] = {0.0, 0.0, 0.0};
+                const double* c = bcov;
+                if (act) {
+                    const uint32_t i = sv[b + jj];
+                    p[0] = bpts[(size_t)i * 3]; p[1] = bpts[(size_t)i * 3 + 1]; p[2] = bpts[(size_t)i * 3 + 2];
+                    c = bcov + (size_t)i * 9;
+                    add_point(p);
+                }
+                group_slab_append(m, act && store, chunks, nslab, p, c, q, gbase);
             }
-            if (!store) flags |= F_DROPPED;
-            refit(cnt, 1);
-            if (flags & F_DROPPED) {
-                if (lane == 0) slab_release(m, chunks, nslab);
-                nslab = 0;
+            if (mine) {
+                if (!store) flags |= F_DROPPED;
+                refit(cnt, 1);
+                if (flags & F_DROPPED) {
+                    __syncwarp(gmask);
+                    if (q == 0) slab_release(m, chunks, nslab);
+                    nslab = 0;
+                }
+            }
+            __syncwarp();
+        } else {
+            for (int jj = 0;; ++jj) {
+                bool act = !done && b + jj < e;
+                bool init = (flags & F_INIT) != 0;
+                if (act && init && !(flags & F_UPDATE)) {
+                    // frozen: the remaining points only call merge() (if plane)
+                    mstart = b + jj;
+                    done = true;
+                    act = false;
+                }
+                if (!__any_sync(0xffffffffu, act)) break;
+                double p[3] = {0.0, 0.0, 0.0};
+                const double* c = bcov;
+                uint32_t i = 0;
+                if (act) {
+                    i = sv[b + jj];
+                    p[0] = bpts[(size_t)i * 3]; p[1] = bpts[(size_t)i * 3 + 1]; p[2] = bpts[(size_t)i * 3 + 2];
+                    c = bcov + (size_t)i * 9;
+                    add_point(p);
+                }
+                group_slab_append(m, act && !(flags & F_DROPPED), chunks, nslab, p, c, q, gbase);
+                if (act) {
+                    if (!init) {
+                        refit(nslab, 0);
+                    } else {
+                        newly++;
+                        if (newly >= m.update_thresh) {
+                            refit(nslab, 0);
+                            newly = 0;
+                        }
+                        const int size_after = (flags & F_DROPPED) ? n : nslab;
+                        if (size_after >= m.max_thresh) {
+                            flags &= ~F_UPDATE;
+                            flags &= ~F_DROPPED;
+                            if (nref > 0 && !have_saved) {
+                                for (int k = q; k < kMaxChunks; k += kGroupLanes) saved[k] = chunks[k];
+                                have_saved = true;
+                            }
+                            __syncwarp(gmask);
+                            if (q == 0) {
+                                slab_release(m, chunks, nslab);
+                                m.cold[rec].freeze_g = base + i;
+                            }
+                            nslab = 0;
+                            __syncwarp(gmask);
+                        }
+                    }
+                }
                 __syncwarp();
             }
-        } else {
-            for (int j = b; j < e; ++j) {
-                const bool init = (flags & F_INIT) != 0;
-                if (init && !(flags & F_UPDATE)) {
-                    // frozen: the remaining points only call merge() (if plane)
-                    mstart = j;
-                    break;
+        }
+        if (mine) {
+            RecHot& H = m.hot[rec];
+            RecCold& Cc = m.cold[rec];
+            if (nref > 0) {
+                int k = 0;
+                if (q == 0) k = atomicAdd(ss.d_n_covseg, 1);
+                k = __shfl_sync(gmask, k, gbase);
+                CovSeg& cs = ss.covsegs[k];
+                if (q == 0) {
+                    cs.seg = (uint32_t)sidx;
+                    cs.nref = nref;
+                    cs.mstart = mstart;
+                    ss.seg_cov[sidx] = k;
                 }
-                const uint32_t i = sv[j];
-                const double p[3] = {bpts[(size_t)i * 3], bpts[(size_t)i * 3 + 1], bpts[(size_t)i * 3 + 2]};
-                const double* c = bcov + (size_t)i * 9;
-                add_point(p);
-                if (!(flags & F_DROPPED)) warp_slab_append(m, chunks, nslab, p, c, lane);
-                if (!init) {
-                    refit(nslab, 0);
-                } else {
-                    newly++;
-                    if (newly >= m.update_thresh) {
-                        refit(nslab, 0);
-                        newly = 0;
-                    }
-                    const int size_after = (flags & F_DROPPED) ? n : nslab;
-                    if (size_after >= m.max_thresh) {
-                        flags &= ~F_UPDATE;
-                        flags &= ~F_DROPPED;
-                        if (nref > 0 && !have_saved) {
-                            if (lane < kMaxChunks) saved[lane] = chunks[lane];
-                            have_saved = true;
-                        }
-                        __syncwarp();
-                        if (lane == 0) {
-                            slab_release(m, chunks, nslab);
-                            Cc.freeze_g = base + i;
-                        }
-                        nslab = 0;
-                        __syncwarp();
-                    }
-                }
+                for (int t = q; t < kMaxChunks; t += kGroupLanes) cs.chunks[t] = have_saved ? saved[t] : chunks[t];
+            } else if (flags & F_PLANE) {
+                for (int j = mstart + q; j < e; j += kGroupLanes) ev_rec[sv[j]] = rec;  // merge() calls
             }
-        }
-        if (nref > 0) {
-            int k = 0;
-            if (lane == 0) k = atomicAdd(ss.d_n_covseg, 1);
-            k = __shfl_sync(0xffffffffu, k, 0);
-            CovSeg& cs = ss.covsegs[k];
-            if (lane == 0) {
-                cs.seg = (uint32_t)sidx;
-                cs.nref = nref;
-                cs.mstart = mstart;
-                ss.seg_cov[sidx] = k;
+            if (q == 0) {
+                H.flags = flags;
+                H.n = n;
+                Cc.newly = newly;
+                Cc.nslab = nslab;
+                Cc.stamp = base + sv[e - 1];
             }
-            if (lane < kMaxChunks) cs.chunks[lane] = have_saved ? saved[lane] : chunks[lane];
-        } else if (flags & F_PLANE) {
-            for (int j = mstart + lane; j < e; j += 32) ev_rec[sv[j]] = rec;  // merge() calls
+            if (q < 3) H.mean[q] = mean_l;
+            if (q < 9) Cc.ppt[q] = ppt_l;
+            for (int t = q; t < kMaxChunks; t += kGroupLanes) Cc.chunks[t] = chunks[t];
         }
-        if (lane == 0) {
-            H.flags = flags;
-            H.n = n;
-            Cc.newly = newly;
-            Cc.nslab = nslab;
-            Cc.stamp = base + sv[e - 1];
-        }
-        if (lane < 3) H.mean[lane] = mean_l;
-        if (lane < 9) Cc.ppt[lane] = ppt_l;
-        if (lane < kMaxChunks) Cc.chunks[lane] = chunks[lane];
         __syncwarp();
     }
 }
@@ -704,7 +762,13 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
     const int nc = *ss.d_n_covseg;
     int* chunks = sh.chunks[wib];
     double (*stage)[36] = sh.stage[wib];
-    for (int li = gw; li < nc; li += nw) {
+    (void)gw;
+    (void)nw;
+    for (;;) {
+        int li = 0;
+        if (lane == 0) li = atomicAdd(ss.d_work_cov, 1);
+        li = __shfl_sync(0xffffffffu, li, 0);
+        if (li >= nc) break;
         const CovSeg& cs = ss.covsegs[li];
         const uint32_t sidx = cs.seg;
         const int nref = cs.nref, mstart = cs.mstart;
@@ -880,42 +944,55 @@ void launch_map_segments(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
 // Phase B1: the per-voxel pushPoint / addPoint state machine.
 void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
                       cudaStream_t st) {
+    // warps take their work from counters; the grids keep enough warps for
+    // the longest chains to start at once
     int sg = (n_max + (kSegThreads / 32) - 1) / (kSegThreads / 32);
     if (sg > 152 * 16) sg = 152 * 16;
     if (sg < 1) sg = 1;
+    const int cg = sg;
     SegScratch ss{static_cast<RefitSnap*>(ms.seg_snaps), ms.refit_list, static_cast<CovSeg*>(ms.covsegs),
                   ms.seg_cov, ms.term_snap, ms.terms, ms.term_cap, ms.max_batch + 16, ms.d_scratch_int + 5,
-                  ms.d_scratch_int + 6, ms.d_scratch_int + 7};
-    cudaMemsetAsync(ms.d_scratch_int + 5, 0, 3 * sizeof(int), st);
+                  ms.d_scratch_int + 6, ms.d_scratch_int + 7, ms.d_scratch_int + 8, ms.d_scratch_int + 9};
+    cudaMemsetAsync(ms.d_scratch_int + 5, 0, 5 * sizeof(int), st);
     cudaMemsetAsync(ms.term_snap, 0xFF, sizeof(uint32_t) * (size_t)ms.term_cap, st);
     VMP_NOTE_LAUNCH();
     k_seg_chain<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.d_n_seg, ms.sv, bpts, bcov,
                                             ms.ev_rec, ss, build ? 1 : 0);
     // one warp per block so that the refits spread over all SMs
+    int eg = (n_max + 255) / 256;
+    if (eg > 152 * 8) eg = 152 * 8;
+    if (eg < 1) eg = 1;
     VMP_NOTE_LAUNCH();
-    k_refit_eig<<<152 * 8, 32, 0, st>>>(m, ss);
+    k_refit_eig<<<eg, 32, 0, st>>>(m, ss);
     int tg = (2 * n_max + kTermThreads - 1) / kTermThreads;
     if (tg > 152 * 8) tg = 152 * 8;
     if (tg < 1) tg = 1;
     VMP_NOTE_LAUNCH();
     k_cov_terms<<<tg, kTermThreads, 0, st>>>(m, ms.seg_start, ms.sv, bpts, bcov, ss);
     VMP_NOTE_LAUNCH();
-    k_seg_cov<<<sg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.sv, bpts, bcov, ms.ev_rec, ss);
+    k_seg_cov<<<cg, kSegThreads, 0, st>>>(m, ms.seg_start, ms.seg_end, ms.seg_rec, ms.sv, bpts, bcov, ms.ev_rec, ss);
 }
-// Phase B2: merges, LRU queue, evictions, counters.
-void launch_map_finish(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st) {
+// Phase B2: merges, LRU queue, evictions, counters.  In two halves around the
+// merge resolution, so that a captured graph can hold each half.
+void launch_map_finish_pre(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st) {
     const int g = grid_for_map(n_max);
-    if (!build) {
-        VMP_NOTE_LAUNCH(); k_ev_flags<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, ms.flag2);
-        exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_ev, ms.scan, st);
-        VMP_NOTE_LAUNCH(); k_compact_idx<<<g, kMapThreads, 0, st>>>(ms.flag2, ms.rank2, ms.d_n, ms.ev_list);
-        run_merge_events(m, ms, ms.merge, n_max, ms.merge_mode, &ms.merge_rounds, st);
-    }
+    if (build) return;
+    VMP_NOTE_LAUNCH(); k_ev_flags<<<g, kMapThreads, 0, st>>>(ms.ev_rec, ms.d_n, ms.flag2);
+    exclusive_scan_u32(ms.flag2, ms.rank2, ms.d_n, ms.d_n_ev, ms.scan, st);
+    VMP_NOTE_LAUNCH(); k_compact_idx<<<g, kMapThreads, 0, st>>>(ms.flag2, ms.rank2, ms.d_n, ms.ev_list);
+}
+void launch_map_finish_post(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
+    const int g = grid_for_map(n_max);
     exclusive_scan_u32(ms.last_touch, ms.rank2, ms.d_n, ms.d_n_touch, ms.scan, st);
     VMP_NOTE_LAUNCH(); k_queue_append<<<g, kMapThreads, 0, st>>>(m, ms.last_touch, ms.rank2, ms.rec, ms.d_n, ms.d_n_touch);
     VMP_NOTE_LAUNCH(); k_finalize<<<g, kMapThreads, 0, st>>>(m, ms.victims);
     VMP_NOTE_LAUNCH(); k_finalize_chunks<<<g, kMapThreads, 0, st>>>(m);
     VMP_NOTE_LAUNCH(); k_finalize_counters<<<1, 32, 0, st>>>(m, ms.d_n, ms.d_n_touch);
+}
+void launch_map_finish(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st) {
+    launch_map_finish_pre(m, ms, n_max, build, st);
+    if (!build) run_merge_events(m, ms, ms.merge, n_max, ms.merge_mode, &ms.merge_rounds, st);
+    launch_map_finish_post(m, ms, n_max, st);
 }
 void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
                         cudaStream_t st) {

@@ -118,9 +118,11 @@ __device__ inline bool b_entry(const StepSm& d, int i, int j, double& b) {
 
 __device__ inline int inactive_index(int q) { return q < 6 ? 6 + q : 15 + (q - 6); }  // rows/cols 6..11, 15..20
 
-__global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, const vmp_imu* imus, int n_imu,
-                                                                 double t_begin, double t_end, DPose* poses,
+__global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, const vmp_imu* imus,
+                                                                 const DScanHdr* __restrict__ hdr, DPose* poses,
                                                                  DStep* st) {
+    const int n_imu = hdr->n_imu;
+    const double t_begin = hdr->t_start, t_end = hdr->t_end;
     __shared__ double sP[2][529];
     __shared__ double sFP[529];
     __shared__ StepSm sStep[2];
@@ -347,8 +349,8 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
     }
 }
 
-void launch_predict_chain2(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st) {
-    VMP_NOTE_LAUNCH(); k_predict_chain2<<<1, kPredThreads, 0, st>>>(f, s.imus, n_imu, t_start, t_end, s.poses, s.steps);
+void launch_predict_chain2(DFilter* f, DScan& s, cudaStream_t st) {
+    VMP_NOTE_LAUNCH(); k_predict_chain2<<<1, kPredThreads, 0, st>>>(f, s.imus, s.hdr, s.poses, s.steps);
 }
 
 }  // namespace vmp

@@ -15,6 +15,10 @@ namespace vmp {
 
 std::atomic<long long> g_launch_count{0};
 
+static thread_local long long* t_capture_counter = nullptr;
+long long* capture_launch_counter() { return t_capture_counter; }
+void set_capture_launch_counter(long long* c) { t_capture_counter = c; }
+
 long long& dev_bytes_counter() {
     static thread_local long long bytes = 0;
     return bytes;

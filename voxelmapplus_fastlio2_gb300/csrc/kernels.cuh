@@ -7,7 +7,17 @@
 namespace vmp {
 
 // Per-scan device buffers of one stream.
+// Per-scan scalars on the device (one host->device copy per scan), so that a
+// captured graph of the scan needs no per-scan kernel parameters.
+struct DScanHdr {
+    int n_raw;
+    int n_imu;
+    double t_start;
+    double t_end;
+};
+
 struct DScan {
+    DScanHdr* hdr;         // n_raw / n_imu / package times of the current scan
     // raw scan (input) and its time-sorted, undistorted copy
     float4* raw;           // [max_pts] x, y, z, t_ms
     float4* cloud;         // [max_pts] sorted by time, compensated in place
@@ -51,7 +61,7 @@ void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& c
                      cudaStream_t st);
 void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st);
 // ---- k_predict.cu
-void launch_predict_chain2(DFilter* f, DScan& s, int n_imu, double t_start, double t_end, cudaStream_t st);
+void launch_predict_chain2(DFilter* f, DScan& s, cudaStream_t st);
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st);
 void launch_update_begin(DFilter* f, cudaStream_t st);
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
@@ -67,6 +77,9 @@ void launch_body_cov(DScan& s, int n_max, double range_inc, double sin_deg, cuda
 // update) or from the full undistorted cloud (map init)
 void launch_map_batch(DFilter* f, DScan& s, int n_max, bool from_full_cloud, double range_inc, double sin_deg,
                       cudaStream_t st);
+
+// ---- graph capture bookkeeping (k_sort.cu)
+void set_capture_launch_counter(long long* c);
 
 // ---- k_map.cu
 struct MapScratch {
@@ -102,7 +115,7 @@ struct MapScratch {
     int* d_n_seg;
     int* d_n_ev;
     int* d_n_touch;
-    int* d_scratch_int;   // [32]: batch counters; [5], [6], [7] refit / voxel / term list lengths
+    int* d_scratch_int;   // [32]: batch counters; [5]-[7] refit / voxel / term list lengths, [8], [9] work counters
     int max_batch;
     SortScratch sort;
     ScanScratch scan;
@@ -121,6 +134,8 @@ void launch_map_phase_b(DMap& m, MapScratch& ms, const double* bpts, const doubl
 void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
                       cudaStream_t st);
 void launch_map_finish(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st);
+void launch_map_finish_pre(DMap& m, MapScratch& ms, int n_max, bool build, cudaStream_t st);
+void launch_map_finish_post(DMap& m, MapScratch& ms, int n_max, cudaStream_t st);
 void launch_rehash(DMap& m, cudaStream_t st);
 void launch_queue_compact(DMap& m, uint32_t* flag, uint32_t* rank, uint32_t* tr, uint64_t* ts, int* d_len,
                           int* d_live, int len_max, ScanScratch& sc, cudaStream_t st);

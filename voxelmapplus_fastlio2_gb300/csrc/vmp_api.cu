@@ -253,6 +253,13 @@ struct vmp_stream_s {
     long long last_evicted_total = 0;
     long long dev_bytes = 0;  // device memory allocated by vmp_create
     long long eviction_splits = 0;  // batches split by the eviction walk
+    DScanHdr* h_hdr = nullptr;      // pinned staging of the scan header
+    // captured graphs of the steady-state scan, per size class: g1 = time
+    // sort .. voxel state machine, g2 = LRU queue .. result copy (the merge
+    // resolution runs between them)
+    struct ScanGraphs { int nb; cudaGraphExec_t g1, g2; long long k1, k2; };
+    std::vector<ScanGraphs> graphs;
+    bool use_graphs = true;
     bool blocking_wait = false;  // vmp_set_wait_mode
     cudaEvent_t done_ev = nullptr;
     // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
@@ -409,6 +416,11 @@ vmp_status vmp_destroy(vmp_stream_t s) {
     cudaFreeHost(s->h_res);
     cudaFreeHost(s->h_cnt);
     cudaFreeHost(s->h_int);
+    for (auto& gp : s->graphs) {
+        if (gp.g1) cudaGraphExecDestroy(gp.g1);
+        if (gp.g2) cudaGraphExecDestroy(gp.g2);
+    }
+    if (s->h_hdr) cudaFreeHost(s->h_hdr);
     if (s->done_ev) cudaEventDestroy(s->done_ev);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
@@ -482,7 +494,8 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     CREATE_TRY(dalloc(s, &sc.sort_v, max_pts + 16));
     CREATE_TRY(dalloc(s, &sc.flags, max_pts + 16));
     CREATE_TRY(dalloc(s, &sc.scan_out, max_pts + 16));
-    CREATE_TRY(dalloc(s, &sc.d_n_raw, 4));
+    CREATE_TRY(dalloc(s, &sc.hdr, 1));
+    sc.d_n_raw = &sc.hdr->n_raw;
     CREATE_TRY(dalloc(s, &sc.down, max_pts));
     CREATE_TRY(dalloc(s, &sc.d_n_down, 4));
     CREATE_TRY(dalloc(s, &sc.minmax, 8));
@@ -555,6 +568,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     CREATE_TRY(cudaMallocHost(&s->h_res, sizeof(DResult)));
     CREATE_TRY(cudaMallocHost(&s->h_cnt, sizeof(Counters)));
     CREATE_TRY(cudaMallocHost(&s->h_int, sizeof(int) * 16));
+    CREATE_TRY(cudaMallocHost(&s->h_hdr, sizeof(DScanHdr)));
     CREATE_TRY(dalloc(s, &s->d_res, 1));
     launch_map_reset(m, s->st);
     CREATE_TRY(cudaGetLastError());
@@ -675,8 +689,30 @@ static vmp_status upload_scan(vmp_stream_t s, const vmp_point* pts, int n, bool 
         std::memcpy(s->h_pts, pts, sizeof(vmp_point) * (size_t)n);
         VMP_TRY(cudaMemcpyAsync(s->s.raw, s->h_pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyHostToDevice, s->st), "scan upload");
     }
-    VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_raw, n);
     return VMP_OK;
+}
+
+// The scan's scalars (point count, IMU count, package times) in one copy.
+static vmp_status upload_header(vmp_stream_t s, int n, int n_imu, double t_start, double t_end) {
+    s->h_hdr->n_raw = n;
+    s->h_hdr->n_imu = n_imu;
+    s->h_hdr->t_start = t_start;
+    s->h_hdr->t_end = t_end;
+    VMP_TRY(cudaMemcpyAsync(s->s.hdr, s->h_hdr, sizeof(DScanHdr), cudaMemcpyHostToDevice, s->st), "header");
+    s->io_h2d += (long long)sizeof(DScanHdr);
+    return VMP_OK;
+}
+
+// Grid sizes of a scan come from its size class (steps of a quarter octave,
+// at least 1024 points, at most max_scan_points): a captured graph then
+// serves every scan of the class, and graph and direct launches use the same
+// grids (the reduction orders follow the grids).
+static int size_class(int n, int max_pts) {
+    const unsigned v = (unsigned)(n < 1024 ? 1024 : n);
+    const int e = 31 - __builtin_clz(v);
+    const unsigned step = (1u << e) >> 2;
+    const unsigned c = (v + step - 1) / step * step;
+    return (int)(c < (unsigned)max_pts ? c : (unsigned)max_pts);
 }
 
 static vmp_status upload_imus(vmp_stream_t s, const vmp_imu* imus, int n, bool device_ptr) {
@@ -692,13 +728,27 @@ static vmp_status upload_imus(vmp_stream_t s, const vmp_imu* imus, int n, bool d
     return VMP_OK;
 }
 
-static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
-    s->pbeg();
+// The result gathered on the device and copied to the pinned host mirror.
+static vmp_status enqueue_result(vmp_stream_t s) {
     VMP_NOTE_LAUNCH(); k_gather_result<<<1, 256, 0, s->st>>>(s->f, s->s.d_n_down, s->cnt, s->d_res);
     VMP_TRY(cudaGetLastError(), "result launch");
     VMP_TRY(cudaMemcpyAsync(s->h_res, s->d_res, sizeof(DResult), cudaMemcpyDeviceToHost, s->st), "result copy");
+    return VMP_OK;
+}
+
+static vmp_status finish_result_host(vmp_stream_t s, int n_raw, vmp_result* out);
+
+static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
+    s->pbeg();
+    vmp_status v = enqueue_result(s);
+    if (v != VMP_OK) return v;
     s->io_d2h += (long long)sizeof(DResult);
     s->pend(VMP_PROF_RESULT, -1);
+    return finish_result_host(s, n_raw, out);
+}
+
+// Waits for the stream, then reads the result and the device error word.
+static vmp_status finish_result_host(vmp_stream_t s, int n_raw, vmp_result* out) {
     if (s->blocking_wait && s->done_ev) {
         VMP_TRY(cudaEventRecord(s->done_ev, s->st), "scan");
         VMP_TRY(cudaEventSynchronize(s->done_ev), "scan");
@@ -736,6 +786,114 @@ static vmp_status finish_result(vmp_stream_t s, int n_raw, vmp_result* out) {
             return fail(s, VMP_ERR_CAPACITY, "voxel record / slab pool exhausted (error bits " + std::to_string(e) + ")");
     }
     return VMP_OK;
+}
+
+// The scan from the time sort to the map batch (LIOBuilder::process before
+// VoxelMap::update, lio_builder.cpp:175-246); nb sizes the grids.  With
+// map_init the undistorted cloud goes to the map batch (VoxelMap::build).
+static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
+    const vmp_config& cfg = s->cfg;
+    cudaStream_t st = s->st;
+    s->pbeg();
+    launch_time_sort(s->s, nb, s->ss, st);
+    s->pend(VMP_PROF_TIME_SORT, 0);
+    s->pbeg();
+    launch_predict_chain2(s->f, s->s, st);
+    s->pend(VMP_PROF_PREDICT, -1);
+    s->pbeg();
+    launch_undistort(s->f, s->s, nb, st);
+    s->pend(VMP_PROF_UNDISTORT, 0);
+    if (map_init) {
+        s->pbeg();
+        launch_map_batch(s->f, s->s, nb, true, cfg.ranging_cov, s->sin_deg, st);
+        s->pend(VMP_PROF_MAP_BATCH, 0);
+        return;
+    }
+    s->pbeg();
+    if (cfg.scan_resolution > 0.0) launch_downsample(s->s, nb, cfg.scan_resolution, s->ss, s->sc, st);
+    else launch_copy_down(s->s, nb, st);
+    s->pend(VMP_PROF_DOWNSAMPLE, 0);
+    s->pbeg();
+    launch_body_cov(s->s, nb, cfg.ranging_cov, s->sin_deg, st);
+    s->pend(VMP_PROF_BODY_COV, 1);
+    s->pbeg();
+    launch_update_begin(s->f, st);
+    s->pend(VMP_PROF_UPDATE_OTHER, -1);
+    for (int it = 0; it < cfg.ieskf_max_iter; ++it) {
+        s->pbeg();
+        launch_residual_iter(s->f, s->s, s->m, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+        s->pend(VMP_PROF_RESIDUAL, 1);
+    }
+    s->pbeg();
+    launch_update_end(s->f, cfg.estimate_ext, st);
+    s->pend(VMP_PROF_UPDATE_OTHER, -1);
+    s->pbeg();
+    launch_map_batch(s->f, s->s, nb, false, cfg.ranging_cov, s->sin_deg, st);
+    s->pend(VMP_PROF_MAP_BATCH, 1);
+}
+
+// Captures the two graphs of a steady-state scan of size class nb.
+static vmp_status capture_scan_graphs(vmp_stream_t s, int nb, vmp_stream_s::ScanGraphs& gp) {
+    cudaStream_t st = s->st;
+    MapScratch& ms = s->ms;
+    gp = {nb, nullptr, nullptr, 0, 0};
+    for (int part = 0; part < 2; ++part) {
+        long long launches = 0;
+        set_capture_launch_counter(&launches);
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            if (part == 0) {
+                enqueue_scan_front(s, nb, false);
+                VMP_NOTE_LAUNCH(); k_copy_int<<<1, 32, 0, st>>>(ms.d_n, s->s.d_n_batch);
+                launch_map_phase_a(s->m, ms, s->s.bpts, nb, st);
+                launch_map_segments(s->m, ms, nb, st);
+                launch_map_state(s->m, ms, s->s.bpts, s->s.bcov, nb, false, st);
+                launch_map_finish_pre(s->m, ms, nb, false, st);
+            } else {
+                launch_map_finish_post(s->m, ms, nb, st);
+                enqueue_result(s);
+            }
+            cudaGraph_t g = nullptr;
+            e = cudaStreamEndCapture(st, &g);
+            if (e == cudaSuccess) {
+                cudaGraphExec_t x = nullptr;
+                e = cudaGraphInstantiate(&x, g, 0);
+                cudaGraphDestroy(g);
+                if (part == 0) { gp.g1 = x; gp.k1 = launches; }
+                else { gp.g2 = x; gp.k2 = launches; }
+            }
+        }
+        set_capture_launch_counter(nullptr);
+        if (e != cudaSuccess) return cuda_fail(s, e, "scan graph capture");
+    }
+    return VMP_OK;
+}
+
+// The steady-state scan (LIO_MAPPING, no eviction possible, profiler off)
+// as two graph launches around the merge resolution: ~90 kernel launches
+// per scan become 3.
+static vmp_status process_graph(vmp_stream_t s, int n, int nb, vmp_result* out) {
+    cudaStream_t st = s->st;
+    map_maintenance(s);  // host-decided rehash / queue compaction, before the graph
+    vmp_stream_s::ScanGraphs* gp = nullptr;
+    for (auto& g : s->graphs)
+        if (g.nb == nb) gp = &g;
+    if (!gp) {
+        vmp_stream_s::ScanGraphs g{};
+        vmp_status v = capture_scan_graphs(s, nb, g);
+        if (v != VMP_OK) return v;
+        s->graphs.push_back(g);
+        gp = &s->graphs.back();
+    }
+    VMP_TRY(cudaGraphLaunch(gp->g1, st), "scan graph");
+    g_launch_count.fetch_add(gp->k1, std::memory_order_relaxed);
+    s->cur_batch_kind = 1;
+    VMP_TRY(run_merge_events(s->m, s->ms, s->ms.merge, nb, s->ms.merge_mode, &s->ms.merge_rounds, st), "merges");
+    VMP_TRY(cudaGraphLaunch(gp->g2, st), "scan graph");
+    g_launch_count.fetch_add(gp->k2, std::memory_order_relaxed);
+    s->h_size += n;  // upper bound until the result's counters arrive
+    s->io_d2h += (long long)sizeof(DResult);
+    return finish_result_host(s, n, out);
 }
 
 static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, double t_start, double t_end,
@@ -791,57 +949,31 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
         VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
         return finish_result(s, n, out);
     }
+    const int nb = size_class(n, cfg.max_scan_points);
     s->pbeg();
     vmp_status v = upload_scan(s, pts, n, device_ptrs);
     if (v != VMP_OK) return v;
     v = upload_imus(s, imus, n_imu, device_ptrs);
     if (v != VMP_OK) return v;
+    v = upload_header(s, n, n_imu, t_start, t_end);
+    if (v != VMP_OK) return v;
     s->pend(VMP_PROF_UPLOAD, 0);
-    s->pbeg();
-    launch_time_sort(s->s, n, s->ss, st);
-    s->pend(VMP_PROF_TIME_SORT, 0);
-    s->pbeg();
-    launch_predict_chain2(s->f, s->s, n_imu, t_start, t_end, st);
-    s->pend(VMP_PROF_PREDICT, -1);
-    s->pbeg();
-    launch_undistort(s->f, s->s, n, st);
-    s->pend(VMP_PROF_UNDISTORT, 0);
+    if (s->lio_status == VMP_LIO_MAPPING && s->use_graphs && !s->prof_on && s->h_size + (long long)n <= s->m.capacity)
+        return process_graph(s, n, nb, out);
     if (s->lio_status == VMP_MAP_INIT) {
-        s->pbeg();
-        launch_map_batch(s->f, s->s, n, true, cfg.ranging_cov, s->sin_deg, st);
-        s->pend(VMP_PROF_MAP_BATCH, 0);
+        enqueue_scan_front(s, nb, true);
         VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
         VMP_TRY(cudaGetLastError(), "map init launch");
         s->cur_batch_kind = 0;
-        v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, n, true);
+        v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, nb, true);
         if (v != VMP_OK) return v;
         s->lio_status = VMP_LIO_MAPPING;
         return finish_result(s, n, out);
     }
-    s->pbeg();
-    if (cfg.scan_resolution > 0.0) launch_downsample(s->s, n, cfg.scan_resolution, s->ss, s->sc, st);
-    else launch_copy_down(s->s, n, st);
-    s->pend(VMP_PROF_DOWNSAMPLE, 0);
-    s->pbeg();
-    launch_body_cov(s->s, n, cfg.ranging_cov, s->sin_deg, st);
-    s->pend(VMP_PROF_BODY_COV, 1);
-    s->pbeg();
-    launch_update_begin(s->f, st);
-    s->pend(VMP_PROF_UPDATE_OTHER, -1);
-    for (int it = 0; it < cfg.ieskf_max_iter; ++it) {
-        s->pbeg();
-        launch_residual_iter(s->f, s->s, s->m, n, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
-        s->pend(VMP_PROF_RESIDUAL, 1);
-    }
-    s->pbeg();
-    launch_update_end(s->f, cfg.estimate_ext, st);
-    s->pend(VMP_PROF_UPDATE_OTHER, -1);
-    s->pbeg();
-    launch_map_batch(s->f, s->s, n, false, cfg.ranging_cov, s->sin_deg, st);
-    s->pend(VMP_PROF_MAP_BATCH, 1);
+    enqueue_scan_front(s, nb, false);
     VMP_TRY(cudaGetLastError(), "scan launch");
     s->cur_batch_kind = 1;
-    v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, n, false);
+    v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, nb, false);
     if (v != VMP_OK) return v;
     return finish_result(s, n, out);
 }
@@ -1103,9 +1235,12 @@ vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* im
     if (v != VMP_OK) return v;
     v = upload_imus(s, imus, n_imu, false);
     if (v != VMP_OK) return v;
-    launch_time_sort(s->s, n, s->ss, s->st);
-    launch_predict_chain2(s->f, s->s, n_imu, scan->t_start, scan->t_end, s->st);
-    launch_undistort(s->f, s->s, n, s->st);
+    v = upload_header(s, n, n_imu, scan->t_start, scan->t_end);
+    if (v != VMP_OK) return v;
+    const int nb = size_class(n, s->cfg.max_scan_points);
+    launch_time_sort(s->s, nb, s->ss, s->st);
+    launch_predict_chain2(s->f, s->s, s->st);
+    launch_undistort(s->f, s->s, nb, s->st);
     VMP_TRY(cudaGetLastError(), "undistort");
     VMP_TRY(cudaMemcpyAsync(out, s->s.cloud, sizeof(vmp_point) * (size_t)n, cudaMemcpyDeviceToHost, s->st), "cloud");
     VMP_TRY(cudaStreamSynchronize(s->st), "undistort");
@@ -1194,6 +1329,11 @@ vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode) {
     return VMP_OK;
 }
 long long vmp_device_bytes(vmp_stream_t s) { return s ? s->dev_bytes : -1; }
+vmp_status vmp_set_graphs(vmp_stream_t s, int on) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    s->use_graphs = on != 0;
+    return VMP_OK;
+}
 long long vmp_eviction_splits(vmp_stream_t s) { return s ? s->eviction_splits : -1; }
 vmp_status vmp_set_wait_mode(vmp_stream_t s, int blocking) {
     if (!s) return VMP_ERR_INVALID_ARG;
