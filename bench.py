@@ -71,7 +71,7 @@ def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed scans (per stream for the served workload; default 8 there, 60 otherwise)")
+                    help="timed scans (per stream for the served workload; default 16 there, 60 otherwise)")
     ap.add_argument("--warmup", type=int, default=None, help="warm-up scans (default 3 served, 5 otherwise)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room"])
@@ -88,7 +88,7 @@ def parse():
     ap.add_argument("--flush-mb", type=int, default=256)
     a = ap.parse_args()
     if a.steps is None:
-        a.steps = 8 if a.workload == "serve" else 60
+        a.steps = 16 if a.workload == "serve" else 60
     if a.warmup is None:
         a.warmup = 3 if a.workload == "serve" else 5
     return a
@@ -485,25 +485,41 @@ def run_cpu_served(streams, pkgs, warmup, steps, threads, stream_ids):
     return len(stream_ids) * steps / wall, wall
 
 
-def dist_setup(args):
+def dist_setup(args, backend=None):
+    """One process per GPU (torchrun): rank, world size, a barrier and a max
+    over ranks.  NCCL on GPU machines; gloo (CPU tensors) where no GPU is
+    visible, which is how the multi-rank path is tested here."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws <= 1:
         return rank, ws, (lambda: None), (lambda x: x), None
     import torch
     import torch.distributed as dist
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if backend is None:
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dev = "cuda"
+    else:
+        dist.init_process_group("gloo")
+        dev = "cpu"
 
     def barrier():
         dist.barrier()
 
     def allmax(x):
-        t = torch.tensor([float(x)], device="cuda")
+        t = torch.tensor([float(x)], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
     return rank, ws, barrier, allmax, dist
+
+
+def aggregate_value(ws, scans_per_rank, wall_s, allmax):
+    """Whole-job scans/s: every rank's scans over the slowest rank's time
+    (weak scaling: each rank serves its own streams)."""
+    return ws * scans_per_rank / allmax(wall_s)
 
 
 def roofline_of(prof):
@@ -571,7 +587,7 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
     uval = run_value(uargs, upk, ucfg, 2, barrier)
     uval_s = sum(uval["step_ms"]) / 1e3
     dv = served["device"]
-    value = ws * dv["scans"] / allmax(dv["wall_s"])
+    value = aggregate_value(ws, dv["scans"], dv["wall_s"], allmax)
     hv = served["host"]
     h2d = float(np.mean([p.n * C.sizeof(abi.vmp_point) + p.n_imu * C.sizeof(abi.vmp_imu)
                          for pk in pkgs for p in pk[2 + W + K:2 + W + 2 * K]]))
