@@ -412,9 +412,10 @@ void VoxelGrid::updatePlane() {  // voxel_map.cpp:97-136
     if (evals[0] > plane_thresh) { is_plane = false; return; }
     is_plane = true;
     // J = [evecs * F; I / n] (voxel_map.cpp:115-130).  The per-refit factors
-    // are formed once, and the products with J's known zeros (row 0 of F, the
-    // off-diagonal of I / n) are left out: the same sums without their +-0
-    // terms.
+    // are formed once, the products with J's known zeros (row 0 of F, the
+    // off-diagonal of I / n) are left out (the same sums without their +-0
+    // terms), and J cov J^T is accumulated as the symmetric matrix it is:
+    // its upper triangle per point, mirrored after the refit's points.
     const double inv_n = 1.0 / static_cast<double>(plane.n);
     V3 pn = v3(evecs(0, 0), evecs(1, 0), evecs(2, 0));
     M3 Mm[3];
@@ -435,17 +436,15 @@ void VoxelGrid::updatePlane() {  // voxel_map.cpp:97-136
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) top(i, j) = evecs(i, 1) * F(1, j) + evecs(i, 2) * F(2, j);
         const M3 A = top * pv.cov;  // rows 0-2 of J * cov
-        M3 B;                       // rows 3-5
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) B(i, j) = inv_n * pv.cov(i, j);
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
-                plane.cov(i, j) += (A(i, 0) * top(j, 0) + A(i, 1) * top(j, 1)) + A(i, 2) * top(j, 2);
+                if (j >= i) plane.cov(i, j) += (A(i, 0) * top(j, 0) + A(i, 1) * top(j, 1)) + A(i, 2) * top(j, 2);
                 plane.cov(i, 3 + j) += A(i, j) * inv_n;
-                plane.cov(3 + i, j) += (B(i, 0) * top(j, 0) + B(i, 1) * top(j, 1)) + B(i, 2) * top(j, 2);
-                plane.cov(3 + i, 3 + j) += B(i, j) * inv_n;
+                if (j >= i) plane.cov(3 + i, 3 + j) += (inv_n * pv.cov(i, j)) * inv_n;
             }
     }
+    for (int i = 0; i < 6; ++i)
+        for (int j = i + 1; j < 6; ++j) plane.cov(j, i) = plane.cov(i, j);
     double axis_distance = -dot(plane.mean, pn);
     if (axis_distance < 0.0) pn = -pn;
     plane.norm = pn;

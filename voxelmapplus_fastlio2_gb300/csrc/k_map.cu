@@ -329,10 +329,17 @@ __device__ inline void refit_const(const double* mean, int n, const double* ev, 
     k.inv_n = 1.0 / (double)n;
 }
 
-// Per-point term J * cov * J^T, without the products with J's known zeros
-// (row 0 of F, the off-diagonal of I / n): the same sums without their +-0
-// terms, as the oracle forms them.
-__device__ inline void plane_cov_term(const double* p, const double* cov, const RefitConst& k, double* out36) {
+// J cov J^T is symmetric: its 21 upper-triangle entries (row-major over the
+// 6x6, i <= j) are formed per point and mirrored when the voxel's covariance
+// is written back, as the oracle does.
+constexpr int kCovTerms = 21;
+__device__ __constant__ unsigned char kUpper[kCovTerms] = {0,  1,  2,  3,  4,  5,  7,  8,  9,  10, 11,
+                                                           14, 15, 16, 17, 21, 22, 23, 28, 29, 35};
+
+// Per-point term of J * cov * J^T (its upper triangle), without the products
+// with J's known zeros (row 0 of F, the off-diagonal of I / n): the same sums
+// without their +-0 terms, as the oracle forms them.
+__device__ inline void plane_cov_term(const double* p, const double* cov, const RefitConst& k, double* out21) {
     const double d[3] = {p[0] - k.mean[0], p[1] - k.mean[1], p[2] - k.mean[2]};
     double F1[3], F2[3];
     {
@@ -347,18 +354,28 @@ __device__ inline void plane_cov_term(const double* p, const double* cov, const 
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) top[i * 3 + j] = k.evecs[i * 3 + 1] * F1[j] + k.evecs[i * 3 + 2] * F2[j];
     mm<3, 3, 3>(top, cov, A);
+    int q = 0;
+    for (int i = 0; i < 3; ++i)  // rows 0-2: (i, j >= i) then (i, 3 + j)
+        for (int j = i; j < 3; ++j)
+            out21[q++] = (A[i * 3] * top[j * 3] + A[i * 3 + 1] * top[j * 3 + 1]) + A[i * 3 + 2] * top[j * 3 + 2];
+    // q == 6; the order below follows kUpper: row i's (i, 3 + j) entries come
+    // after row i's (i, j <= 2) entries in row-major order
+    double tr[9], br[6];
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            const double B_ij = k.inv_n * cov[i * 3 + j];
-            out36[i * 6 + j] = (A[i * 3] * top[j * 3] + A[i * 3 + 1] * top[j * 3 + 1]) + A[i * 3 + 2] * top[j * 3 + 2];
-            out36[i * 6 + 3 + j] = A[i * 3 + j] * k.inv_n;
-            out36[(3 + i) * 6 + 3 + j] = B_ij * k.inv_n;
-        }
-    for (int i = 0; i < 3; ++i) {
-        const double B0 = k.inv_n * cov[i * 3], B1 = k.inv_n * cov[i * 3 + 1], B2 = k.inv_n * cov[i * 3 + 2];
-        for (int j = 0; j < 3; ++j)
-            out36[(3 + i) * 6 + j] = (B0 * top[j * 3] + B1 * top[j * 3 + 1]) + B2 * top[j * 3 + 2];
-    }
+        for (int j = 0; j < 3; ++j) tr[i * 3 + j] = A[i * 3 + j] * k.inv_n;
+    int u = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) br[u++] = (k.inv_n * cov[i * 3 + j]) * k.inv_n;
+    // assemble in kUpper order: row 0: (0,0..2) tl, (0,3..5) tr; row 1: (1,1..2) tl,
+    // (1,3..5) tr; row 2: (2,2) tl, (2,3..5) tr; rows 3-5: br
+    const double tl[6] = {out21[0], out21[1], out21[2], out21[3], out21[4], out21[5]};
+    out21[0] = tl[0]; out21[1] = tl[1]; out21[2] = tl[2];
+    out21[3] = tr[0]; out21[4] = tr[1]; out21[5] = tr[2];
+    out21[6] = tl[3]; out21[7] = tl[4];
+    out21[8] = tr[3]; out21[9] = tr[4]; out21[10] = tr[5];
+    out21[11] = tl[5];
+    out21[12] = tr[6]; out21[13] = tr[7]; out21[14] = tr[8];
+    for (int v = 0; v < 6; ++v) out21[15 + v] = br[v];
 }
 
 // ---------------------------------------------------------------- voxel state machine
@@ -420,7 +437,7 @@ struct SegScratch {
     CovSeg* covsegs;      // [max_batch]
     int* seg_cov;         // [max_batch] covseg index of a segment with snapshots
     uint32_t* term_snap;  // [term_cap] snapshot of each covariance term (kNoRec: unused slot)
-    double* terms;        // [term_cap][36]
+    double* terms;        // [term_cap][21] upper triangles
     int term_cap;
     int snap_cap;         // snapshots (max_batch + 16)
     int* d_n_refit;
@@ -713,7 +730,7 @@ __global__ void __launch_bounds__(kTermThreads) k_cov_terms(DMap m, const uint32
                                                            const uint32_t* __restrict__ sv,
                                                            const double* __restrict__ bpts,
                                                            const double* __restrict__ bcov, SegScratch ss) {
-    __shared__ double stage[kTermThreads * 36];
+    __shared__ double stage[kTermThreads * kCovTerms];
     int nt = *ss.d_n_terms;
     if (nt > ss.term_cap) nt = ss.term_cap;
     for (int t0 = blockIdx.x * kTermThreads; t0 < nt; t0 += gridDim.x * kTermThreads) {
@@ -730,18 +747,19 @@ __global__ void __launch_bounds__(kTermThreads) k_cov_terms(DMap m, const uint32
                 double pc[12];
                 const int* chunks = ss.covsegs[ss.seg_cov[sn.seg]].chunks;
                 const double* src = term_point(m, sn, j, chunks, sv, seg_start, bpts, bcov, pc);
-                plane_cov_term(src, src + 3, kc, stage + threadIdx.x * 36);
+                plane_cov_term(src, src + 3, kc, stage + threadIdx.x * kCovTerms);
             }
         }
         __syncthreads();
         const int cnt = min(kTermThreads, nt - t0);
-        for (int q = threadIdx.x; q < cnt * 36; q += kTermThreads) ss.terms[(size_t)t0 * 36 + q] = stage[q];
+        for (int q = threadIdx.x; q < cnt * kCovTerms; q += kTermThreads)
+            ss.terms[(size_t)t0 * kCovTerms + q] = stage[q];
         __syncthreads();
     }
 }
 
 struct CovShared {
-    double stage[kSegThreads / 32][32][36];
+    double stage[kSegThreads / 32][32][kCovTerms];
     int chunks[kSegThreads / 32][kMaxChunks];
 };
 
@@ -761,7 +779,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int nc = *ss.d_n_covseg;
     int* chunks = sh.chunks[wib];
-    double (*stage)[36] = sh.stage[wib];
+    double (*stage)[kCovTerms] = sh.stage[wib];
     (void)gw;
     (void)nw;
     for (;;) {
@@ -779,8 +797,9 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
         uint32_t flags = H.flags;
         double norm[3] = {H.norm[0], H.norm[1], H.norm[2]};
         double center[3] = {Cc.center[0], Cc.center[1], Cc.center[2]};
-        // lane q accumulates entry q, lanes 0-3 also entry 32 + q
-        double c0 = Cc.cov[lane], c1 = lane < 4 ? Cc.cov[32 + lane] : 0.0;
+        // lane q < 21 accumulates upper-triangle entry kUpper[q]
+        const int ent = lane < kCovTerms ? kUpper[lane] : 0;
+        double c0 = lane < kCovTerms ? Cc.cov[ent] : 0.0;
         if (lane < kMaxChunks) chunks[lane] = cs.chunks[lane];
         __syncwarp();
         for (int r = 0; r < nref; ++r) {
@@ -792,11 +811,9 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
             flags |= F_PLANE;
             const int npts = sn.npts;
             if (sn.toff >= 0) {
-                const double* tp = ss.terms + (size_t)sn.toff * 36;
-                for (int j = 0; j < npts; ++j) {
-                    c0 = c0 + tp[j * 36 + lane];
-                    if (lane < 4) c1 = c1 + tp[j * 36 + 32 + lane];
-                }
+                const double* tp = ss.terms + (size_t)sn.toff * kCovTerms;
+                if (lane < kCovTerms)
+                    for (int j = 0; j < npts; ++j) c0 = c0 + tp[j * kCovTerms + lane];
             } else {
                 RefitConst kc;
                 snap_const(sn, kc);
@@ -809,10 +826,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
                     }
                     __syncwarp();
                     const int cnt = min(32, npts - base);
-                    for (int u = 0; u < cnt; ++u) {
-                        c0 = c0 + stage[u][lane];
-                        if (lane < 4) c1 = c1 + stage[u][32 + lane];
-                    }
+                    if (lane < kCovTerms)
+                        for (int u = 0; u < cnt; ++u) c0 = c0 + stage[u][lane];
                     __syncwarp();
                 }
             }
@@ -827,8 +842,10 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
             H.flags = flags;
             for (int k = 0; k < 3; ++k) { H.norm[k] = norm[k]; Cc.center[k] = center[k]; }
         }
-        Cc.cov[lane] = c0;
-        if (lane < 4) Cc.cov[32 + lane] = c1;
+        if (lane < kCovTerms) {  // the upper triangle and its mirror
+            Cc.cov[ent] = c0;
+            Cc.cov[(ent % 6) * 6 + ent / 6] = c0;
+        }
         __syncwarp();
     }
 }
@@ -1128,7 +1145,7 @@ cudaError_t map_scratch_alloc(MapScratch& ms, int max_batch, int rec_pool, int t
     // that do not fit are formed by k_seg_cov itself
     ms.term_cap = term_cap > 0 ? term_cap : 4 * max_batch + 65536;
     if ((e = dev_malloc(&ms.term_snap, sizeof(uint32_t) * (size_t)ms.term_cap)) != cudaSuccess) return e;
-    if ((e = dev_malloc(&ms.terms, sizeof(double) * 36 * (size_t)ms.term_cap)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms.terms, sizeof(double) * kCovTerms * (size_t)ms.term_cap)) != cudaSuccess) return e;
     ms.merge_mode = 0;
     ms.merge_rounds = 0;
     ms.merge_d2h = 0;

@@ -105,7 +105,7 @@ struct MapScratch {
     uint32_t* refit_list; // [max_batch]
     int* seg_cov;         // [max_batch] voxel-with-refits index of a segment
     uint32_t* term_snap;  // [term_cap] refit of each plane covariance term
-    double* terms;        // [term_cap][36] plane covariance terms
+    double* terms;        // [term_cap][21] plane covariance terms (upper triangles)
     int term_cap;
     int merge_mode;
     int merge_rounds;
