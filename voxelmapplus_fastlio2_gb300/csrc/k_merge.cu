@@ -70,6 +70,7 @@ struct MergeCtl {
     int pad;
     unsigned int bar_count;
     unsigned int bar_gen;
+    unsigned int epoch;  // batches resolved so far (tags rec_round)
 };
 
 struct MergeScratch {
@@ -78,6 +79,7 @@ struct MergeScratch {
     uint64_t* sig;          // [max_batch] per call signature
     uint32_t* cand;         // [max_batch * 6] mergeable neighbours per call (kNone: none)
     uint32_t* queue;        // [max_batch] calls that merge in the current round
+    uint32_t* rec_round;    // [rec_pool] (epoch << 8) | the last round that wrote the record
     MergeCtl* ctl;
     int pool;
     int rec_pool;
@@ -327,7 +329,7 @@ __device__ inline void wtraces(const WState& s, double& tn, double& tm) {
 // Appends one output state to the log; returns its contribution to the
 // call's signature (the same on every lane).
 __device__ inline uint64_t wstate_emit(MergeScratch& g, int cur, uint32_t rec, uint32_t t, const WState& s, int lane,
-                                       bool& overflow) {
+                                       bool& overflow, uint32_t round_tag) {
     uint64_t h = mix64(0x51ull + lane, __double_as_longlong(s.c0));
     if (lane < 4) h = mix64(h, __double_as_longlong(s.c1));
     if (lane == 0) {
@@ -345,6 +347,7 @@ __device__ inline uint64_t wstate_emit(MergeScratch& g, int cur, uint32_t rec, u
         return h;
     }
     MEntry& en = g.ent[cur][pos];
+    if (lane == 0) g.rec_round[rec] = round_tag;
     en.s.cov[lane] = s.c0;
     if (lane < 4) en.s.cov[32 + lane] = s.c1;
     if (lane == 0) {
@@ -362,7 +365,8 @@ __device__ inline uint64_t wstate_emit(MergeScratch& g, int cur, uint32_t rec, u
 // One merge() call on one warp, against the previous round's log; writes its
 // outputs to log `cur` and returns the call's signature.
 __device__ uint64_t warp_merge_call(const DMap& m, MergeScratch& g, uint32_t a_rec, uint32_t t, const uint32_t* cand,
-                                    const MEntry* pent, const uint32_t* phead, int cur, bool& overflow) {
+                                    const MEntry* pent, const uint32_t* phead, int cur, bool& overflow,
+                                    uint32_t round_tag) {
     const int lane = threadIdx.x & 31;
     uint32_t ea = 0;
     if (lane == 0) ea = find_entry(a_rec, t, pent, phead);
@@ -413,10 +417,10 @@ __device__ uint64_t warp_merge_call(const DMap& m, MergeScratch& g, uint32_t a_r
         b.merged = 1;
         for (int r = 0; r < 3; ++r) { a.mean[r] = nmean[r]; a.norm[r] = nnorm[r]; b.mean[r] = nmean[r]; b.norm[r] = nnorm[r]; }
         a.c0 = nc0; a.c1 = nc1; b.c0 = nc0; b.c1 = nc1;
-        sig = mix64(sig, wstate_emit(g, cur, b_rec, t, b, lane, overflow));
+        sig = mix64(sig, wstate_emit(g, cur, b_rec, t, b, lane, overflow, round_tag));
         ++nout;
     }
-    if (nout > 0) sig = mix64(sig, wstate_emit(g, cur, a_rec, t, a, lane, overflow));
+    if (nout > 0) sig = mix64(sig, wstate_emit(g, cur, a_rec, t, a, lane, overflow, round_tag));
     return mix64(sig, (uint64_t)nout);
 }
 
@@ -434,7 +438,9 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
     // the three logs still hold the previous batch's entries: unlink them
     int old_n[kLogs];
     for (int b = 0; b < kLogs; ++b) old_n[b] = min(c->n_ent[b], g.pool);
+    const unsigned int epoch = (c->epoch + 1u) & 0xFFFFFFu;  // tags of this batch: (epoch << 8) | round
     grid_barrier(c);
+    if (tid == 0) c->epoch = epoch;
     if (tid == 0) {
         for (int b = 0; b < kLogs; ++b) c->n_ent[b] = 0;
         c->overflow = 0;
@@ -455,11 +461,22 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
             const int nn = min(c->n_ent[nxt], g.pool);
             for (int e = tid; e < nn; e += nth) g.head[nxt][g.ent[nxt][e].rec] = kNone;
         }
-        // one thread per call: does it merge anything?
+        // one thread per call: does it merge anything?  A call that merged
+        // nothing last time and none of whose records the last two logs
+        // wrote sees the base states it saw then: the same no-op.
+        const uint32_t cut = (epoch << 8) | (uint32_t)(r >= 2 ? r - 2 : 0);
         for (int e = tid; e < ne; e += nth) {
             const uint32_t t = ev_list[e];
             const uint32_t a_rec = ev_rec[t];
             uint32_t cl[6];
+            if (!first && g.sig[e] == noop_sig) {
+                bool dirty = g.rec_round[a_rec] >= cut && (g.rec_round[a_rec] >> 8) == epoch;
+                for (int k = 0; k < 6 && !dirty; ++k) {
+                    const uint32_t b = g.cand[(size_t)e * 6 + k];
+                    if (b != kNone) dirty = g.rec_round[b] >= cut && (g.rec_round[b] >> 8) == epoch;
+                }
+                if (!dirty) continue;
+            }
             if (first) {
                 const unsigned long long T = m.cnt->batch_base + t;
                 int64_t x, y, z;
@@ -490,7 +507,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
             const uint32_t a_rec = ev_rec[t];
             uint32_t cl[6];
             for (int k = 0; k < 6; ++k) cl[k] = g.cand[(size_t)e * 6 + k];
-            const uint64_t sg = warp_merge_call(m, g, a_rec, t, cl, pent, phead, cur, ovf);
+            const uint64_t sg = warp_merge_call(m, g, a_rec, t, cl, pent, phead, cur, ovf, (epoch << 8) | (uint32_t)r);
             if (lane == 0) {
                 if (first || g.sig[e] != sg) atomicAdd(&c->changed[r], 1);
                 g.sig[e] = sg;
@@ -535,6 +552,8 @@ cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool) {
     if ((e = dev_malloc(&ms->sig, sizeof(uint64_t) * nb)) != cudaSuccess) return e;
     if ((e = dev_malloc(&ms->cand, sizeof(uint32_t) * 6 * nb)) != cudaSuccess) return e;
     if ((e = dev_malloc(&ms->queue, sizeof(uint32_t) * nb)) != cudaSuccess) return e;
+    if ((e = dev_malloc(&ms->rec_round, sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
+    if ((e = cudaMemset(ms->rec_round, 0, sizeof(uint32_t) * (size_t)rec_pool)) != cudaSuccess) return e;
     if ((e = dev_malloc(&ms->ctl, sizeof(MergeCtl))) != cudaSuccess) return e;
     if ((e = cudaMemset(ms->ctl, 0, sizeof(MergeCtl))) != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
@@ -560,6 +579,7 @@ void merge_scratch_free(void* p) {
     cudaFree(ms->sig);
     cudaFree(ms->cand);
     cudaFree(ms->queue);
+    cudaFree(ms->rec_round);
     cudaFree(ms->ctl);
     delete ms;
 }
