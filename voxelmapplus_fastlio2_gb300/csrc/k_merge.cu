@@ -83,8 +83,8 @@ struct MergeScratch {
     MergeCtl* ctl;
     int pool;
     int rec_pool;
-    int coop_grid;   // CTAs of one fixed-point launch
-    int coop_slots;  // launches that may be on the device at once (their CTAs all fit co-resident)
+    int coop_capacity;  // CTAs of k_merge_fixpoint the device holds at once
+    int sms;
 };
 
 __device__ inline void base_state(const DMap& m, uint32_t r, MState& s) {
@@ -561,15 +561,8 @@ cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool) {
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge_fixpoint, kMergeThreads, 0)) != cudaSuccess)
         return e;
-    // half the SMs per launch: a few launches (from the streams of a server)
-    // can be resident together, and their grids together never exceed what
-    // the device holds at once
-    const int capacity = sms * per_sm;
-    ms->coop_grid = sms / 2 > 0 ? sms / 2 : 1;
-    if (ms->coop_grid > capacity) ms->coop_grid = capacity;
-    ms->coop_slots = capacity / (ms->coop_grid > 0 ? ms->coop_grid : 1);
-    if (ms->coop_slots < 1) ms->coop_slots = 1;
-    if (ms->coop_slots > 8) ms->coop_slots = 8;
+    ms->coop_capacity = sms * per_sm;
+    ms->sms = sms;
     return cudaSuccess;
 }
 void merge_scratch_free(void* p) {
@@ -582,6 +575,18 @@ void merge_scratch_free(void* p) {
     cudaFree(ms->rec_round);
     cudaFree(ms->ctl);
     delete ms;
+}
+
+constexpr int kMaxCoopSlots = 8;
+static std::mutex g_coop_mu;
+static std::vector<cudaEvent_t> g_coop_done;  // completion of the last launches, one per slot
+static unsigned long long g_coop_next = 0;
+static int g_coop_slots = 1;
+static bool g_coop_throughput = false;
+
+void merge_set_throughput_mode() {
+    std::lock_guard<std::mutex> lk(g_coop_mu);
+    g_coop_throughput = true;
 }
 
 // The merge calls of one batch: the cooperative fixed point, then the replay
@@ -599,31 +604,46 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     cudaError_t e;
     // converged = 0; wait_error, pad, bar_count = 0 (bar_gen keeps counting)
     if ((e = cudaMemsetAsync(&g.ctl->converged, 0, sizeof(int) * 3 + sizeof(unsigned int), st)) != cudaSuccess) return e;
-    if (g.coop_grid > 0) {
-        // At most coop_slots fixed-point launches on the device at once (from
-        // any stream of the process): launch i waits for launch i - slots.
-        // Their CTAs then always fit co-resident, so no launch can wait for
-        // CTAs that the others hold while they wait themselves.
-        static std::mutex mu;
-        static std::vector<cudaEvent_t> done;
-        static unsigned long long next = 0;
-        std::lock_guard<std::mutex> lk(mu);
-        if (done.empty()) {
-            done.assign(g.coop_slots, nullptr);
-            for (auto& ev : done)
+    if (g.coop_capacity > 0) {
+        // Launch sizing (process-wide): alone, one launch at a time on the
+        // whole device; once a server runs many streams, half the SMs per
+        // launch and at most capacity / grid launches on the device at once
+        // (launch i waits for launch i - slots; on a switch, for all
+        // earlier ones).  Their CTAs then always fit co-resident, so no
+        // launch can wait for CTAs that the others hold while they wait.
+        std::lock_guard<std::mutex> lk(g_coop_mu);
+        if (g_coop_done.empty()) {
+            g_coop_done.assign(kMaxCoopSlots, nullptr);
+            for (auto& ev : g_coop_done)
                 if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
                     cudaGetLastError();
                     ev = nullptr;
                 }
         }
-        cudaEvent_t slot = done[next++ % done.size()];
-        if (slot) cudaStreamWaitEvent(st, slot, 0);
+        int grid = g.coop_capacity, slots = 1;
+        if (g_coop_throughput) {
+            grid = g.sms / 2 > 0 ? g.sms / 2 : 1;
+            if (grid > g.coop_capacity) grid = g.coop_capacity;
+            slots = g.coop_capacity / grid;
+            if (slots < 1) slots = 1;
+            if (slots > kMaxCoopSlots) slots = kMaxCoopSlots;
+        }
+        if (slots != g_coop_slots) {
+            for (auto ev : g_coop_done)
+                if (ev) cudaStreamWaitEvent(st, ev, 0);
+            g_coop_slots = slots;
+            g_coop_next = 0;
+        } else {
+            cudaEvent_t prev = g_coop_done[g_coop_next % slots];
+            if (prev) cudaStreamWaitEvent(st, prev, 0);
+        }
+        cudaEvent_t mine = g_coop_done[g_coop_next % slots];
+        ++g_coop_next;
         void* args[] = {(void*)&m, (void*)&g, (void*)&ms.ev_list, (void*)&ms.ev_rec, (void*)&ms.d_n_ev};
         VMP_NOTE_LAUNCH();
-        e = cudaLaunchCooperativeKernel((const void*)k_merge_fixpoint, dim3(g.coop_grid), dim3(kMergeThreads), args, 0,
-                                        st);
+        e = cudaLaunchCooperativeKernel((const void*)k_merge_fixpoint, dim3(grid), dim3(kMergeThreads), args, 0, st);
         if (e != cudaSuccess) cudaGetLastError();  // the replay below produces the result
-        if (slot) cudaEventRecord(slot, st);
+        if (mine) cudaEventRecord(mine, st);
     }
     VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev, g.ctl);
     return cudaGetLastError();

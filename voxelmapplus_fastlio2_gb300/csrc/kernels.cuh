@@ -149,5 +149,8 @@ void merge_scratch_free(void* p);
 cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, int mode, int* rounds_out,
                              cudaStream_t st);
 int merge_rounds_read(void* scratch, cudaStream_t st);
+// Many streams from now on (a server exists): cooperative merge launches use
+// half the SMs and run several at once instead of one at a time on all SMs.
+void merge_set_throughput_mode();
 
 }  // namespace vmp

@@ -23,6 +23,10 @@
 
 #include "vmp.h"
 
+namespace vmp {
+void merge_set_throughput_mode();
+}
+
 namespace {
 
 struct Package {
@@ -143,6 +147,8 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
     // if the process has not created its CUDA context yet; a caller's own
     // setting wins.
     setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+    // cooperative merges of many streams: half the device each, several at once
+    vmp::merge_set_throughput_mode();
     vmp_server_t sv = new (std::nothrow) vmp_server_s();
     if (!sv) return VMP_ERR_OUT_OF_MEMORY;
     sv->cfg = cfg;
