@@ -74,7 +74,10 @@ def parse():
                     help="timed scans (per stream for the served workload; default 16 there, 60 otherwise)")
     ap.add_argument("--warmup", type=int, default=None, help="warm-up scans (default 3 served, 5 otherwise)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room", "planefit", "corridor"])
+    ap.add_argument("--voxels", type=int, default=1_000_000, help="planefit workload: voxels per batch")
+    ap.add_argument("--fit-mode", default="fp32c", choices=["fp64", "fp32", "fp32c"],
+                    help="planefit workload: arithmetic mode of the headline value")
     ap.add_argument("--streams", type=int, default=64, help="served workload: concurrent sensor streams")
     ap.add_argument("--workers", type=int, default=0, help="served workload: server worker threads (0: streams, <= 32)")
     ap.add_argument("--open-loop-scans", type=int, default=15, help="served workload: 10 Hz scans per stream")
@@ -88,9 +91,11 @@ def parse():
     ap.add_argument("--flush-mb", type=int, default=256)
     a = ap.parse_args()
     if a.steps is None:
-        a.steps = 16 if a.workload == "serve" else 60
+        a.steps = {"serve": 16, "planefit": 200, "corridor": 400}.get(a.workload, 60)
     if a.warmup is None:
-        a.warmup = 3 if a.workload == "serve" else 5
+        a.warmup = 3 if a.workload in ("serve", "corridor") else 5
+    if a.workload == "corridor" and "--streams" not in sys.argv:
+        a.streams = 16
     return a
 
 
@@ -369,7 +374,7 @@ def _stage_device(pk):
     return torch.from_numpy(pts).cuda(), torch.from_numpy(imu).cuda()
 
 
-def run_served(args, streams, pkgs, workers, phases, barrier):
+def run_served(args, streams, pkgs, workers, phases, barrier, keep_results=False):
     """One server, all streams.  Per stream the packages run in order:
     IMU_INIT + MAP_INIT + warm-up, then the phases:
       "device": K packages per stream, already in HBM, all submitted at once;
@@ -450,6 +455,10 @@ def run_served(args, streams, pkgs, workers, phases, barrier):
                        "service_ms": {"p50": float(np.percentile(svc, 50)), "p99": float(np.percentile(svc, 99))},
                        "launches": launches, "clocks": clk, "host_cpu_cores_busy": cpu_s / wall,
                        "n_down_mean": float(np.mean([r.result.n_down for r in res]))}
+            if keep_results:
+                out[ph]["results"] = [(sids.index(r.stream_id), r.cookie, np.array(r.result.x.pos[:]),
+                                       np.array(r.result.x.rot[:]).reshape(3, 3), r.result.evicted,
+                                       r.result.map_size) for r in res]
             if ph == "device":
                 del dev
     finally:
@@ -630,6 +639,278 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
         dist.destroy_process_group()
 
 
+CORRIDOR_NAME = ("long-horizon stress: {s} independent streams, each a 1 km corridor (walls, floor, ceiling, "
+                 "pillars; its own seed and trajectory) seen by a spinning 32-beam LiDAR, 100k rays/scan, 10 Hz, "
+                 "{k} mapping scans per stream, LRU capacity {cap} voxels per stream")
+
+
+def main_corridor(args, rank, ws, barrier, allmax, dist):
+    """configs[4]-style long-horizon stress: many corridor streams served
+    with the LRU cap in force; throughput, latency, eviction counts, and the
+    drift of stream 0 against the oracle and against the ground truth."""
+    from voxelmapplus_fastlio2_gb300 import abi, synth
+    from voxelmapplus_fastlio2_gb300 import build as vbuild
+    cap = args.map_capacity or 8000
+    W, K = args.warmup, args.steps
+    cfg = abi.default_config(scan_resolution=0.2, map_capacity=cap, max_scan_points=100000 + 64)
+    streams = [(synth.KIND_CORRIDOR, 100000, cfg, 0x5EED0000 + 1000 * rank + 64 + s) for s in range(args.streams)]
+    name = CORRIDOR_NAME.format(s=args.streams, k=K, cap=cap)
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        pkgs = list(ex.map(lambda st: make_packages(st[0], st[1], st[3], 2 + W + K), streams))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        v, wall = run_cpu_served(streams, pkgs, W, K, threads, list(range(len(streams))))
+        print(json.dumps({"metric": METRIC, "value": v, "unit": "scans/s", "impl": "reference", "n_gpus": args.gpus,
+                          "steps": K, "warmup": W, "ms_per_step": 1e3 / v, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                          "config": {"workload": name},
+                          "cpu_baseline": {"value": v, "unit": "scans/s", "cores": threads, "kind": "port",
+                                           "sample": f"{K} mapping scans of each of {len(streams)} streams, one "
+                                                     "single-threaded oracle per stream"},
+                          "e2e": {"value": v, "unit": "scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    vbuild.build_all()
+    workers = args.workers or min(32, len(streams))
+    served = run_served(args, streams, pkgs, workers, ["device"], barrier, keep_results=True)
+    dv = served["device"]
+    value = aggregate_value(ws, dv["scans"], dv["wall_s"], allmax)
+    # stream 0 against the oracle (same packages) and the ground truth
+    import oracle
+    res0 = sorted([r for r in dv["results"] if r[0] == 0], key=lambda r: r[1])
+    o = oracle.Oracle(cfg)
+    seq = synth.Sequence(synth.KIND_CORRIDOR, seed=streams[0][3], points_per_scan=100000)
+    d_oracle, d_truth_g, d_truth_o, p_first = [], [], [], None
+    ro = None
+    for k, pk in enumerate(pkgs[0]):
+        ro = o.process(pk)
+        if k < 2 + W:
+            continue
+        r = res0[k - 2 - W]
+        _, pg = seq.pose(pk.t_end)
+        if p_first is None:
+            p_first = pg - np.array(ro.x.pos[:])
+        d_oracle.append((float(np.linalg.norm(r[2] - np.array(ro.x.pos[:]))),
+                         float(np.arccos(np.clip((np.trace(r[3].T @ np.array(ro.x.rot[:]).reshape(3, 3)) - 1) / 2,
+                                                 -1, 1)))))
+        d_truth_g.append(float(np.linalg.norm(r[2] - (pg - p_first))))
+        d_truth_o.append(float(np.linalg.norm(np.array(ro.x.pos[:]) - (pg - p_first))))
+    evicted = int(sum(r[4] for r in dv["results"]))
+    line = {"metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * allmax(dv["wall_s"]) / dv["scans"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": name, "streams_per_gpu": args.streams, "map_capacity": cap,
+                       "scan_resolution": 0.2, "voxel_size": 0.5,
+                       "capacity_note": "a 1 km corridor holds ~1e5 surface voxels at 0.5 m, so a 20 M cap never "
+                                        "evicts; the cap is set below the visible voxel set to keep the LRU "
+                                        "eviction path busy"},
+            "latency_ms": dv["latency_ms"], "service_ms": dv["service_ms"],
+            "evicted_voxels_total": evicted, "evicted_per_scan": evicted / max(1, dv["scans"]),
+            "map_size_end_stream0": int(res0[-1][5]) if res0 else None,
+            "stream0_vs_oracle": {"pos_m_max": max(d[0] for d in d_oracle), "rot_rad_max": max(d[1] for d in d_oracle),
+                                  "scans": len(d_oracle)},
+            "stream0_drift_vs_truth_m": {"gpu_end": d_truth_g[-1], "gpu_max": max(d_truth_g),
+                                         "oracle_end": d_truth_o[-1], "oracle_max": max(d_truth_o)},
+            "clocks": dv["clocks"], "gpu_launches": dv["launches"]}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+PLANEFIT_METRIC = "voxels/s: batched plane fit (updatePlane over every voxel), FP32 compensated vs FP32 vs FP64"
+PLANEFIT_NAME = ("batched plane fit + precision study: {v} voxels of a 0.5 m grid over +-100 x +-100 x +-10 m, "
+                 "points/voxel lognormal (median 40, sigma 1) clipped to [5, 4000], 1 cm normal noise, "
+                 "10% isotropic voxels")
+
+
+def planefit_bytes(off, rec):
+    """Algorithmic bytes per launch of the three fit kernels and of the whole
+    call: point data read once per pass that needs it (12 B xyz in the sums,
+    36 B xyz + covariance in the plane terms), offsets, parked sums / factors
+    and the 296 B record."""
+    counts = np.diff(off)
+    plane = (rec["flags"] & 2) != 0
+    V, N = len(counts), int(off[-1])
+    Np = int(counts[plane].sum())
+    Vp = int(plane.sum())
+    return {"sums": 12.0 * N + (8 + 72) * V, "eig": (8 + 72 + 296) * V, "terms": 36.0 * Np + (8 + 4 + 120 + 168) * Vp,
+            "call": 36.0 * N + (8 + 296) * V}
+
+
+def main_planefit(args, rank, ws, barrier, allmax, dist):
+    """configs[2]-style batched plane fitting: value = voxels/s of the chosen
+    mode with the batch resident in HBM; e2e = the host-buffer call
+    (vmp_fit_planes) with the copies inside; precision of all three modes
+    against the oracle (FP64, the reference's sequential arithmetic)."""
+    from voxelmapplus_fastlio2_gb300 import abi, fit
+    import oracle
+    modes = {"fp64": fit.FP64, "fp32": fit.FP32, "fp32c": fit.FP32C}
+    xyz, cov, off = fit.synth_voxels(args.voxels, seed=0x5EED0000 + rank)
+    V, N = len(off) - 1, xyz.shape[1]
+    name = PLANEFIT_NAME.format(v=V)
+    olib = oracle.load()
+    threads = os.cpu_count() or 1
+
+    def oracle_fit(lo, hi, nthreads):
+        o = off[lo:hi + 1] - off[lo]
+        px = np.ascontiguousarray(xyz[:, off[lo]:off[hi]])
+        pc = np.ascontiguousarray(cov[:, off[lo]:off[hi]])
+        out = np.zeros(hi - lo, dtype=abi.fit_rec_dtype())
+        olib.orc_fit_planes(px.ctypes.data_as(C.POINTER(C.c_float)), pc.ctypes.data_as(C.POINTER(C.c_float)),
+                            o.ctypes.data_as(C.POINTER(C.c_longlong)), hi - lo, px.shape[1], 10, 0.01,
+                            out.ctypes.data_as(C.POINTER(abi.vmp_fit_rec)), nthreads)
+        return out
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sample = min(V, 50_000)
+        ts = []
+        for i in range(args.warmup + args.steps):
+            lo = (i * sample) % max(1, V - sample + 1)
+            t0 = time.perf_counter()
+            oracle_fit(lo, lo + sample, threads)
+            if i >= args.warmup:
+                ts.append(time.perf_counter() - t0)
+        v = sample * len(ts) / sum(ts)
+        print(json.dumps({"metric": PLANEFIT_METRIC, "value": v, "unit": "voxels/s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * sum(ts) / len(ts), "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                          "config": {"workload": name, "voxels": V, "points": N},
+                          "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": threads, "kind": "port",
+                                           "sample": f"{sample} consecutive voxels per step, CPU restatement "
+                                                     f"of addPoint + updatePlane on {threads} OpenMP threads"},
+                          "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    from voxelmapplus_fastlio2_gb300 import build as vbuild
+    from voxelmapplus_fastlio2_gb300._lib import load
+    vbuild.build_all()
+    import torch
+    lib = load()
+    stream = torch.cuda.Stream()
+    d_xyz = torch.from_numpy(xyz).cuda()
+    d_cov = torch.from_numpy(cov).cuda()
+    d_off = torch.from_numpy(off).cuda()
+    rs = abi.fit_rec_dtype().itemsize
+    d_out = torch.zeros(V * rs, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+
+    def run(mode):
+        fit.fit_planes_device(d_xyz.data_ptr(), d_cov.data_ptr(), d_off.data_ptr(), V, N, d_out.data_ptr(),
+                              mode=mode, cuda_stream=stream.cuda_stream)
+
+    # precision of every mode against the oracle on the whole batch
+    t0 = time.perf_counter()
+    ref = oracle_fit(0, V, threads)
+    t_oracle = time.perf_counter() - t0
+    precision, per_mode = {}, {}
+    for mname, mode in modes.items():
+        run(mode)
+        stream.synchronize()
+        rec = d_out.cpu().numpy().view(abi.fit_rec_dtype()).reshape(-1)
+        precision[mname] = fit.compare(rec, ref)
+    bytes_ = planefit_bytes(off, ref)
+    mode = modes[args.fit_mode]
+    for mname, m in modes.items():  # short timing of every mode
+        for _ in range(2):
+            run(m)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 10 if mname == "fp64" else 30
+        a.record(stream)
+        for _ in range(reps):
+            run(m)
+        b.record(stream)
+        b.synchronize()
+        per_mode[mname] = {"voxels_per_s": V * reps / (a.elapsed_time(b) * 1e-3),
+                           "ms_per_call": a.elapsed_time(b) / reps}
+    for _ in range(args.warmup):
+        run(mode)
+    stream.synchronize()
+    barrier()
+    l0 = lib.vmp_launch_count()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    evs = []
+    for _ in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run(mode)
+        b.record(stream)
+        evs.append((a, b))
+    stream.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = lib.vmp_launch_count() - l0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    t_step = allmax(sum(step_ms) / 1e3)
+    value = ws * V * args.steps / t_step
+    # per-kernel device time (profiled calls)
+    lib.vmp_fit_profile(1)
+    P = 10
+    for _ in range(P):
+        run(mode)
+    ms = (C.c_double * 3)()
+    calls = C.c_longlong()
+    lib.vmp_fit_profile_read(ms, C.byref(calls))
+    lib.vmp_fit_profile(0)
+    kms = {k: ms[i] / max(1, calls.value) for i, k in enumerate(["sums", "eig", "terms"])}
+    dom = max(kms, key=kms.get)
+    peak, peak_src = load_peaks()
+    achieved = bytes_[dom] / (kms[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_fit_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": load_traffic("fit_" + dom + "_" + args.fit_mode, 1.0),
+            "algorithmic_bytes_per_launch": bytes_[dom], "avg_launch_ms": kms[dom], "peak_source": peak_src,
+            "per_kernel_ms": kms,
+            "call_achieved_gbs": bytes_["call"] / (sum(step_ms) / len(step_ms) * 1e-3) / 1e9}
+    # e2e: the host-buffer entry point from pinned memory, copies inside
+    h_xyz = torch.from_numpy(xyz).pin_memory()
+    h_cov = torch.from_numpy(cov).pin_memory()
+    h_off = torch.from_numpy(off).pin_memory()
+    h_out = torch.zeros(V * rs, dtype=torch.uint8).pin_memory()
+    p = fit.params(mode)
+    walls = []
+    E = max(3, min(20, args.steps // 10))
+    for i in range(1 + E):
+        t0 = time.perf_counter()
+        rc = lib.vmp_fit_planes(C.c_void_p(h_xyz.data_ptr()), C.c_void_p(h_cov.data_ptr()),
+                                C.c_void_p(h_off.data_ptr()), V, N, C.byref(p), C.c_void_p(h_out.data_ptr()))
+        if rc != 0:
+            raise RuntimeError(f"vmp_fit_planes: status {rc}")
+        if i > 0:
+            walls.append(time.perf_counter() - t0)
+    e2e_v = ws * V * len(walls) / allmax(sum(walls))
+    # CPU baseline: the oracle on the whole batch, all host threads (it is
+    # also the precision reference above), and one thread on a slice
+    t1 = time.perf_counter()
+    n1 = min(V, 20_000)
+    oracle_fit(0, n1, 1)
+    t1 = time.perf_counter() - t1
+    line = {"metric": PLANEFIT_METRIC, "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32", "fp32c": "f32"}[args.fit_mode],
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": name, "voxels": V, "points": N, "mode": args.fit_mode,
+                       "update_point_thresh": 10, "plane_thresh": 0.01,
+                       "l2": f"inputs {(36 * N) / 1e9:.2f} GB > L2 (129 MB): no flush"},
+            "e2e": {"value": e2e_v, "unit": "voxels/s", "h2d_bytes_per_step": int(36 * N + 8 * (V + 1)),
+                    "d2h_bytes_per_step": int(rs * V)},
+            "roofline": roof, "clocks": clk, "gpu_launches": int(launches), "modes": per_mode,
+            "precision_vs_oracle": precision,
+            "cpu_baseline": {"value": V / t_oracle, "unit": "voxels/s", "cores": threads, "kind": "port",
+                             "sample": f"all {V} voxels, CPU restatement of addPoint + updatePlane on {threads} "
+                                       f"OpenMP threads; one thread: {n1 / t1:.0f} voxels/s on {n1} voxels"}}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     from voxelmapplus_fastlio2_gb300 import build as vbuild
@@ -640,6 +921,10 @@ def main():
     rank, ws, barrier, allmax, dist = dist_setup(args)
     if args.workload == "serve":
         return main_serve(args, rank, ws, barrier, allmax, dist)
+    if args.workload == "planefit":
+        return main_planefit(args, rank, ws, barrier, allmax, dist)
+    if args.workload == "corridor":
+        return main_corridor(args, rank, ws, barrier, allmax, dist)
     kind, pts, cfg, seed, wname = workload(args, rank)
     n_init = 2  # IMU_INIT + MAP_INIT packages
     if args.impl == "reference":

@@ -23,6 +23,8 @@
  *   vmp_ieskf_update             kf::IESKF::update             src/map_builder/ieskf.cpp:125-156
  *   vmp_get_state / vmp_set_state kf::IESKF::x(), P(), change_x, change_P  src/map_builder/ieskf.h:86-94
  *   vmp_map_export / vmp_map_import  direct featmap access by the node  src/utils.cpp:154-208
+ *   vmp_fit_planes               lio::VoxelGrid::updatePlane over all voxels, as VoxelMap::build
+ *                                fits them  src/map_builder/voxel_map.cpp:97-136, 200-230
  *
  * Conventions: all matrices are row-major double.  Points are float as in
  * pcl::PointXYZINormal; the per-point time is the field the reference keeps in
@@ -229,6 +231,66 @@ vmp_status vmp_undistort(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* im
 /* pcl::VoxelGrid leaf-centroid downsample at the given leaf size. */
 vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double leaf,
                           vmp_point* out, int* n_out);
+/* ---- input decode and output clouds (the steps either side of the path) ----
+ * livox_ros_driver2 CustomPoint (CustomPoint.msg) in the field order of the
+ * message and of its generated C++ struct (20 bytes with the tail padding),
+ * so a CustomMsg's points array can be passed as it is. */
+typedef struct vmp_livox_point {
+    uint32_t offset_time; /* ns after the message time */
+    float x, y, z;        /* m, LiDAR frame */
+    uint8_t reflectivity;
+    uint8_t tag;
+    uint8_t line;
+    uint8_t pad;
+} vmp_livox_point;
+/* livox2pcl (src/utils.cpp:3-28) on the device: keeps the points with
+ * line < 4 and tag bits 4-5 equal to 0 or 1, of those every filter_num-th
+ * (the first included), of those the ones with
+ * range_min^2 < x^2 + y^2 + z^2 < range_max^2 (the sum in float, the test in
+ * double); t_ms = offset_time / 1e6 (float), intensity = reflectivity.  The
+ * decoded cloud stays in the stream's device scan buffer for
+ * vmp_process_decoded.  out / intensity (host, may be NULL) receive the n_out
+ * kept points; last_t_ms (may be NULL) the last kept point's t_ms, from which
+ * the node's syncPackage forms the package end time (lio_node.cpp:142-146).
+ * n <= max_scan_points. */
+vmp_status vmp_livox_decode(vmp_stream_t s, const vmp_livox_point* pts, int n, int filter_num, double range_min,
+                            double range_max, vmp_point* out, float* intensity, int* n_out, float* last_t_ms);
+/* vmp_process on the cloud of the last vmp_livox_decode, without uploading it
+ * again (VMP_ERR_STATE when no decoded cloud is pending). */
+vmp_status vmp_process_decoded(vmp_stream_t s, double t_start, double t_end, const vmp_imu* imus, int n_imu,
+                               vmp_result* out);
+/* lidarToBody (frame 0) / lidarToWorld (frame 1) (lio_builder.cpp:155-173)
+ * of the last processed scan's undistorted, time-sorted cloud -- the node's
+ * sync_pack.cloud after process -- under the state after that scan's update,
+ * as a float 4x4 transform in pcl::transformPointCloud's operation order.
+ * out (host, max points; x y z t_ms) and intensity (host, may be NULL;
+ * reflectivity of decoded scans, 0 otherwise); *n_out = points in the cloud
+ * (0 after an IMU-initialisation package). */
+vmp_status vmp_output_cloud(vmp_stream_t s, int frame, vmp_point* out, float* intensity, int max, int* n_out);
+/* The same into device buffers the caller owns; only enqueues the work on
+ * the stream's CUDA stream.  *n_out (host) = points written. */
+vmp_status vmp_output_cloud_device(vmp_stream_t s, int frame, vmp_point* d_out, float* d_intensity, int max,
+                                   int* n_out);
+
+/* ---- voxel-map export for visualisation ----
+ * What voxel2MarkerArray (src/utils.cpp:154-208) reads from the map for one
+ * plane marker.  The reference walks the LRU list from its front (most
+ * recently touched) and emits the frozen planes (is_plane && !update_enable),
+ * at most max_capacity of them. */
+typedef struct vmp_plane_marker {
+    double center[3];      /* VoxelGrid::center (the mean at the last refit) */
+    double norm[3];        /* plane normal */
+    double orientation[4]; /* w x y z: Quaterniond::FromTwoVectors((0, 0, 1), norm) (calcVectQuation) */
+    double trace;          /* trace of the plane covariance's top-left 3x3 */
+    uint8_t rgb[3];        /* mapJet((min(trace, 0.25) / 0.25)^0.2, 0, 1) */
+    uint8_t merged;        /* 1: CUBE marker, 0: CYLINDER */
+    int32_t pad;
+} vmp_plane_marker;
+/* The first min(planes, max) frozen plane voxels in LRU order, selected,
+ * sorted and formed on the device.  out (host) holds max markers; *n_out =
+ * markers written. */
+vmp_status vmp_map_planes(vmp_stream_t s, vmp_plane_marker* out, int max, int* n_out);
+
 /* The same leaf-centroid downsample for callers that cannot allocate device
  * memory (no counterpart in the reference): a real-time sensor thread that
  * must not call cudaMalloc/cudaFree, or a host framework whose own allocator
@@ -243,6 +305,61 @@ vmp_status vmp_downsample(vmp_stream_t s, const vmp_point* pts, int n, double le
  * NULL (default stream); the call returns after that stream finished. */
 vmp_status vmp_downsample_noalloc(const vmp_point* d_in, int n, double leaf, vmp_point* d_out, int* n_out,
                                   void* cuda_stream);
+
+/* ---- batched plane fitting ----
+ * VoxelGrid::updatePlane (src/map_builder/voxel_map.cpp:97-136) over all
+ * points of many voxels at once, as VoxelMap::build fits every voxel after
+ * adding its points (voxel_map.cpp:200-230): mean, point covariance
+ * C = ppt / n - mean mean^T, ascending eigenvalues, plane test
+ * evals[0] <= plane_thresh, and for a plane the normal (sign flipped so that
+ * -mean . normal >= 0) and the 6x6 plane covariance sum_p J cov_p J^T with
+ * J = [evecs F_p; I / n].  Voxels with fewer than update_point_thresh points
+ * are not fitted (only mean and n are set), as updatePlane returns early.
+ * A non-plane gets a zero normal and plane covariance (updatePlane returns
+ * before forming them).
+ * Arithmetic modes: */
+enum {
+    VMP_FIT_FP64 = 0,  /* the reference's FP64 arithmetic (parallel sums) */
+    VMP_FIT_FP32 = 1,  /* plain FP32 throughout, world coordinates */
+    VMP_FIT_FP32C = 2  /* FP32 with compensated covariance sums: coordinates
+                          relative to the voxel's first point (an exact
+                          float subtraction) and TwoSum-compensated sums of
+                          the coordinates and their products */
+};
+enum { VMP_FIT_FITTED = 1, VMP_FIT_PLANE = 2, VMP_FIT_FLIPPED = 4 };
+typedef struct vmp_fit_params {
+    int mode;                 /* VMP_FIT_* */
+    int update_point_thresh;  /* fits voxels with n >= this (>= 1) */
+    double plane_thresh;      /* plane test on the smallest eigenvalue */
+} vmp_fit_params;
+/* One fitted voxel (296 bytes). */
+typedef struct vmp_fit_rec {
+    double mean[3];
+    double cov[6];        /* C, upper triangle: xx xy xz yy yz zz */
+    double evals[3];      /* ascending */
+    double norm[3];       /* plane normal after the sign flip (VMP_FIT_FLIPPED: it was negated) */
+    double plane_cov[21]; /* 6x6 plane covariance, upper triangle row by row */
+    int n;                /* points of the voxel */
+    int flags;            /* VMP_FIT_FITTED | VMP_FIT_PLANE | VMP_FIT_FLIPPED */
+} vmp_fit_rec;
+/* Device-buffer form (allocation-free; cuda_stream may be NULL).  Points are
+ * structure-of-arrays floats: xyz = 3 arrays of n_pts (x, then y, then z),
+ * cov = 6 arrays of n_pts (xx xy xz yy yz zz of each point's covariance);
+ * voxel v owns points offsets[v] .. offsets[v + 1] - 1 (offsets ascending,
+ * offsets[0] = 0, offsets[n_vox] = n_pts).  out holds n_vox records.  The
+ * call only enqueues work on cuda_stream. */
+vmp_status vmp_fit_planes_device(const float* xyz, const float* cov, const long long* offsets, int n_vox,
+                                 long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out,
+                                 void* cuda_stream);
+/* Host-buffer form: copies in, fits, copies the records out and returns
+ * after they arrived (allocates and frees device memory per call). */
+vmp_status vmp_fit_planes(const float* xyz, const float* cov, const long long* offsets, int n_vox,
+                          long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out);
+/* Measurement hook: while on, every fit call records CUDA events around its
+ * three kernels (sums, eigen, plane terms), waits for them and adds up their
+ * device time.  vmp_fit_profile resets the totals. */
+vmp_status vmp_fit_profile(int on);
+vmp_status vmp_fit_profile_read(double* ms /* 3 */, long long* calls);
 
 /* ---- measurement hooks (no reference counterpart) ----
  * Per-phase device time of vmp_process, from CUDA events recorded on the

@@ -58,6 +58,15 @@ def load():
     lib.orc_ieskf_update.argtypes = [vp, P(C.c_float), C.c_int, P(C.c_int), P(C.c_int)]
     lib.orc_undistort.argtypes = [vp, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, P(abi.vmp_point)]
     lib.orc_downsample.argtypes = [P(abi.vmp_point), C.c_int, d, P(abi.vmp_point)]
+    lib.orc_livox_decode.argtypes = [P(abi.vmp_livox_point), C.c_int, C.c_int, d, d, P(abi.vmp_point), P(C.c_float)]
+    lib.orc_livox_decode.restype = C.c_int
+    lib.orc_set_intensity.argtypes = [vp, P(C.c_float), C.c_int]
+    lib.orc_output_cloud.argtypes = [vp, C.c_int, P(abi.vmp_point), P(C.c_float), C.c_int]
+    lib.orc_output_cloud.restype = C.c_int
+    lib.orc_map_planes.argtypes = [vp, P(abi.vmp_plane_marker), C.c_int]
+    lib.orc_map_planes.restype = C.c_int
+    lib.orc_fit_planes.argtypes = [P(C.c_float), P(C.c_float), P(C.c_longlong), C.c_int, C.c_longlong, C.c_int, d,
+                                   P(abi.vmp_fit_rec), C.c_int]
     lib.orc_downsample.restype = C.c_int
     lib.orc_calc_body_cov.argtypes = [P(d), C.c_int, d, d, P(d), P(d)]
     lib.orc_last_cloud.argtypes = [vp, C.c_int, P(abi.vmp_point), C.c_int]
@@ -91,3 +100,38 @@ class Oracle:
         scan = pkg.scan()
         self.lib.orc_process(self.h, C.byref(scan), pkg.imus, pkg.n_imu, C.byref(res))
         return res
+
+    def process_points(self, pts4, t_start, t_end, imus, n_imu, intensity=None):
+        """process() on a (n, 4) float32 cloud (x y z t_ms), optional intensities."""
+        import numpy as np
+        pts4 = np.ascontiguousarray(pts4, dtype=np.float32)
+        if intensity is not None:
+            inten = np.ascontiguousarray(intensity, dtype=np.float32)
+            self.lib.orc_set_intensity(self.h, inten.ctypes.data_as(C.POINTER(C.c_float)), len(inten))
+        scan = abi.vmp_scan(pts4.ctypes.data_as(C.POINTER(abi.vmp_point)), len(pts4), t_start, t_end)
+        res = abi.vmp_result()
+        self.lib.orc_process(self.h, C.byref(scan), imus, n_imu, C.byref(res))
+        return res
+
+    def output_cloud(self, frame):
+        import numpy as np
+        n = self.lib.orc_output_cloud(self.h, frame, None, None, 0)
+        out = np.zeros((max(1, n), 4), dtype=np.float32)
+        inten = np.zeros(max(1, n), dtype=np.float32)
+        self.lib.orc_output_cloud(self.h, frame, out.ctypes.data_as(C.POINTER(abi.vmp_point)),
+                                  inten.ctypes.data_as(C.POINTER(C.c_float)), n)
+        return out[:n], inten[:n]
+
+
+def livox_decode(livox, filter_num=1, range_min=0.5, range_max=20.0):
+    """livox2pcl restated on the CPU: (points (m, 4) float32, intensity (m,))."""
+    import numpy as np
+    lib = load()
+    livox = np.ascontiguousarray(livox, dtype=abi.livox_dtype())
+    n = len(livox)
+    out = np.zeros((max(1, n), 4), dtype=np.float32)
+    inten = np.zeros(max(1, n), dtype=np.float32)
+    m = lib.orc_livox_decode(livox.ctypes.data_as(C.POINTER(abi.vmp_livox_point)), n, filter_num, range_min,
+                             range_max, out.ctypes.data_as(C.POINTER(abi.vmp_point)),
+                             inten.ctypes.data_as(C.POINTER(C.c_float)))
+    return out[:m], inten[:m]

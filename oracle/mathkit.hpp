@@ -369,4 +369,29 @@ inline Mat<N, N> inverse(const Mat<N, N>& A) {
     return inv;
 }
 
+// Eigen's Quaternion::setFromTwoVectors (rotation taking a onto b), output
+// w x y z: c = a.b of the normalised vectors; axis = a x b, s = sqrt(2 (1 + c)),
+// q = (s / 2, axis / s).  For c < -1 + 1e-12 (antiparallel) Eigen takes an
+// axis from an SVD; this restatement takes the unit vector of a x e_x (or
+// a x e_y when a is along x), rotated by pi.
+inline void quatFromTwoVectors(const V3& a0, const V3& b0, double q[4]) {
+    const V3 v0 = a0 / std::sqrt(dot(a0, a0));
+    const V3 v1 = b0 / std::sqrt(dot(b0, b0));
+    const double c = dot(v1, v0);
+    if (c < -1.0 + 1e-12) {
+        V3 e = std::fabs(v0[0]) < 0.9 ? v3(1, 0, 0) : v3(0, 1, 0);
+        V3 ax = cross(v0, e);
+        ax = ax / std::sqrt(dot(ax, ax));
+        q[0] = 0.0; q[1] = ax[0]; q[2] = ax[1]; q[3] = ax[2];
+        return;
+    }
+    const V3 axis = cross(v0, v1);
+    const double s = std::sqrt((1.0 + c) * 2.0);
+    const double invs = 1.0 / s;
+    q[0] = s * 0.5;
+    q[1] = axis[0] * invs;
+    q[2] = axis[1] * invs;
+    q[3] = axis[2] * invs;
+}
+
 }  // namespace orc

@@ -669,10 +669,15 @@ struct LIOBuilder {  // lio_builder.h:56-83
         return r_wl * cov_l * T(r_wl) + cm * kf.P_.block<3, 3>(3, 3) * T(cm) + kf.P_.block<3, 3>(0, 0);
     }
 
+    std::vector<float> next_intensity;  // intensities of the next package's points (else 0)
+
     void process(const vmp_scan& scan, const std::vector<IMUData>& imus) {  // lio_builder.cpp:175-248
         cloud.resize(scan.n);
+        const bool has_int = (int)next_intensity.size() == scan.n;
         for (int i = 0; i < scan.n; ++i)
-            cloud[i] = CPoint{scan.points[i].x, scan.points[i].y, scan.points[i].z, 0.0f, scan.points[i].t_ms};
+            cloud[i] = CPoint{scan.points[i].x, scan.points[i].y, scan.points[i].z,
+                              has_int ? next_intensity[i] : 0.0f, scan.points[i].t_ms};
+        next_intensity.clear();
         if (status == VMP_IMU_INIT) {
             if (initializeImu(imus)) {
                 status = VMP_MAP_INIT;
@@ -1050,6 +1055,142 @@ void orc_eig_sym3(const double* A, double* evals, double* evecs) {
     V3 e; M3 v; eigSym3(a, e, v);
     for (int i = 0; i < 3; ++i) evals[i] = e[i];
     for (int i = 0; i < 9; ++i) evecs[i] = v[i];
+}
+
+// Batched plane fit (vmp_fit_planes): per voxel, VoxelGrid::addPoint for each
+// of its points in order, then one updatePlane -- what VoxelMap::build does
+// for a voxel (voxel_map.cpp:200-230, 29-40, 97-136).  FP64; voxels are
+// independent, so they are spread over `threads` OpenMP threads.
+void orc_fit_planes(const float* xyz, const float* cov, const long long* off, int n_vox, long long n_pts,
+                    int update_point_thresh, double plane_thresh, vmp_fit_rec* out, int threads) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads < 1 ? 1 : threads)
+    for (int v = 0; v < n_vox; ++v) {
+        const long long p0 = off[v], p1 = off[v + 1];
+        const int n = (int)(p1 - p0);
+        VoxelGrid g(n > 0 ? n : 1, update_point_thresh, plane_thresh, VoxelKey{0, 0, 0}, nullptr, 0);
+        for (long long i = p0; i < p1; ++i) {
+            PointWithCov pv;
+            pv.point = v3(xyz[i], xyz[n_pts + i], xyz[2 * n_pts + i]);
+            const double c[6] = {cov[i], cov[n_pts + i], cov[2 * n_pts + i], cov[3 * n_pts + i],
+                                 cov[4 * n_pts + i], cov[5 * n_pts + i]};
+            pv.cov(0, 0) = c[0]; pv.cov(0, 1) = c[1]; pv.cov(0, 2) = c[2];
+            pv.cov(1, 0) = c[1]; pv.cov(1, 1) = c[3]; pv.cov(1, 2) = c[4];
+            pv.cov(2, 0) = c[2]; pv.cov(2, 1) = c[4]; pv.cov(2, 2) = c[5];
+            g.addPoint(pv);
+        }
+        g.updatePlane();
+        vmp_fit_rec& r = out[v];
+        std::memset(&r, 0, sizeof(r));
+        r.n = n;
+        for (int k = 0; k < 3; ++k) r.mean[k] = g.plane.mean[k];
+        if (!g.is_init) continue;
+        // C and its eigen decomposition as updatePlane formed them
+        M3 C = g.plane.ppt / static_cast<double>(g.plane.n) - g.plane.mean * T(g.plane.mean);
+        V3 ev; M3 E;
+        eigSym3(C, ev, E);
+        r.cov[0] = C(0, 0); r.cov[1] = C(0, 1); r.cov[2] = C(0, 2);
+        r.cov[3] = C(1, 1); r.cov[4] = C(1, 2); r.cov[5] = C(2, 2);
+        for (int k = 0; k < 3; ++k) r.evals[k] = ev[k];
+        r.flags = VMP_FIT_FITTED;
+        if (!g.is_plane) continue;
+        r.flags |= VMP_FIT_PLANE;
+        if (g.plane.norm[0] != E(0, 0) || g.plane.norm[1] != E(1, 0) || g.plane.norm[2] != E(2, 0))
+            r.flags |= VMP_FIT_FLIPPED;
+        for (int k = 0; k < 3; ++k) r.norm[k] = g.plane.norm[k];
+        int e = 0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) r.plane_cov[e++] = g.plane.cov(i, j);
+    }
+}
+
+// livox2pcl (src/utils.cpp:3-28): line / tag filter, 1-in-filter_num
+// decimation of the passing points, range gate with |p|^2 summed in float.
+int orc_livox_decode(const vmp_livox_point* in, int n, int filter_num, double range_min, double range_max,
+                     vmp_point* out, float* intensity) {
+    unsigned valid_num = 0;
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+        const vmp_livox_point& q = in[i];
+        if ((q.line < 4) && ((q.tag & 0x30) == 0x10 || (q.tag & 0x30) == 0x00)) {
+            if ((valid_num++) % (unsigned)filter_num != 0) continue;
+            const float x = q.x, y = q.y, z = q.z;
+            const float t = q.offset_time / float(1000000);
+            const double sq_range = x * x + y * y + z * z;
+            if (sq_range > (range_min * range_min) && sq_range < range_max * range_max) {
+                out[m] = vmp_point{x, y, z, t};
+                if (intensity) intensity[m] = q.reflectivity;
+                ++m;
+            }
+        }
+    }
+    return m;
+}
+
+// Intensities of the points of the next orc_process package (n must match).
+void orc_set_intensity(void* h, const float* v, int n) {
+    ((LIOBuilder*)h)->next_intensity.assign(v, v + n);
+}
+
+// lidarToBody (frame 0) / lidarToWorld (frame 1) of the package cloud after
+// process (lio_builder.cpp:155-173).
+int orc_output_cloud(void* h, int frame, vmp_point* out, float* intensity, int max) {
+    LIOBuilder* b = (LIOBuilder*)h;
+    float R[9], t[3];
+    if (frame == 0) {
+        for (int i = 0; i < 9; ++i) R[i] = (float)b->kf.x_.rot_ext[i];
+        for (int i = 0; i < 3; ++i) t[i] = (float)b->kf.x_.pos_ext[i];
+    } else {
+        b->worldTransform(R, t);
+    }
+    const int n = (int)b->cloud.size();
+    for (int i = 0; i < n && i < max; ++i) {
+        float w[3];
+        transformFloat(R, t, b->cloud[i], w);
+        out[i] = vmp_point{w[0], w[1], w[2], b->cloud[i].t};
+        if (intensity) intensity[i] = b->cloud[i].intensity;
+    }
+    return n;
+}
+
+// voxel2MarkerArray (src/utils.cpp:154-208) without the ROS message: the
+// frozen planes in LRU order, their trace colour (mapJet, utils.cpp:78-128)
+// and the marker orientation (calcVectQuation -> Quaterniond::FromTwoVectors,
+// utils.cpp:144-152; the antiparallel case picks the x axis, see mathkit).
+static void mapJetRestated(double v, double vmin, double vmax, uint8_t& r, uint8_t& g, uint8_t& b) {
+    if (v < vmin) v = vmin;
+    if (v > vmax) v = vmax;
+    double dr, dg, db;
+    if (v < 0.1242) { db = 0.504 + ((1. - 0.504) / 0.1242) * v; dg = dr = 0.; }
+    else if (v < 0.3747) { db = 1.; dr = 0.; dg = (v - 0.1242) * (1. / (0.3747 - 0.1242)); }
+    else if (v < 0.6253) { db = (0.6253 - v) * (1. / (0.6253 - 0.3747)); dg = 1.; dr = (v - 0.3747) * (1. / (0.6253 - 0.3747)); }
+    else if (v < 0.8758) { db = 0.; dr = 1.; dg = (0.8758 - v) * (1. / (0.8758 - 0.6253)); }
+    else { db = 0.; dg = 0.; dr = 1. - (v - 0.8758) * ((1. - 0.504) / (1. - 0.8758)); }
+    r = (uint8_t)(255 * dr);
+    g = (uint8_t)(255 * dg);
+    b = (uint8_t)(255 * db);
+}
+int orc_map_planes(void* h, vmp_plane_marker* out, int max) {
+    LIOBuilder* b = (LIOBuilder*)h;
+    VoxelMap& m = *b->map;
+    const int size = std::min((int)m.cache.size(), max);
+    int count = 0;
+    for (auto& k : m.cache) {
+        if (count >= size) break;
+        VoxelGrid* g = m.featmap[k].get();
+        if (!g->is_plane || g->update_enable) continue;
+        vmp_plane_marker& o = out[count++];
+        std::memset(&o, 0, sizeof(o));
+        for (int i = 0; i < 3; ++i) { o.center[i] = g->center[i]; o.norm[i] = g->plane.norm[i]; }
+        double trace = (g->plane.cov(0, 0) + g->plane.cov(1, 1)) + g->plane.cov(2, 2);
+        o.trace = trace;
+        if (trace >= 0.25) trace = 0.25;
+        trace = trace * (1.0 / 0.25);
+        trace = std::pow(trace, 0.2);
+        mapJetRestated(trace, 0, 1, o.rgb[0], o.rgb[1], o.rgb[2]);
+        o.merged = g->merged ? 1 : 0;
+        quatFromTwoVectors(v3(0, 0, 1), g->plane.norm, o.orientation);
+    }
+    return count;
 }
 
 }  // extern "C"

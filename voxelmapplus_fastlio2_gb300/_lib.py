@@ -71,6 +71,15 @@ def _declare(lib):
         "vmp_server_stream": ([vp, C.c_int, P(vp)], st),
         "vmp_server_info": ([vp, P(C.c_longlong), P(C.c_int), P(C.c_int), P(C.c_int)], st),
         "vmp_server_last_error": ([vp], C.c_char_p),
+        "vmp_fit_planes": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp], st),
+        "vmp_fit_planes_device": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp, vp], st),
+        "vmp_fit_profile": ([C.c_int], st),
+        "vmp_map_planes": ([vp, vp, C.c_int, P(C.c_int)], st),
+        "vmp_livox_decode": ([vp, vp, C.c_int, C.c_int, d, d, vp, vp, P(C.c_int), P(C.c_float)], st),
+        "vmp_process_decoded": ([vp, d, d, P(abi.vmp_imu), C.c_int, P(abi.vmp_result)], st),
+        "vmp_output_cloud": ([vp, C.c_int, vp, vp, C.c_int, P(C.c_int)], st),
+        "vmp_output_cloud_device": ([vp, C.c_int, vp, vp, C.c_int, P(C.c_int)], st),
+        "vmp_fit_profile_read": ([P(d), P(C.c_longlong)], st),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -50,6 +50,18 @@ class vmp_imu(C.Structure):
     _fields_ = [("t", C.c_double), ("acc", C.c_double * 3), ("gyro", C.c_double * 3)]
 
 
+class vmp_livox_point(C.Structure):
+    """livox_ros_driver2 CustomPoint (20 bytes)."""
+    _fields_ = [("offset_time", C.c_uint32), ("x", C.c_float), ("y", C.c_float), ("z", C.c_float),
+                ("reflectivity", C.c_uint8), ("tag", C.c_uint8), ("line", C.c_uint8), ("pad", C.c_uint8)]
+
+
+def livox_dtype():
+    import numpy as np
+    return np.dtype([("offset_time", "<u4"), ("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("reflectivity", "u1"),
+                     ("tag", "u1"), ("line", "u1"), ("pad", "u1")])
+
+
 class vmp_scan(C.Structure):
     _fields_ = [("points", C.POINTER(vmp_point)), ("n", C.c_int), ("t_start", C.c_double), ("t_end", C.c_double)]
 
@@ -136,3 +148,36 @@ def state_to_dict(x):
         "rot_ext": np.array(x.rot_ext[:]).reshape(3, 3), "pos_ext": np.array(x.pos_ext[:]),
         "vel": np.array(x.vel[:]), "bg": np.array(x.bg[:]), "ba": np.array(x.ba[:]), "g": np.array(x.g[:]),
     }
+
+
+# ---- batched plane fitting (vmp_fit_planes)
+VMP_FIT_FP64, VMP_FIT_FP32, VMP_FIT_FP32C = 0, 1, 2
+FIT_MODE_NAMES = {VMP_FIT_FP64: "fp64", VMP_FIT_FP32: "fp32", VMP_FIT_FP32C: "fp32c"}
+VMP_FIT_FITTED, VMP_FIT_PLANE, VMP_FIT_FLIPPED = 1, 2, 4
+
+
+class vmp_fit_params(C.Structure):
+    _fields_ = [("mode", C.c_int), ("update_point_thresh", C.c_int), ("plane_thresh", C.c_double)]
+
+
+class vmp_fit_rec(C.Structure):
+    _fields_ = [("mean", C.c_double * 3), ("cov", C.c_double * 6), ("evals", C.c_double * 3),
+                ("norm", C.c_double * 3), ("plane_cov", C.c_double * 21), ("n", C.c_int), ("flags", C.c_int)]
+
+
+def fit_rec_dtype():
+    """numpy dtype with the layout of vmp_fit_rec (296 bytes)."""
+    import numpy as np
+    return np.dtype([("mean", "<f8", (3,)), ("cov", "<f8", (6,)), ("evals", "<f8", (3,)), ("norm", "<f8", (3,)),
+                     ("plane_cov", "<f8", (21,)), ("n", "<i4"), ("flags", "<i4")])
+
+
+class vmp_plane_marker(C.Structure):
+    _fields_ = [("center", C.c_double * 3), ("norm", C.c_double * 3), ("orientation", C.c_double * 4),
+                ("trace", C.c_double), ("rgb", C.c_uint8 * 3), ("merged", C.c_uint8), ("pad", C.c_int32)]
+
+
+def plane_marker_dtype():
+    import numpy as np
+    return np.dtype([("center", "<f8", (3,)), ("norm", "<f8", (3,)), ("orientation", "<f8", (4,)), ("trace", "<f8"),
+                     ("rgb", "u1", (3,)), ("merged", "u1"), ("pad", "<i4")])

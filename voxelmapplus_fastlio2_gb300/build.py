@@ -33,6 +33,7 @@ CU_SOURCES = [
     "k_iekf.cu",
     "k_map.cu",
     "k_merge.cu",
+    "k_fit.cu",
     "vmp_noalloc.cu",
     "vmp_server.cu",
 ]

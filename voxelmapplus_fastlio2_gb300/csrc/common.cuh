@@ -493,4 +493,62 @@ __device__ inline double warp_sum(double v) {
     return v;
 }
 
+// Symmetric 3x3 eigen decomposition (cyclic Jacobi), the same operation
+// sequence as the oracle's restatement of Eigen's SelfAdjointEigenSolver
+// (ascending eigenvalues, eigenvectors as columns of evecs, row-major).  T is
+// double on the odometry path; the float instance serves the FP32 plane-fit
+// modes, with a stopping threshold suited to float.
+template <class T> struct EigStop;
+template <> struct EigStop<double> {
+    static __device__ __forceinline__ double tiny() { return 1e-300; }
+    static __device__ __forceinline__ double rel() { return 1e-18; }
+};
+template <> struct EigStop<float> {
+    static __device__ __forceinline__ float tiny() { return 1e-37f; }
+    static __device__ __forceinline__ float rel() { return 1e-12f; }
+};
+template <class T>
+__device__ void eig_sym3(const T* A, T* evals, T* evecs) {
+    T a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) a[i][j] = A[i * 3 + j];
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+        T scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+        if (off == T(0) || off <= EigStop<T>::tiny() || off < EigStop<T>::rel() * scale) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                T apq = a[p][q];
+                if (apq == T(0)) continue;
+                T theta = (a[q][q] - a[p][p]) / (T(2) * apq);
+                T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+                T c = T(1) / sqrt(t * t + T(1)), s = t * c;
+                for (int k = 0; k < 3; ++k) {
+                    T akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    T apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    T vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int idx[3] = {0, 1, 2};
+    T d[3] = {a[0][0], a[1][1], a[2][2]};
+    for (int i = 0; i < 3; ++i)
+        for (int j = i + 1; j < 3; ++j)
+            if (d[idx[j]] < d[idx[i]]) { int t = idx[i]; idx[i] = idx[j]; idx[j] = t; }
+    for (int c = 0; c < 3; ++c) {
+        evals[c] = d[idx[c]];
+        for (int r = 0; r < 3; ++r) evecs[r * 3 + c] = v[r][idx[c]];
+    }
+}
+
 }  // namespace vmp

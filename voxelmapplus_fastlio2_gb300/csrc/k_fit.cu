@@ -1,0 +1,554 @@
+// Batched plane fitting (vmp_fit_planes): VoxelGrid::updatePlane
+// (voxel_map.cpp:97-136) over every point of many voxels at once, as
+// VoxelMap::build fits each voxel after adding all its points
+// (voxel_map.cpp:200-230), in three arithmetic modes:
+//   FP64   the reference's FP64 arithmetic, sums formed in parallel;
+//   FP32   plain FP32 throughout, on world coordinates;
+//   FP32C  FP32 with compensated covariance sums: each point is taken
+//          relative to its voxel's first point (a float subtraction of two
+//          nearby values, free of cancellation error) and the sums of the
+//          coordinates and of their products are TwoSum-compensated
+//          (Knuth's error-free addition); the plane terms use the same
+//          relative coordinates.
+//
+// Three launches per call:
+//   k_fit_sums   one warp per voxel: sums of p and p p^T (lane-strided, four
+//                points per lane in flight), reduced across the warp by a
+//                transpose reduction (16 shuffles for 9 sums instead of 45);
+//                the sums are parked in the record's plane_cov slots.
+//   k_fit_eig    one thread per voxel: mean, C = ppt / n - mean mean^T, the
+//                eigen decomposition, the plane test, the normal's sign flip
+//                and the per-voxel factors of J (parked in plane_cov).
+//   k_fit_terms  one warp per plane voxel: the per-point terms of
+//                J cov J^T in factored form, reduced like the sums; lane
+//                e < 21 forms entry e of the 6x6 and writes it.
+//
+// Factored J cov J^T.  With evecs E = [n v1 v2], d = p - mean, a = n . d,
+// b_m = v_m . d and k_m = 1 / (n_pts (l0 - l_m)), row m of updatePlane's F is
+// f_m^T with f_m = k_m (a v_m + b_m n) (m = 1, 2; row 0 is zero), so the top
+// block of J is A = E F = v1 f1^T + v2 f2^T and, with g_m = cov f_m and
+// s_mk = f_m . g_k,
+//   A cov A^T = s11 v1 v1^T + s12 (v1 v2^T + v2 v1^T) + s22 v2 v2^T,
+//   A cov / n = (v1 g1^T + v2 g2^T) / n,      cov / n^2 (bottom right).
+// Summed over the points, 15 numbers per voxel (S11 S12 S22, G1, G2 and the
+// sum of the point covariances) give the whole 6x6: the reference's sums,
+// regrouped (rounding-level differences in FP64).
+#include <mutex>
+
+#include "kernels.cuh"
+
+namespace vmp {
+namespace {
+
+constexpr int FIT_FP64 = VMP_FIT_FP64, FIT_FP32 = VMP_FIT_FP32, FIT_FP32C = VMP_FIT_FP32C;
+constexpr int kFitWarps = 8;  // warps per CTA in the warp-per-voxel kernels
+
+struct FitArgs {
+    const float* x;
+    const float* y;
+    const float* z;
+    const float* c[6];  // point covariance: xx xy xz yy yz zz
+    const long long* off;
+    long long n_pts;
+    int n_vox;
+    int min_pts;
+    double plane_thresh;
+    vmp_fit_rec* out;
+};
+
+// A compensated float sum: value s plus the running error c.
+struct F2 {
+    float s, c;
+};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+__device__ __forceinline__ float shx(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shx(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ F2 shx(F2 v, int o) { return {shx(v.s, o), shx(v.c, o)}; }
+__device__ __forceinline__ float comb(float a, float b) { return a + b; }
+__device__ __forceinline__ double comb(double a, double b) { return a + b; }
+__device__ __forceinline__ F2 comb(F2 a, F2 b) {
+    float s, e;
+    two_sum(a.s, b.s, s, e);
+    return {s, (a.c + b.c) + e};
+}
+__device__ __forceinline__ void acc_add(F2& a, float v) {
+    float s, e;
+    two_sum(a.s, v, s, e);
+    a.s = s;
+    a.c += e;
+}
+__device__ __forceinline__ double as_double(float v) { return (double)v; }
+__device__ __forceinline__ double as_double(double v) { return v; }
+__device__ __forceinline__ double as_double(F2 v) { return (double)v.s + (double)v.c; }
+template <class V> __device__ __forceinline__ V vzero() { return V(0); }
+template <> __device__ __forceinline__ F2 vzero<F2>() { return {0.f, 0.f}; }
+
+__device__ __forceinline__ float mad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double mad(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// Sum of 16 per-lane values over the warp in 16 shuffles: at each level a
+// lane keeps half of its values and trades the other half with its partner.
+// Afterwards lanes red_lane(k) and red_lane(k) + 1 hold the total of value k.
+template <class V>
+__device__ __forceinline__ void transpose_reduce16(V (&v)[16], int lane) {
+#pragma unroll
+    for (int lvl = 0; lvl < 4; ++lvl) {
+        const int o = 16 >> lvl, half = 8 >> lvl;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < half; ++k) {
+            const V send = up ? v[k] : v[k + half];
+            const V keep = up ? v[k + half] : v[k];
+            v[k] = comb(keep, shx(send, o));
+        }
+    }
+    v[0] = comb(v[0], shx(v[0], 1));
+}
+__host__ __device__ constexpr int red_lane(int k) {
+    return (((k >> 3) & 1) << 4) | (((k >> 2) & 1) << 3) | (((k >> 1) & 1) << 2) | ((k & 1) << 1);
+}
+__device__ __forceinline__ int red_index(int lane) {
+    return (((lane >> 4) & 1) << 3) | (((lane >> 3) & 1) << 2) | (((lane >> 2) & 1) << 1) | ((lane >> 1) & 1);
+}
+
+template <int MODE> struct FitTypes;
+template <> struct FitTypes<FIT_FP64> { using T = double; using Acc = double; };
+template <> struct FitTypes<FIT_FP32> { using T = float; using Acc = float; };
+template <> struct FitTypes<FIT_FP32C> { using T = float; using Acc = F2; };
+
+__device__ __forceinline__ void voxel_range(const FitArgs& a, long long v, long long& p0, long long& p1) {
+    // offsets are clamped into [0, n_pts]: a malformed list gives wrong
+    // records, never an access outside the point arrays
+    p0 = a.off[v];
+    p1 = a.off[v + 1];
+    p0 = p0 < 0 ? 0 : (p0 > a.n_pts ? a.n_pts : p0);
+    p1 = p1 < p0 ? p0 : (p1 > a.n_pts ? a.n_pts : p1);
+}
+
+// ---------------------------------------------------------------- sums
+template <int MODE>
+__global__ void __launch_bounds__(kFitWarps * 32) k_fit_sums(FitArgs a) {
+    using T = typename FitTypes<MODE>::T;
+    using Acc = typename FitTypes<MODE>::Acc;
+    const int lane = threadIdx.x & 31;
+    const long long v = (long long)blockIdx.x * kFitWarps + (threadIdx.x >> 5);
+    if (v >= a.n_vox) return;  // uniform per warp
+    long long p0, p1;
+    voxel_range(a, v, p0, p1);
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (MODE == FIT_FP32C && p1 > p0) {
+        ax = a.x[p0];
+        ay = a.y[p0];
+        az = a.z[p0];
+    }
+    Acc acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = vzero<Acc>();
+    for (long long i = p0 + lane; i < p1; i += 128) {
+        float px[4], py[4], pz[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long k = i + 32 * u;
+            const bool ok = k < p1;
+            px[u] = ok ? __ldg(a.x + k) : 0.f;
+            py[u] = ok ? __ldg(a.y + k) : 0.f;
+            pz[u] = ok ? __ldg(a.z + k) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (i + 32 * u >= p1) break;
+            if constexpr (MODE == FIT_FP32C) {
+                const float dx = px[u] - ax, dy = py[u] - ay, dz = pz[u] - az;
+                acc_add(acc[0], dx);
+                acc_add(acc[1], dy);
+                acc_add(acc[2], dz);
+                acc_add(acc[3], dx * dx);
+                acc_add(acc[4], dx * dy);
+                acc_add(acc[5], dx * dz);
+                acc_add(acc[6], dy * dy);
+                acc_add(acc[7], dy * dz);
+                acc_add(acc[8], dz * dz);
+            } else {
+                const T x = (T)px[u], y = (T)py[u], z = (T)pz[u];
+                acc[0] += x;
+                acc[1] += y;
+                acc[2] += z;
+                acc[3] = mad(x, x, acc[3]);
+                acc[4] = mad(x, y, acc[4]);
+                acc[5] = mad(x, z, acc[5]);
+                acc[6] = mad(y, y, acc[6]);
+                acc[7] = mad(y, z, acc[7]);
+                acc[8] = mad(z, z, acc[8]);
+            }
+        }
+    }
+    transpose_reduce16(acc, lane);
+    const int k = red_index(lane);
+    if ((lane & 1) == 0 && k < 9) a.out[v].plane_cov[k] = as_double(acc[0]);
+}
+
+// ---------------------------------------------------------------- eigen
+// Parked per-voxel factors for k_fit_terms (plane_cov slots 0..14): the mean
+// the points are taken relative to (FP32C: relative to the first point),
+// the unflipped normal, v1, v2, k1, k2, 1 / n.
+template <int MODE>
+__global__ void k_fit_eig(FitArgs a) {
+    using T = typename FitTypes<MODE>::T;
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= a.n_vox) return;
+    vmp_fit_rec& r = a.out[v];
+    long long p0, p1;
+    voxel_range(a, v, p0, p1);
+    const int n = (int)(p1 - p0);
+    double S[9];
+    for (int k = 0; k < 9; ++k) S[k] = r.plane_cov[k];
+    for (int k = 0; k < 21; ++k) r.plane_cov[k] = 0.0;
+    for (int k = 0; k < 3; ++k) r.norm[k] = 0.0;
+    r.n = n;
+    r.flags = 0;
+    if (n <= 0) {
+        for (int k = 0; k < 3; ++k) r.mean[k] = 0.0, r.evals[k] = 0.0;
+        for (int k = 0; k < 6; ++k) r.cov[k] = 0.0;
+        return;
+    }
+    const T tn = (T)n;
+    T m[3];  // mean, relative to the first point in FP32C
+    for (int k = 0; k < 3; ++k) m[k] = (T)S[k] / tn;
+    double mean[3];
+    if (MODE == FIT_FP32C) {
+        const double anchor[3] = {(double)a.x[p0], (double)a.y[p0], (double)a.z[p0]};
+        for (int k = 0; k < 3; ++k) mean[k] = anchor[k] + (double)m[k];
+    } else {
+        for (int k = 0; k < 3; ++k) mean[k] = (double)m[k];
+    }
+    for (int k = 0; k < 3; ++k) r.mean[k] = mean[k];
+    if (n < a.min_pts) {
+        for (int k = 0; k < 3; ++k) r.evals[k] = 0.0;
+        for (int k = 0; k < 6; ++k) r.cov[k] = 0.0;
+        return;
+    }
+    // C = ppt / n - mean mean^T (upper triangle mirrored)
+    constexpr int kU[3][3] = {{3, 4, 5}, {4, 6, 7}, {5, 7, 8}};
+    T C[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) C[i * 3 + j] = (T)S[kU[i][j]] / tn - m[i] * m[j];
+    T ev[3], E[9];
+    eig_sym3<T>(C, ev, E);
+    r.cov[0] = (double)C[0];
+    r.cov[1] = (double)C[1];
+    r.cov[2] = (double)C[2];
+    r.cov[3] = (double)C[4];
+    r.cov[4] = (double)C[5];
+    r.cov[5] = (double)C[8];
+    for (int k = 0; k < 3; ++k) r.evals[k] = (double)ev[k];
+    int flags = VMP_FIT_FITTED;
+    if ((double)ev[0] > a.plane_thresh) {
+        r.flags = flags;
+        return;
+    }
+    flags |= VMP_FIT_PLANE;
+    const T pn[3] = {E[0], E[3], E[6]};
+    // sign flip of updatePlane (voxel_map.cpp:131-133)
+    bool flip;
+    if (MODE == FIT_FP32) {
+        flip = -(m[0] * pn[0] + m[1] * pn[1] + m[2] * pn[2]) < T(0);
+    } else {
+        flip = -(mean[0] * (double)pn[0] + mean[1] * (double)pn[1] + mean[2] * (double)pn[2]) < 0.0;
+    }
+    if (flip) flags |= VMP_FIT_FLIPPED;
+    for (int k = 0; k < 3; ++k) r.norm[k] = flip ? -(double)pn[k] : (double)pn[k];
+    double* pk = r.plane_cov;
+    for (int k = 0; k < 3; ++k) {
+        pk[k] = (double)m[k];
+        pk[3 + k] = (double)pn[k];
+        pk[6 + k] = (double)E[k * 3 + 1];
+        pk[9 + k] = (double)E[k * 3 + 2];
+    }
+    pk[12] = (double)(T(1) / (tn * (ev[0] - ev[1])));
+    pk[13] = (double)(T(1) / (tn * (ev[0] - ev[2])));
+    pk[14] = (double)(T(1) / tn);
+    r.flags = flags;
+}
+
+// ---------------------------------------------------------------- terms
+template <int MODE>
+__global__ void __launch_bounds__(kFitWarps * 32) k_fit_terms(FitArgs a) {
+    using T = typename FitTypes<MODE>::T;
+    const int lane = threadIdx.x & 31;
+    const long long v = (long long)blockIdx.x * kFitWarps + (threadIdx.x >> 5);
+    if (v >= a.n_vox) return;
+    vmp_fit_rec& r = a.out[v];
+    if (!(r.flags & VMP_FIT_PLANE)) return;  // uniform per warp
+    const double* pk = r.plane_cov;
+    T m[3], nn[3], v1[3], v2[3];
+    for (int k = 0; k < 3; ++k) {
+        m[k] = (T)pk[k];
+        nn[k] = (T)pk[3 + k];
+        v1[k] = (T)pk[6 + k];
+        v2[k] = (T)pk[9 + k];
+    }
+    const T k1 = (T)pk[12], k2 = (T)pk[13], inv_n = (T)pk[14];
+    long long p0, p1;
+    voxel_range(a, v, p0, p1);
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (MODE == FIT_FP32C) {
+        ax = a.x[p0];
+        ay = a.y[p0];
+        az = a.z[p0];
+    }
+    T acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = T(0);
+    for (long long i = p0 + lane; i < p1; i += 128) {
+        float px[4], py[4], pz[4], pc[4][6];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long k = i + 32 * u;
+            const bool ok = k < p1;
+            px[u] = ok ? __ldg(a.x + k) : 0.f;
+            py[u] = ok ? __ldg(a.y + k) : 0.f;
+            pz[u] = ok ? __ldg(a.z + k) : 0.f;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) pc[u][q] = ok ? __ldg(a.c[q] + k) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (i + 32 * u >= p1) break;
+            T d[3];
+            if constexpr (MODE == FIT_FP32C) {
+                d[0] = (px[u] - ax) - m[0];
+                d[1] = (py[u] - ay) - m[1];
+                d[2] = (pz[u] - az) - m[2];
+            } else {
+                d[0] = (T)px[u] - m[0];
+                d[1] = (T)py[u] - m[1];
+                d[2] = (T)pz[u] - m[2];
+            }
+            const T an = mad(nn[2], d[2], mad(nn[1], d[1], nn[0] * d[0]));
+            const T b1 = mad(v1[2], d[2], mad(v1[1], d[1], v1[0] * d[0]));
+            const T b2 = mad(v2[2], d[2], mad(v2[1], d[1], v2[0] * d[0]));
+            T f1[3], f2[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                f1[q] = k1 * mad(an, v1[q], b1 * nn[q]);
+                f2[q] = k2 * mad(an, v2[q], b2 * nn[q]);
+            }
+            const T c00 = (T)pc[u][0], c01 = (T)pc[u][1], c02 = (T)pc[u][2], c11 = (T)pc[u][3],
+                    c12 = (T)pc[u][4], c22 = (T)pc[u][5];
+            T g1[3], g2[3];
+            g1[0] = mad(c02, f1[2], mad(c01, f1[1], c00 * f1[0]));
+            g1[1] = mad(c12, f1[2], mad(c11, f1[1], c01 * f1[0]));
+            g1[2] = mad(c22, f1[2], mad(c12, f1[1], c02 * f1[0]));
+            g2[0] = mad(c02, f2[2], mad(c01, f2[1], c00 * f2[0]));
+            g2[1] = mad(c12, f2[2], mad(c11, f2[1], c01 * f2[0]));
+            g2[2] = mad(c22, f2[2], mad(c12, f2[1], c02 * f2[0]));
+            acc[0] += mad(f1[2], g1[2], mad(f1[1], g1[1], f1[0] * g1[0]));
+            acc[1] += mad(f1[2], g2[2], mad(f1[1], g2[1], f1[0] * g2[0]));
+            acc[2] += mad(f2[2], g2[2], mad(f2[1], g2[1], f2[0] * g2[0]));
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                acc[3 + q] += g1[q];
+                acc[6 + q] += g2[q];
+            }
+            acc[9] += c00;
+            acc[10] += c01;
+            acc[11] += c02;
+            acc[12] += c11;
+            acc[13] += c12;
+            acc[14] += c22;
+        }
+    }
+    transpose_reduce16(acc, lane);
+    // lane e < 21 forms entry e = (i, j), i <= j, row by row
+    int i = 0, j = 0;
+    {
+        int e = lane < 21 ? lane : 0, row = 0, len = 6;
+        while (e >= len) { e -= len; ++row; --len; }
+        i = row;
+        j = row + e;
+    }
+    const T s11 = __shfl_sync(0xffffffffu, acc[0], red_lane(0));
+    const T s12 = __shfl_sync(0xffffffffu, acc[0], red_lane(1));
+    const T s22 = __shfl_sync(0xffffffffu, acc[0], red_lane(2));
+    const int jc = j >= 3 ? j - 3 : j;
+    const T g1j = __shfl_sync(0xffffffffu, acc[0], red_lane(3 + jc));
+    const T g2j = __shfl_sync(0xffffffffu, acc[0], red_lane(6 + jc));
+    int ss = 0;
+    if (i >= 3) {
+        const int a3 = i - 3, b3 = j - 3;  // index in xx xy xz yy yz zz
+        ss = a3 == 0 ? b3 : (a3 == 1 ? 2 + b3 : 5);
+    }
+    const T sij = __shfl_sync(0xffffffffu, acc[0], red_lane(9 + ss));
+    if (lane < 21) {
+        T val;
+        if (j < 3) {
+            val = s11 * v1[i] * v1[j] + s12 * (v1[i] * v2[j] + v2[i] * v1[j]) + s22 * v2[i] * v2[j];
+        } else if (i < 3) {
+            val = (v1[i] * g1j + v2[i] * g2j) * inv_n;
+        } else {
+            val = sij * inv_n * inv_n;
+        }
+        r.plane_cov[lane] = (double)val;
+    }
+}
+
+// Measurement hook (vmp_fit_profile): CUDA events around each kernel, the
+// call waits for them and adds up the per-kernel device time.
+struct FitProfile {
+    std::mutex mu;
+    bool on = false;
+    cudaEvent_t ev[4] = {};
+    double ms[3] = {};
+    long long calls = 0;
+};
+FitProfile& fit_profile() {
+    static FitProfile p;
+    return p;
+}
+
+template <int MODE>
+void launch_mode(const FitArgs& a, cudaStream_t st, cudaEvent_t* ev) {
+    const unsigned wgrid = (unsigned)((a.n_vox + kFitWarps - 1) / kFitWarps);
+    const unsigned tgrid = (unsigned)((a.n_vox + 255) / 256);
+    if (ev) cudaEventRecord(ev[0], st);
+    VMP_NOTE_LAUNCH(); k_fit_sums<MODE><<<wgrid, kFitWarps * 32, 0, st>>>(a);
+    if (ev) cudaEventRecord(ev[1], st);
+    VMP_NOTE_LAUNCH(); k_fit_eig<MODE><<<tgrid, 256, 0, st>>>(a);
+    if (ev) cudaEventRecord(ev[2], st);
+    VMP_NOTE_LAUNCH(); k_fit_terms<MODE><<<wgrid, kFitWarps * 32, 0, st>>>(a);
+    if (ev) cudaEventRecord(ev[3], st);
+}
+
+bool params_ok(const vmp_fit_params* p) {
+    return p && p->mode >= VMP_FIT_FP64 && p->mode <= VMP_FIT_FP32C && p->update_point_thresh >= 1 &&
+           p->plane_thresh == p->plane_thresh;
+}
+
+cudaError_t fit_enqueue(const float* xyz, const float* cov, const long long* offsets, int n_vox, long long n_pts,
+                        const vmp_fit_params* p, vmp_fit_rec* out, cudaStream_t st) {
+    FitArgs a;
+    a.x = xyz;
+    a.y = xyz + n_pts;
+    a.z = xyz + 2 * n_pts;
+    for (int q = 0; q < 6; ++q) a.c[q] = cov + q * n_pts;
+    a.off = offsets;
+    a.n_pts = n_pts;
+    a.n_vox = n_vox;
+    a.min_pts = p->update_point_thresh;
+    a.plane_thresh = p->plane_thresh;
+    a.out = out;
+    FitProfile& prof = fit_profile();
+    std::unique_lock<std::mutex> lk(prof.mu);
+    cudaEvent_t* ev = nullptr;
+    if (prof.on) {
+        for (auto& e : prof.ev)
+            if (!e && cudaEventCreate(&e) != cudaSuccess) return cudaGetLastError();
+        ev = prof.ev;
+    } else {
+        lk.unlock();
+    }
+    switch (p->mode) {
+        case VMP_FIT_FP64: launch_mode<FIT_FP64>(a, st, ev); break;
+        case VMP_FIT_FP32: launch_mode<FIT_FP32>(a, st, ev); break;
+        default: launch_mode<FIT_FP32C>(a, st, ev); break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (ev && e == cudaSuccess && (e = cudaEventSynchronize(ev[3])) == cudaSuccess) {
+        for (int k = 0; k < 3; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            prof.ms[k] += t;
+        }
+        ++prof.calls;
+    }
+    return e;
+}
+
+}  // namespace
+}  // namespace vmp
+
+using namespace vmp;
+
+extern "C" vmp_status vmp_fit_planes_device(const float* xyz, const float* cov, const long long* offsets,
+                                            int n_vox, long long n_pts, const vmp_fit_params* params,
+                                            vmp_fit_rec* out, void* cuda_stream) {
+    if (!params_ok(params) || n_vox < 0 || n_pts < 0) return VMP_ERR_INVALID_ARG;
+    if (n_vox == 0) return VMP_OK;
+    if (!offsets || !out || (n_pts > 0 && (!xyz || !cov))) return VMP_ERR_INVALID_ARG;
+    if (fit_enqueue(xyz, cov, offsets, n_vox, n_pts, params, out, (cudaStream_t)cuda_stream) != cudaSuccess)
+        return VMP_ERR_CUDA;
+    return VMP_OK;
+}
+
+extern "C" vmp_status vmp_fit_planes(const float* xyz, const float* cov, const long long* offsets, int n_vox,
+                                     long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out) {
+    if (!params_ok(params) || n_vox < 0 || n_pts < 0) return VMP_ERR_INVALID_ARG;
+    if (n_vox == 0) return VMP_OK;
+    if (!offsets || !out || (n_pts > 0 && (!xyz || !cov))) return VMP_ERR_INVALID_ARG;
+    if (offsets[0] != 0 || offsets[n_vox] != n_pts) return VMP_ERR_INVALID_ARG;
+    for (int v = 0; v < n_vox; ++v)
+        if (offsets[v + 1] < offsets[v]) return VMP_ERR_INVALID_ARG;
+    cudaStream_t st = nullptr;
+    float* d_pts = nullptr;
+    long long* d_off = nullptr;
+    vmp_fit_rec* d_out = nullptr;
+    vmp_status rc = VMP_OK;
+    const size_t pts_bytes = sizeof(float) * 9 * (size_t)(n_pts > 0 ? n_pts : 1);
+    do {
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { rc = VMP_ERR_CUDA; break; }
+        if (cudaMalloc((void**)&d_pts, pts_bytes) != cudaSuccess ||
+            cudaMalloc((void**)&d_off, sizeof(long long) * ((size_t)n_vox + 1)) != cudaSuccess ||
+            cudaMalloc((void**)&d_out, sizeof(vmp_fit_rec) * (size_t)n_vox) != cudaSuccess) {
+            rc = VMP_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        float* d_xyz = d_pts;
+        float* d_cov = d_pts + 3 * (size_t)n_pts;
+        if (n_pts > 0 &&
+            (cudaMemcpyAsync(d_xyz, xyz, sizeof(float) * 3 * (size_t)n_pts, cudaMemcpyHostToDevice, st) !=
+                 cudaSuccess ||
+             cudaMemcpyAsync(d_cov, cov, sizeof(float) * 6 * (size_t)n_pts, cudaMemcpyHostToDevice, st) !=
+                 cudaSuccess)) {
+            rc = VMP_ERR_CUDA;
+            break;
+        }
+        if (cudaMemcpyAsync(d_off, offsets, sizeof(long long) * ((size_t)n_vox + 1), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            fit_enqueue(d_xyz, d_cov, d_off, n_vox, n_pts, params, d_out, st) != cudaSuccess ||
+            cudaMemcpyAsync(out, d_out, sizeof(vmp_fit_rec) * (size_t)n_vox, cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            rc = VMP_ERR_CUDA;
+            break;
+        }
+    } while (false);
+    if (rc != VMP_OK) cudaGetLastError();
+    if (st) cudaStreamSynchronize(st);
+    if (d_pts) cudaFree(d_pts);
+    if (d_off) cudaFree(d_off);
+    if (d_out) cudaFree(d_out);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
+extern "C" vmp_status vmp_fit_profile(int on) {
+    FitProfile& p = fit_profile();
+    std::lock_guard<std::mutex> lk(p.mu);
+    p.on = on != 0;
+    for (double& m : p.ms) m = 0.0;
+    p.calls = 0;
+    return VMP_OK;
+}
+
+extern "C" vmp_status vmp_fit_profile_read(double* ms, long long* calls) {
+    FitProfile& p = fit_profile();
+    std::lock_guard<std::mutex> lk(p.mu);
+    if (ms)
+        for (int k = 0; k < 3; ++k) ms[k] = p.ms[k];
+    if (calls) *calls = p.calls;
+    return VMP_OK;
+}

@@ -261,51 +261,6 @@ __device__ inline double* slab_pt(const DMap& m, const int* chunks, int j) {
     return m.slab + ((size_t)chunks[j / kChunkPts] * kChunkPts + (j % kChunkPts)) * kSlabStride;
 }
 
-// Symmetric 3x3 eigen decomposition (cyclic Jacobi), the same operation
-// sequence as the oracle's restatement of Eigen's SelfAdjointEigenSolver.
-__device__ void eig_sym3(const double* A, double* evals, double* evecs) {
-    double a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) a[i][j] = A[i * 3 + j];
-    for (int sweep = 0; sweep < 50; ++sweep) {
-        double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-        double scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
-        if (off == 0.0 || off <= 1e-300 || off < 1e-18 * scale) break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q) {
-                double apq = a[p][q];
-                if (apq == 0.0) continue;
-                double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; ++k) {
-                    double akp = a[k][p], akq = a[k][q];
-                    a[k][p] = c * akp - s * akq;
-                    a[k][q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double apk = a[p][k], aqk = a[q][k];
-                    a[p][k] = c * apk - s * aqk;
-                    a[q][k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double vkp = v[k][p], vkq = v[k][q];
-                    v[k][p] = c * vkp - s * vkq;
-                    v[k][q] = s * vkp + c * vkq;
-                }
-            }
-    }
-    int idx[3] = {0, 1, 2};
-    double d[3] = {a[0][0], a[1][1], a[2][2]};
-    for (int i = 0; i < 3; ++i)
-        for (int j = i + 1; j < 3; ++j)
-            if (d[idx[j]] < d[idx[i]]) { int t = idx[i]; idx[i] = idx[j]; idx[j] = t; }
-    for (int c = 0; c < 3; ++c) {
-        evals[c] = d[idx[c]];
-        for (int r = 0; r < 3; ++r) evecs[r * 3 + c] = v[r][idx[c]];
-    }
-}
-
 // Per-refit factors of VoxelGrid::updatePlane's J (voxel_map.cpp:115-130):
 // J = [evecs * F; I / n], F row m = ((p - mean) / (n (l0 - lm)))^T (vm pn^T + pn vm^T).
 struct RefitConst {
@@ -680,7 +635,7 @@ __global__ void k_refit_eig(DMap m, SegScratch ss) {
         double C[9], ev[3], evecs[9];
         for (int k = 0; k < 3; ++k)
             for (int l = 0; l < 3; ++l) C[k * 3 + l] = sn.ppt[k * 3 + l] / dn - sn.mean[k] * sn.mean[l];
-        eig_sym3(C, ev, evecs);
+        eig_sym3<double>(C, ev, evecs);
         for (int k = 0; k < 3; ++k) sn.ev[k] = ev[k];
         for (int k = 0; k < 9; ++k) sn.evecs[k] = evecs[k];
         const int plane = ev[0] > m.plane_thresh ? 0 : 1;

@@ -29,10 +29,16 @@ __global__ void k_time_keys(const float4* __restrict__ raw, const int* d_n, uint
         v[i] = (uint32_t)i;
     }
 }
-__global__ void k_gather4(const float4* __restrict__ src, const uint32_t* __restrict__ perm, const int* d_n,
-                          float4* __restrict__ dst) {
+// Applies the time-sort permutation to the points and their intensities.
+__global__ void k_gather4(const float4* __restrict__ src, const float* __restrict__ src_int,
+                          const uint32_t* __restrict__ perm, const int* d_n, float4* __restrict__ dst,
+                          float* __restrict__ dst_int) {
     const int n = *d_n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[perm[i]];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t j = perm[i];
+        dst[i] = src[j];
+        dst_int[i] = src_int[j];
+    }
 }
 
 static int grid_for(int n_max) {
@@ -45,7 +51,7 @@ void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st) {
     int g = grid_for(n_max);
     VMP_NOTE_LAUNCH(); k_time_keys<<<g, kPtThreads, 0, st>>>(s.raw, s.d_n_raw, s.sort_k, s.sort_v);
     radix_sort_pairs(s.sort_k, s.sort_v, s.d_n_raw, 32, ss, st);
-    VMP_NOTE_LAUNCH(); k_gather4<<<g, kPtThreads, 0, st>>>(s.raw, s.sort_v, s.d_n_raw, s.cloud);
+    VMP_NOTE_LAUNCH(); k_gather4<<<g, kPtThreads, 0, st>>>(s.raw, s.raw_int, s.sort_v, s.d_n_raw, s.cloud, s.cloud_int);
 }
 
 // ---------------------------------------------------------------- downsample
@@ -285,6 +291,93 @@ void launch_map_batch(DFilter* f, DScan& s, int n_max, bool from_full_cloud, dou
     else
         k_map_batch<<<grid_for(n_max), kPtThreads, 0, st>>>(f, s.down, s.d_n_down, s.pl, s.covl, 0, range_inc,
                                                              sin_deg, s.bpts, s.bcov, s.d_n_batch);
+}
+
+// ---------------------------------------------------------------- Livox decode
+// livox2pcl (src/utils.cpp:3-28) as a stream compaction: a point passes the
+// line / tag test, then every filter_num-th passing point (counted from 0)
+// goes on to the range test, |p|^2 summed in float as in the reference and
+// compared in double.
+__device__ inline bool livox_line_tag_ok(const vmp_livox_point& p) {
+    const unsigned t = p.tag & 0x30u;
+    return p.line < 4 && (t == 0x10u || t == 0x00u);
+}
+__global__ void k_livox_valid(const vmp_livox_point* __restrict__ in, int n, uint32_t* __restrict__ valid,
+                              int* d_n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_n = n;  // count for the scans that follow
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        valid[i] = livox_line_tag_ok(in[i]) ? 1u : 0u;
+}
+__global__ void k_livox_keep(const vmp_livox_point* __restrict__ in, int n, const uint32_t* __restrict__ valid,
+                             const uint32_t* __restrict__ rank, unsigned filter_num, double rmin2, double rmax2,
+                             uint32_t* __restrict__ keep) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = 0;
+        if (valid[i] && rank[i] % filter_num == 0u) {
+            const vmp_livox_point p = in[i];
+            const float sq = p.x * p.x + p.y * p.y + p.z * p.z;
+            const double d = (double)sq;
+            k = (d > rmin2 && d < rmax2) ? 1u : 0u;
+        }
+        keep[i] = k;
+    }
+}
+__global__ void k_livox_scatter(const vmp_livox_point* __restrict__ in, int n, const uint32_t* __restrict__ keep,
+                                const uint32_t* __restrict__ pos, float4* __restrict__ raw, float* __restrict__ raw_int) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!keep[i]) continue;
+        const vmp_livox_point p = in[i];
+        const uint32_t o = pos[i];
+        raw[o] = make_float4(p.x, p.y, p.z, (float)p.offset_time / 1000000.0f);  // ns -> ms
+        raw_int[o] = (float)p.reflectivity;
+    }
+}
+
+void launch_livox_decode(DScan& s, const vmp_livox_point* d_in, int n, int filter_num, double range_min,
+                         double range_max, ScanScratch& sc, cudaStream_t st) {
+    const int g = grid_for(n);
+    VMP_NOTE_LAUNCH(); k_livox_valid<<<g, kPtThreads, 0, st>>>(d_in, n, s.flags, s.d_n_in);
+    exclusive_scan_u32(s.flags, s.scan_out, s.d_n_in, s.d_n_in + 1, sc, st);
+    VMP_NOTE_LAUNCH(); k_livox_keep<<<g, kPtThreads, 0, st>>>(d_in, n, s.flags, s.scan_out, (unsigned)filter_num,
+                                                             range_min * range_min, range_max * range_max, s.sort_k);
+    exclusive_scan_u32(s.sort_k, s.sort_v, s.d_n_in, s.d_n_raw, sc, st);
+    VMP_NOTE_LAUNCH(); k_livox_scatter<<<g, kPtThreads, 0, st>>>(d_in, n, s.sort_k, s.sort_v, s.raw, s.raw_int);
+}
+
+// ---------------------------------------------------------------- output clouds
+// lidarToBody / lidarToWorld (lio_builder.cpp:155-173): the undistorted cloud
+// under a float 4x4 transform, in pcl::transformPointCloud's operation order.
+__global__ void k_output_cloud(const DFilter* __restrict__ f, const float4* __restrict__ cloud,
+                               const float* __restrict__ cloud_int, int n, int frame, float4* __restrict__ out,
+                               float* __restrict__ out_int) {
+    __shared__ float sR[9], sT[3];
+    if (threadIdx.x == 0) {
+        const DState& x = f->x;
+        if (frame == 0) {
+            for (int a = 0; a < 9; ++a) sR[a] = (float)x.rot_ext[a];
+            for (int a = 0; a < 3; ++a) sT[a] = (float)x.pos_ext[a];
+        } else {
+            double rwl[9], rp[3];
+            mm<3, 3, 3>(x.rot, x.rot_ext, rwl);
+            m3v(x.rot, x.pos_ext, rp);
+            for (int a = 0; a < 9; ++a) sR[a] = (float)rwl[a];
+            for (int a = 0; a < 3; ++a) sT[a] = (float)(rp[a] + x.pos[a]);
+        }
+    }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 q = cloud[i];
+        float w[3];
+        for (int r = 0; r < 3; ++r) w[r] = q.x * sR[r * 3] + (q.y * sR[r * 3 + 1] + (q.z * sR[r * 3 + 2] + sT[r]));
+        out[i] = make_float4(w[0], w[1], w[2], q.w);
+        if (out_int) out_int[i] = cloud_int[i];
+    }
+}
+
+void launch_output_cloud(const DFilter* f, const DScan& s, int n, int frame, float4* out, float* out_int,
+                         cudaStream_t st) {
+    if (n <= 0) return;
+    VMP_NOTE_LAUNCH(); k_output_cloud<<<grid_for(n), kPtThreads, 0, st>>>(f, s.cloud, s.cloud_int, n, frame, out, out_int);
 }
 
 }  // namespace vmp

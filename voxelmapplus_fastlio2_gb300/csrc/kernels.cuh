@@ -21,6 +21,9 @@ struct DScan {
     // raw scan (input) and its time-sorted, undistorted copy
     float4* raw;           // [max_pts] x, y, z, t_ms
     float4* cloud;         // [max_pts] sorted by time, compensated in place
+    float* raw_int;        // [max_pts] intensity of each raw point (0 unless decoded from Livox points)
+    float* cloud_int;      // [max_pts] the same in time order
+    int* d_n_in;           // [4] decode input count and scratch
     uint32_t* sort_k;      // [max_pts]
     uint32_t* sort_v;      // [max_pts]
     uint32_t* flags;       // [max_pts]
@@ -71,6 +74,12 @@ void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st);
 // ---- k_points.cu
 void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st);
 void launch_downsample(DScan& s, int n_max, double leaf, SortScratch& ss, ScanScratch& sc, cudaStream_t st);
+// livox2pcl on the device: n Livox points at d_in -> s.raw / s.raw_int, count in *s.d_n_raw.
+void launch_livox_decode(DScan& s, const vmp_livox_point* d_in, int n, int filter_num, double range_min,
+                         double range_max, ScanScratch& sc, cudaStream_t st);
+// lidarToBody (frame 0) / lidarToWorld (frame 1) of the first n points of s.cloud.
+void launch_output_cloud(const DFilter* f, const DScan& s, int n, int frame, float4* out, float* out_int,
+                         cudaStream_t st);
 void launch_copy_down(DScan& s, int n_max, cudaStream_t st);
 void launch_body_cov(DScan& s, int n_max, double range_inc, double sin_deg, cudaStream_t st);
 // world points + covariances for the map: from the downsampled cloud (after

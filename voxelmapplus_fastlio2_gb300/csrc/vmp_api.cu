@@ -104,6 +104,83 @@ __global__ void k_export(DMap m, vmp_voxel* out, int* d_count, int max) {
         for (int k = 0; k < 36; ++k) v.cov[k] = c.cov[k];
     }
 }
+// ---- voxel-map export for visualisation (voxel2MarkerArray, utils.cpp:154-208)
+// Frozen planes (is_plane && !update_enable) with their LRU stamps, as sort
+// keys that order the most recently touched first (complemented halves).
+__global__ void k_plane_collect(DMap m, int* d_count, uint32_t* key_lo, uint32_t* key_hi, uint32_t* rec, int cap) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m.rec_pool; r += gridDim.x * blockDim.x) {
+        const uint32_t f = m.hot[r].flags;
+        if (!(f & F_ALIVE) || !(f & F_PLANE) || (f & F_UPDATE)) continue;
+        const int pos = atomicAdd(d_count, 1);
+        if (pos >= cap) continue;
+        const uint64_t st = m.cold[r].stamp;
+        key_lo[pos] = ~(uint32_t)st;
+        key_hi[pos] = ~(uint32_t)(st >> 32);
+        rec[pos] = (uint32_t)r;
+    }
+}
+__global__ void k_iota_u32(uint32_t* v, const int* d_n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *d_n; i += gridDim.x * blockDim.x) v[i] = (uint32_t)i;
+}
+__global__ void k_permute_pair(const uint32_t* perm, const uint32_t* a, const uint32_t* b, uint32_t* a2,
+                               uint32_t* b2, const int* d_n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *d_n; i += gridDim.x * blockDim.x) {
+        a2[i] = a[perm[i]];
+        b2[i] = b[perm[i]];
+    }
+}
+// mapJet (utils.cpp:78-128) on v in [0, 1].
+__device__ void map_jet(double v, uint8_t* rgb) {
+    if (v < 0.0) v = 0.0;
+    if (v > 1.0) v = 1.0;
+    double dr, dg, db;
+    if (v < 0.1242) { db = 0.504 + ((1. - 0.504) / 0.1242) * v; dg = dr = 0.; }
+    else if (v < 0.3747) { db = 1.; dr = 0.; dg = (v - 0.1242) * (1. / (0.3747 - 0.1242)); }
+    else if (v < 0.6253) { db = (0.6253 - v) * (1. / (0.6253 - 0.3747)); dg = 1.; dr = (v - 0.3747) * (1. / (0.6253 - 0.3747)); }
+    else if (v < 0.8758) { db = 0.; dr = 1.; dg = (0.8758 - v) * (1. / (0.8758 - 0.6253)); }
+    else { db = 0.; dg = 0.; dr = 1. - (v - 0.8758) * ((1. - 0.504) / (1. - 0.8758)); }
+    rgb[0] = (uint8_t)(255 * dr);
+    rgb[1] = (uint8_t)(255 * dg);
+    rgb[2] = (uint8_t)(255 * db);
+}
+// Rotation taking (0, 0, 1) onto n (Quaternion::setFromTwoVectors as
+// calcVectQuation uses it, utils.cpp:144-152), w x y z.  Antiparallel
+// (c < -1 + 1e-12): a rotation by pi about the x axis.
+__device__ void quat_from_z(const double* n0, double* q) {
+    const double nn = sqrt(n0[0] * n0[0] + n0[1] * n0[1] + n0[2] * n0[2]);
+    const double v1[3] = {n0[0] / nn, n0[1] / nn, n0[2] / nn};
+    const double c = v1[2];
+    if (c < -1.0 + 1e-12) {
+        q[0] = 0.0; q[1] = 1.0; q[2] = 0.0; q[3] = 0.0;
+        return;
+    }
+    // (0, 0, 1) x v1
+    const double axis[3] = {-v1[1], v1[0], 0.0};
+    const double sq = sqrt((1.0 + c) * 2.0);
+    const double invs = 1.0 / sq;
+    q[0] = sq * 0.5;
+    for (int k = 0; k < 3; ++k) q[1 + k] = axis[k] * invs;
+}
+__global__ void k_plane_markers(DMap m, const uint32_t* rec_sorted, int n, vmp_plane_marker* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = rec_sorted[i];
+        const RecHot& h = m.hot[r];
+        const RecCold& c = m.cold[r];
+        vmp_plane_marker o;
+        for (int k = 0; k < 3; ++k) { o.center[k] = c.center[k]; o.norm[k] = h.norm[k]; }
+        double trace = (c.cov[0] + c.cov[7]) + c.cov[14];
+        o.trace = trace;
+        if (trace >= 0.25) trace = 0.25;
+        trace = trace * (1.0 / 0.25);
+        trace = pow(trace, 0.2);
+        map_jet(trace, o.rgb);
+        o.merged = (h.flags & F_MERGED) ? 1 : 0;
+        o.pad = 0;
+        quat_from_z(o.norm, o.orientation);
+        out[i] = o;
+    }
+}
+
 // Buffered points of the given records (offsets = prefix of their counts).
 __global__ void k_export_points(DMap m, const int* recs, const long long* offs, int nrec, double* pts, double* cov) {
     for (int q = blockIdx.x; q < nrec; q += gridDim.x) {
@@ -260,6 +337,11 @@ struct vmp_stream_s {
     struct ScanGraphs { int nb; cudaGraphExec_t g1, g2; long long k1, k2; };
     std::vector<ScanGraphs> graphs;
     bool use_graphs = true;
+    // vmp_map_planes scratch (allocated by its first call)
+    SortScratch vis_ss{};
+    uint32_t* vis_buf = nullptr;  // 6 arrays of rec_pool + 16 u32, then the count
+    int decoded_n = -1;  // points of a vmp_livox_decode cloud waiting for vmp_process_decoded
+    int cloud_n = 0;     // points of the last processed scan's undistorted cloud
     bool blocking_wait = false;  // vmp_set_wait_mode
     cudaEvent_t done_ev = nullptr;
     // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
@@ -409,6 +491,10 @@ vmp_status vmp_destroy(vmp_stream_t s) {
     for (void* p : s->allocs) cudaFree(p);
     map_scratch_free(s->ms);
     sort_scratch_free(s->ss);
+    if (s->vis_buf) {
+        sort_scratch_free(s->vis_ss);
+        cudaFree(s->vis_buf);
+    }
     scan_scratch_free(s->sc);
     scan_scratch_free(s->qsc);
     cudaFreeHost(s->h_pts);
@@ -490,6 +576,9 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     sc.res_blocks = 2 * 152;
     CREATE_TRY(dalloc(s, &sc.raw, max_pts));
     CREATE_TRY(dalloc(s, &sc.cloud, max_pts));
+    CREATE_TRY(dalloc(s, &sc.raw_int, max_pts));
+    CREATE_TRY(dalloc(s, &sc.cloud_int, max_pts));
+    CREATE_TRY(dalloc(s, &sc.d_n_in, 4));
     CREATE_TRY(dalloc(s, &sc.sort_k, max_pts + 16));
     CREATE_TRY(dalloc(s, &sc.sort_v, max_pts + 16));
     CREATE_TRY(dalloc(s, &sc.flags, max_pts + 16));
@@ -679,6 +768,8 @@ static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bc
 }
 
 static vmp_status upload_scan(vmp_stream_t s, const vmp_point* pts, int n, bool device_ptr) {
+    if (pts == reinterpret_cast<const vmp_point*>(s->s.raw)) return VMP_OK;  // decoded on the device
+    VMP_TRY(cudaMemsetAsync(s->s.raw_int, 0, sizeof(float) * (size_t)n, s->st), "intensity");
     if (!device_ptr) s->io_h2d += (long long)sizeof(vmp_point) * n;
     if (device_ptr) {
         VMP_TRY(cudaMemcpyAsync(s->s.raw, pts, sizeof(vmp_point) * (size_t)n, cudaMemcpyDeviceToDevice, s->st), "scan copy");
@@ -900,6 +991,7 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
                                const vmp_imu* imus, int n_imu, bool device_ptrs, vmp_result* out) {
     if (!s) return VMP_ERR_INVALID_ARG;
     if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    if (pts != reinterpret_cast<const vmp_point*>(s->s.raw)) s->decoded_n = -1;  // its buffer is overwritten
     if (!pts || n <= 0) return fail(s, VMP_ERR_INVALID_ARG, "empty scan");
     if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "scan larger than max_scan_points");
     if (!imus || n_imu <= 0) return fail(s, VMP_ERR_INVALID_ARG, "package without IMU samples");
@@ -947,8 +1039,10 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
             s->lio_status = VMP_MAP_INIT;
         }
         VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, st>>>(s->s.d_n_down, 0);
+        s->cloud_n = 0;
         return finish_result(s, n, out);
     }
+    s->cloud_n = n;
     const int nb = size_class(n, cfg.max_scan_points);
     s->pbeg();
     vmp_status v = upload_scan(s, pts, n, device_ptrs);
@@ -988,6 +1082,86 @@ vmp_status vmp_process(vmp_stream_t s, const vmp_scan* scan, const vmp_imu* imus
 vmp_status vmp_process_device(vmp_stream_t s, const vmp_point* d_points, int n, double t_start, double t_end,
                               const vmp_imu* d_imus, int n_imu, vmp_result* out) {
     return process_impl(s, d_points, n, t_start, t_end, d_imus, n_imu, true, out);
+}
+
+vmp_status vmp_livox_decode(vmp_stream_t s, const vmp_livox_point* pts, int n, int filter_num, double range_min,
+                            double range_max, vmp_point* out, float* intensity, int* n_out, float* last_t_ms) {
+    if (!s || !n_out || n < 0 || (n > 0 && !pts)) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    if (filter_num < 1) return fail(s, VMP_ERR_INVALID_ARG, "filter_num must be >= 1");
+    if (n > s->cfg.max_scan_points) return fail(s, VMP_ERR_CAPACITY, "more points than max_scan_points");
+    *n_out = 0;
+    if (last_t_ms) *last_t_ms = 0.0f;
+    s->decoded_n = -1;
+    if (n == 0) {
+        s->decoded_n = 0;
+        return VMP_OK;
+    }
+    // the raw Livox points are staged in the map-batch buffer (24 B per
+    // point, free until the scan's map batch)
+    vmp_livox_point* d_in = reinterpret_cast<vmp_livox_point*>(s->s.bpts);
+    VMP_TRY(cudaMemcpyAsync(d_in, pts, sizeof(vmp_livox_point) * (size_t)n, cudaMemcpyDefault, s->st), "livox upload");
+    s->io_h2d += (long long)sizeof(vmp_livox_point) * n;
+    launch_livox_decode(s->s, d_in, n, filter_num, range_min, range_max, s->sc, s->st);
+    VMP_TRY(cudaGetLastError(), "livox decode");
+    VMP_TRY(cudaMemcpyAsync(s->h_int, s->s.d_n_raw, sizeof(int), cudaMemcpyDeviceToHost, s->st), "count");
+    VMP_TRY(cudaStreamSynchronize(s->st), "livox decode");
+    const int m = s->h_int[0];
+    *n_out = m;
+    s->decoded_n = m;
+    if (m > 0) {
+        if (last_t_ms) {
+            VMP_TRY(cudaMemcpyAsync(last_t_ms, reinterpret_cast<const float*>(s->s.raw + (m - 1)) + 3, sizeof(float),
+                                    cudaMemcpyDefault, s->st), "last time");
+        }
+        if (out)
+            VMP_TRY(cudaMemcpyAsync(out, s->s.raw, sizeof(vmp_point) * (size_t)m, cudaMemcpyDefault, s->st), "cloud");
+        if (intensity)
+            VMP_TRY(cudaMemcpyAsync(intensity, s->s.raw_int, sizeof(float) * (size_t)m, cudaMemcpyDefault, s->st),
+                    "intensity");
+        VMP_TRY(cudaStreamSynchronize(s->st), "livox decode");
+    }
+    return VMP_OK;
+}
+
+vmp_status vmp_process_decoded(vmp_stream_t s, double t_start, double t_end, const vmp_imu* imus, int n_imu,
+                               vmp_result* out) {
+    if (!s) return VMP_ERR_INVALID_ARG;
+    if (s->decoded_n < 0) return fail(s, VMP_ERR_STATE, "no decoded cloud pending (call vmp_livox_decode first)");
+    const int n = s->decoded_n;
+    s->decoded_n = -1;
+    return process_impl(s, reinterpret_cast<const vmp_point*>(s->s.raw), n, t_start, t_end, imus, n_imu, false, out);
+}
+
+vmp_status vmp_output_cloud_device(vmp_stream_t s, int frame, vmp_point* d_out, float* d_intensity, int max,
+                                   int* n_out) {
+    if (!s || !n_out || (frame != 0 && frame != 1) || max < 0 || (max > 0 && !d_out)) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    const int n = s->cloud_n < max ? s->cloud_n : max;
+    *n_out = n;
+    launch_output_cloud(s->f, s->s, n, frame, reinterpret_cast<float4*>(d_out), d_intensity, s->st);
+    VMP_TRY(cudaGetLastError(), "output cloud");
+    return VMP_OK;
+}
+
+vmp_status vmp_output_cloud(vmp_stream_t s, int frame, vmp_point* out, float* intensity, int max, int* n_out) {
+    if (!s || !n_out || (frame != 0 && frame != 1) || max < 0 || (max > 0 && !out)) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    const int n = s->cloud_n;
+    *n_out = n;
+    const int m = n < max ? n : max;
+    if (m <= 0) return VMP_OK;
+    // staged in the map-batch buffer (24 B per point: 16 B point + 4 B intensity)
+    float4* d_pts = reinterpret_cast<float4*>(s->s.bpts);
+    float* d_int = reinterpret_cast<float*>(d_pts + s->s.max_pts);
+    launch_output_cloud(s->f, s->s, m, frame, d_pts, d_int, s->st);
+    VMP_TRY(cudaGetLastError(), "output cloud");
+    VMP_TRY(cudaMemcpyAsync(out, d_pts, sizeof(vmp_point) * (size_t)m, cudaMemcpyDefault, s->st), "cloud");
+    if (intensity)
+        VMP_TRY(cudaMemcpyAsync(intensity, d_int, sizeof(float) * (size_t)m, cudaMemcpyDefault, s->st), "intensity");
+    VMP_TRY(cudaStreamSynchronize(s->st), "output cloud");
+    s->io_d2h += (long long)(sizeof(vmp_point) + (intensity ? sizeof(float) : 0)) * m;
+    return VMP_OK;
 }
 
 // ------------------------------------------------------------- component API
@@ -1078,6 +1252,49 @@ vmp_status vmp_map_export(vmp_stream_t s, vmp_voxel* out, long long max, long lo
     long long n = std::min<long long>(max, (long long)all.size());
     if (n > 0) std::memcpy(out, all.data(), sizeof(vmp_voxel) * (size_t)n);
     if (n_out) *n_out = (long long)all.size();
+    return VMP_OK;
+}
+
+vmp_status vmp_map_planes(vmp_stream_t s, vmp_plane_marker* out, int max, int* n_out) {
+    if (!s || !n_out || max < 0 || (max > 0 && !out)) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    *n_out = 0;
+    if (max == 0) return VMP_OK;
+    const int cap = s->m.rec_pool;
+    const size_t stride = (size_t)cap + 16;
+    if (!s->vis_buf) {
+        VMP_TRY(cudaMalloc(&s->vis_buf, sizeof(uint32_t) * (6 * stride + 16)), "marker scratch");
+        VMP_TRY(sort_scratch_alloc(s->vis_ss, cap), "marker scratch");
+    }
+    uint32_t* lo = s->vis_buf;
+    uint32_t* hi = lo + stride;
+    uint32_t* rec = hi + stride;
+    uint32_t* perm = rec + stride;
+    uint32_t* hi2 = perm + stride;
+    uint32_t* rec2 = hi2 + stride;
+    int* d_count = reinterpret_cast<int*>(rec2 + stride);
+    cudaStream_t st = s->st;
+    VMP_TRY(cudaMemsetAsync(d_count, 0, sizeof(int), st), "count");
+    VMP_NOTE_LAUNCH(); k_plane_collect<<<1216, 256, 0, st>>>(s->m, d_count, lo, hi, rec, cap);
+    const int g = std::max(1, std::min(1216, (cap + 255) / 256));
+    VMP_NOTE_LAUNCH(); k_iota_u32<<<g, 256, 0, st>>>(perm, d_count);
+    // LSD order: by the low stamp word, then stably by the high word
+    radix_sort_pairs(lo, perm, d_count, 32, s->vis_ss, st);
+    VMP_NOTE_LAUNCH(); k_permute_pair<<<g, 256, 0, st>>>(perm, hi, rec, hi2, rec2, d_count);
+    radix_sort_pairs(hi2, rec2, d_count, 32, s->vis_ss, st);
+    VMP_TRY(cudaMemcpyAsync(s->h_int, d_count, sizeof(int), cudaMemcpyDeviceToHost, st), "count");
+    VMP_TRY(cudaStreamSynchronize(st), "markers");
+    const int n = std::min(s->h_int[0], max);
+    if (n <= 0) return VMP_OK;
+    vmp_plane_marker* d_out = nullptr;
+    VMP_TRY(cudaMallocAsync(&d_out, sizeof(vmp_plane_marker) * (size_t)n, st), "marker buffer");
+    VMP_NOTE_LAUNCH(); k_plane_markers<<<std::max(1, std::min(1216, (n + 127) / 128)), 128, 0, st>>>(s->m, rec2, n, d_out);
+    cudaError_t e = cudaMemcpyAsync(out, d_out, sizeof(vmp_plane_marker) * (size_t)n, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d_out, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(s, e, "markers");
+    s->io_d2h += (long long)sizeof(vmp_plane_marker) * n;
+    *n_out = n;
     return VMP_OK;
 }
 

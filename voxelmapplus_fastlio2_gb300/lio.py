@@ -92,6 +92,14 @@ class VoxelMapView:
         check(self._o.h, self._o.lib.vmp_map_export(self._o.h, arr, n.value, C.byref(n)))
         return arr, n.value
 
+    def planes(self, max_markers=100000):
+        """voxel2MarkerArray's data: the frozen planes in LRU order
+        (records of abi.plane_marker_dtype())."""
+        out = np.zeros(max(1, max_markers), dtype=abi.plane_marker_dtype())
+        n = C.c_int()
+        check(self._o.h, self._o.lib.vmp_map_planes(self._o.h, C.c_void_p(out.ctypes.data), max_markers, C.byref(n)))
+        return out[: n.value]
+
     def export_points(self):
         n = C.c_longlong()
         check(self._o.h, self._o.lib.vmp_map_export_points(self._o.h, None, None, 0, C.byref(n)))
@@ -157,6 +165,39 @@ class LIOBuilder:
         check(self.h, self.lib.vmp_process_device(self.h, C.c_void_p(d_points), n, t_start, t_end,
                                                   C.c_void_p(d_imus), n_imu, C.byref(res)))
         return res
+
+    def livox_decode(self, livox, filter_num=1, range_min=0.5, range_max=20.0):
+        """livox2pcl on the device (src/utils.cpp:3-28).  livox: numpy array of
+        abi.livox_dtype().  Returns (points (m, 4) float32: x y z t_ms,
+        intensity (m,), last point's t_ms); the cloud stays on the device for
+        process_decoded."""
+        livox = np.ascontiguousarray(livox, dtype=abi.livox_dtype())
+        n = len(livox)
+        out = np.zeros((max(1, n), 4), dtype=np.float32)
+        inten = np.zeros(max(1, n), dtype=np.float32)
+        m = C.c_int()
+        last = C.c_float()
+        check(self.h, self.lib.vmp_livox_decode(self.h, C.c_void_p(livox.ctypes.data), n, filter_num, range_min,
+                                                range_max, C.c_void_p(out.ctypes.data), C.c_void_p(inten.ctypes.data),
+                                                C.byref(m), C.byref(last)))
+        return out[: m.value], inten[: m.value], last.value
+
+    def process_decoded(self, t_start, t_end, imus, n_imu):
+        """process() on the cloud of the last livox_decode."""
+        res = abi.vmp_result()
+        check(self.h, self.lib.vmp_process_decoded(self.h, t_start, t_end, imus, n_imu, C.byref(res)))
+        return res
+
+    def output_cloud(self, frame):
+        """lidarToBody (frame 0) / lidarToWorld (frame 1) of the last scan's
+        undistorted cloud: (points (n, 4) float32, intensity (n,))."""
+        n = C.c_int()
+        check(self.h, self.lib.vmp_output_cloud(self.h, frame, None, None, 0, C.byref(n)))
+        out = np.zeros((max(1, n.value), 4), dtype=np.float32)
+        inten = np.zeros(max(1, n.value), dtype=np.float32)
+        check(self.h, self.lib.vmp_output_cloud(self.h, frame, C.c_void_p(out.ctypes.data),
+                                                C.c_void_p(inten.ctypes.data), n.value, C.byref(n)))
+        return out[: n.value], inten[: n.value]
 
     def residual_reduce(self, x, P, pts_l, cov_l):
         pts = np.ascontiguousarray(pts_l, dtype=np.float64).reshape(-1, 3)
