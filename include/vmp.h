@@ -322,9 +322,10 @@ enum {
     VMP_FIT_FP64 = 0,  /* the reference's FP64 arithmetic (parallel sums) */
     VMP_FIT_FP32 = 1,  /* plain FP32 throughout, world coordinates */
     VMP_FIT_FP32C = 2  /* FP32 with compensated covariance sums: coordinates
-                          relative to the voxel's first point (an exact
-                          float subtraction) and TwoSum-compensated sums of
-                          the coordinates and their products */
+                          relative to the voxel's first point (a subtraction
+                          of nearby floats, free of cancellation error) and
+                          Kahan-compensated sums of the coordinates and
+                          their products */
 };
 enum { VMP_FIT_FITTED = 1, VMP_FIT_PLANE = 2, VMP_FIT_FLIPPED = 4 };
 typedef struct vmp_fit_params {
@@ -356,10 +357,10 @@ vmp_status vmp_fit_planes_device(const float* xyz, const float* cov, const long 
 vmp_status vmp_fit_planes(const float* xyz, const float* cov, const long long* offsets, int n_vox,
                           long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out);
 /* Measurement hook: while on, every fit call records CUDA events around its
- * three kernels (sums, eigen, plane terms), waits for them and adds up their
- * device time.  vmp_fit_profile resets the totals. */
+ * kernel, waits for them and adds up its device time.  vmp_fit_profile
+ * resets the totals. */
 vmp_status vmp_fit_profile(int on);
-vmp_status vmp_fit_profile_read(double* ms /* 3 */, long long* calls);
+vmp_status vmp_fit_profile_read(double* ms, long long* calls);
 
 /* ---- measurement hooks (no reference counterpart) ----
  * Per-phase device time of vmp_process, from CUDA events recorded on the

@@ -98,6 +98,17 @@ public:
         }
     }
 
+    // LIOBuilder::lidarToBody / lidarToWorld (lio_builder.cpp:155-173) of the
+    // last processed cloud, formed on the device from its undistorted copy.
+    // PointVec: a vector of points with x, y, z, intensity, curvature
+    // (pcl::PointXYZINormal); intensity is the decoded reflectivity after
+    // vmp_livox_decode + vmp_process_decoded, else 0 (the package cloud
+    // written back by process keeps the node's own intensities).
+    template <class PointVec>
+    void lidarToBody(PointVec& out) { outputCloud(0, out); }
+    template <class PointVec>
+    void lidarToWorld(PointVec& out) { outputCloud(1, out); }
+
     // kf::IESKF::x() / P() equivalents (ieskf.h:86-90), row-major.
     const vmp_state& x() const { return res_.x; }
     const double* P() const { return res_.P; }
@@ -107,7 +118,27 @@ public:
     LIOStatus status = IMU_INIT;
 
 private:
+    template <class PointVec>
+    void outputCloud(int frame, PointVec& out) {
+        int n = 0;
+        vmp_status st = vmp_output_cloud(s_, frame, nullptr, nullptr, 0, &n);
+        if (st != VMP_OK) throw std::runtime_error(std::string("vmp_output_cloud: ") + vmp_last_error(s_));
+        cloud_.resize(static_cast<size_t>(n));
+        inten_.resize(static_cast<size_t>(n));
+        if (n > 0) vmp_output_cloud(s_, frame, cloud_.data(), inten_.data(), n, &n);
+        out.resize(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) {
+            out[i].x = cloud_[i].x;
+            out[i].y = cloud_[i].y;
+            out[i].z = cloud_[i].z;
+            out[i].intensity = inten_[i];
+            out[i].curvature = cloud_[i].t_ms;
+        }
+    }
+
     vmp_stream_t s_ = nullptr;
+    std::vector<vmp_point> cloud_;
+    std::vector<float> inten_;
     vmp_result res_{};
     std::vector<vmp_point> pts_;
     std::vector<vmp_imu> imus_;

@@ -33,7 +33,10 @@ int main() {
     for (int i = 0; i < 25; ++i) p.imus.push_back(Imu{{{0, 0, 9.81}}, {{0, 0, 0}}, 0.005 * i});
     p.cloud_end_time = 0.05;
     b.process(p);
-    std::printf("ok %d\n", (int)b.status);
+    std::vector<Pt> body, world;
+    b.lidarToBody(body);
+    b.lidarToWorld(world);
+    std::printf("ok %d %zu %zu\n", (int)b.status, body.size(), world.size());
     return 0;
 }
 '''

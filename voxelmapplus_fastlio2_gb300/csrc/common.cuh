@@ -153,6 +153,7 @@ struct DMap {
     // counters (device)
     struct Counters* cnt;
     double voxel_size;
+    double voxel_inv;  // 1 / voxel_size when that is a power of two (then exact), else 0
     int update_thresh;
     int max_thresh;
     double plane_thresh;
@@ -217,10 +218,13 @@ __device__ inline uint32_t map_find(const DMap& m, uint64_t key) {
 }
 
 // VoxelMap::index (voxel_map.cpp:194-198): floor(p / voxel_size) in FP64.
-__device__ inline bool voxel_index(const double p[3], double vs, int64_t k[3]) {
+// With a power-of-two voxel size (the 0.5 m default) the quotient is the
+// product with the exact reciprocal -- the same correctly rounded value --
+// and the FP64 division (a ~10-instruction sequence) is skipped.
+__device__ inline bool voxel_index(const double p[3], double vs, double inv, int64_t k[3]) {
     bool ok = true;
     for (int a = 0; a < 3; ++a) {
-        double f = floor(__ddiv_rn(p[a], vs));
+        double f = floor(inv != 0.0 ? p[a] * inv : __ddiv_rn(p[a], vs));
         if (!(f >= -(double)kKeyOff && f < (double)kKeyOff)) { ok = false; f = 0.0; }
         k[a] = (int64_t)f;
     }

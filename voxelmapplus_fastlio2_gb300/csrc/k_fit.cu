@@ -7,21 +7,21 @@
 //   FP32C  FP32 with compensated covariance sums: each point is taken
 //          relative to its voxel's first point (a float subtraction of two
 //          nearby values, free of cancellation error) and the sums of the
-//          coordinates and of their products are TwoSum-compensated
-//          (Knuth's error-free addition); the plane terms use the same
-//          relative coordinates.
+//          coordinates and of their products are compensated (Kahan's
+//          summation per lane, Knuth's error-free TwoSum where lanes
+//          combine); the plane terms use the same relative coordinates.
 //
-// Three launches per call:
-//   k_fit_sums   one warp per voxel: sums of p and p p^T (lane-strided, four
-//                points per lane in flight), reduced across the warp by a
-//                transpose reduction (16 shuffles for 9 sums instead of 45);
-//                the sums are parked in the record's plane_cov slots.
-//   k_fit_eig    one thread per voxel: mean, C = ppt / n - mean mean^T, the
-//                eigen decomposition, the plane test, the normal's sign flip
-//                and the per-voxel factors of J (parked in plane_cov).
-//   k_fit_terms  one warp per plane voxel: the per-point terms of
-//                J cov J^T in factored form, reduced like the sums; lane
-//                e < 21 forms entry e of the 6x6 and writes it.
+// One launch per call (k_fit): a warp fits 32 consecutive voxels --
+//   pass 1   voxel by voxel over all lanes: sums of p and p p^T
+//            (lane-strided, four points per lane in flight), reduced across
+//            the warp by a transpose reduction (16 shuffles for 9 sums
+//            instead of 45) and handed to the lane that owns the voxel;
+//   finalize one voxel per lane: mean, C = ppt / n - mean mean^T, the eigen
+//            decomposition, the plane test, the normal's sign flip, the
+//            per-voxel factors of J;
+//   pass 2   voxel by voxel again for the planes: the per-point terms of
+//            J cov J^T in factored form, reduced like the sums; lane e < 21
+//            forms entry e of the 6x6 and writes it.
 //
 // Factored J cov J^T.  With evecs E = [n v1 v2], d = p - mean, a = n . d,
 // b_m = v_m . d and k_m = 1 / (n_pts (l0 - l_m)), row m of updatePlane's F is
@@ -70,20 +70,22 @@ __device__ __forceinline__ double shx(double v, int o) { return __shfl_xor_sync(
 __device__ __forceinline__ F2 shx(F2 v, int o) { return {shx(v.s, o), shx(v.c, o)}; }
 __device__ __forceinline__ float comb(float a, float b) { return a + b; }
 __device__ __forceinline__ double comb(double a, double b) { return a + b; }
+// Combines two Kahan sums (c holds the negated error): TwoSum of the values.
 __device__ __forceinline__ F2 comb(F2 a, F2 b) {
     float s, e;
     two_sum(a.s, b.s, s, e);
-    return {s, (a.c + b.c) + e};
+    return {s, (a.c + b.c) - e};
 }
+// Kahan's compensated summation step: c carries the negated lost low part.
 __device__ __forceinline__ void acc_add(F2& a, float v) {
-    float s, e;
-    two_sum(a.s, v, s, e);
-    a.s = s;
-    a.c += e;
+    const float y = v - a.c;
+    const float t = a.s + y;
+    a.c = (t - a.s) - y;
+    a.s = t;
 }
 __device__ __forceinline__ double as_double(float v) { return (double)v; }
 __device__ __forceinline__ double as_double(double v) { return v; }
-__device__ __forceinline__ double as_double(F2 v) { return (double)v.s + (double)v.c; }
+__device__ __forceinline__ double as_double(F2 v) { return (double)v.s - (double)v.c; }
 template <class V> __device__ __forceinline__ V vzero() { return V(0); }
 template <> __device__ __forceinline__ F2 vzero<F2>() { return {0.f, 0.f}; }
 
@@ -129,107 +131,91 @@ __device__ __forceinline__ void voxel_range(const FitArgs& a, long long v, long 
     p1 = p1 < p0 ? p0 : (p1 > a.n_pts ? a.n_pts : p1);
 }
 
-// ---------------------------------------------------------------- sums
+// ---------------------------------------------------------------- one voxel
+// Pass 1 over voxel [p0, p1): sums of p and p p^T (FP32C: of p - anchor),
+// lane-strided with four points per lane in flight, reduced across the
+// warp; afterwards lanes red_lane(k) hold sum k (as a double).
 template <int MODE>
-__global__ void __launch_bounds__(kFitWarps * 32) k_fit_sums(FitArgs a) {
+__device__ __forceinline__ double voxel_sums(const FitArgs& a, long long p0, long long p1, float ax, float ay,
+                                             float az, int lane) {
     using T = typename FitTypes<MODE>::T;
     using Acc = typename FitTypes<MODE>::Acc;
-    const int lane = threadIdx.x & 31;
-    const long long v = (long long)blockIdx.x * kFitWarps + (threadIdx.x >> 5);
-    if (v >= a.n_vox) return;  // uniform per warp
-    long long p0, p1;
-    voxel_range(a, v, p0, p1);
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    if (MODE == FIT_FP32C && p1 > p0) {
-        ax = a.x[p0];
-        ay = a.y[p0];
-        az = a.z[p0];
-    }
     Acc acc[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) acc[k] = vzero<Acc>();
-    for (long long i = p0 + lane; i < p1; i += 128) {
+    auto add = [&](float px, float py, float pz) {
+        if constexpr (MODE == FIT_FP32C) {
+            const float dx = px - ax, dy = py - ay, dz = pz - az;
+            acc_add(acc[0], dx);
+            acc_add(acc[1], dy);
+            acc_add(acc[2], dz);
+            acc_add(acc[3], dx * dx);
+            acc_add(acc[4], dx * dy);
+            acc_add(acc[5], dx * dz);
+            acc_add(acc[6], dy * dy);
+            acc_add(acc[7], dy * dz);
+            acc_add(acc[8], dz * dz);
+        } else {
+            const T x = (T)px, y = (T)py, z = (T)pz;
+            acc[0] += x;
+            acc[1] += y;
+            acc[2] += z;
+            acc[3] = mad(x, x, acc[3]);
+            acc[4] = mad(x, y, acc[4]);
+            acc[5] = mad(x, z, acc[5]);
+            acc[6] = mad(y, y, acc[6]);
+            acc[7] = mad(y, z, acc[7]);
+            acc[8] = mad(z, z, acc[8]);
+        }
+    };
+    // four points per lane in flight while a whole round of 128 remains,
+    // then one at a time (no predicated-off work for small voxels)
+    long long i = p0 + lane;
+    for (; i + 96 < p1; i += 128) {
         float px[4], py[4], pz[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const long long k = i + 32 * u;
-            const bool ok = k < p1;
-            px[u] = ok ? __ldg(a.x + k) : 0.f;
-            py[u] = ok ? __ldg(a.y + k) : 0.f;
-            pz[u] = ok ? __ldg(a.z + k) : 0.f;
+            px[u] = __ldg(a.x + i + 32 * u);
+            py[u] = __ldg(a.y + i + 32 * u);
+            pz[u] = __ldg(a.z + i + 32 * u);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (i + 32 * u >= p1) break;
-            if constexpr (MODE == FIT_FP32C) {
-                const float dx = px[u] - ax, dy = py[u] - ay, dz = pz[u] - az;
-                acc_add(acc[0], dx);
-                acc_add(acc[1], dy);
-                acc_add(acc[2], dz);
-                acc_add(acc[3], dx * dx);
-                acc_add(acc[4], dx * dy);
-                acc_add(acc[5], dx * dz);
-                acc_add(acc[6], dy * dy);
-                acc_add(acc[7], dy * dz);
-                acc_add(acc[8], dz * dz);
-            } else {
-                const T x = (T)px[u], y = (T)py[u], z = (T)pz[u];
-                acc[0] += x;
-                acc[1] += y;
-                acc[2] += z;
-                acc[3] = mad(x, x, acc[3]);
-                acc[4] = mad(x, y, acc[4]);
-                acc[5] = mad(x, z, acc[5]);
-                acc[6] = mad(y, y, acc[6]);
-                acc[7] = mad(y, z, acc[7]);
-                acc[8] = mad(z, z, acc[8]);
-            }
-        }
+        for (int u = 0; u < 4; ++u) add(px[u], py[u], pz[u]);
     }
+    for (; i < p1; i += 32) add(__ldg(a.x + i), __ldg(a.y + i), __ldg(a.z + i));
     transpose_reduce16(acc, lane);
-    const int k = red_index(lane);
-    if ((lane & 1) == 0 && k < 9) a.out[v].plane_cov[k] = as_double(acc[0]);
+    return as_double(acc[0]);
 }
 
-// ---------------------------------------------------------------- eigen
-// Parked per-voxel factors for k_fit_terms (plane_cov slots 0..14): the mean
-// the points are taken relative to (FP32C: relative to the first point),
-// the unflipped normal, v1, v2, k1, k2, 1 / n.
+// The per-voxel step of updatePlane from the sums: mean, C, eigen
+// decomposition, plane test, sign flip; writes the record's fields except
+// the plane covariance of a plane, and returns the factors of J for pass 2
+// in kc: the mean the points are taken relative to (FP32C: relative to the
+// first point), the unflipped normal, v1, v2, k1, k2, 1 / n.
 template <int MODE>
-__global__ void k_fit_eig(FitArgs a) {
+__device__ int voxel_finalize(const FitArgs& a, const double* S, int n, const float* anchor, vmp_fit_rec& r,
+                              typename FitTypes<MODE>::T* kc) {
     using T = typename FitTypes<MODE>::T;
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= a.n_vox) return;
-    vmp_fit_rec& r = a.out[v];
-    long long p0, p1;
-    voxel_range(a, v, p0, p1);
-    const int n = (int)(p1 - p0);
-    double S[9];
-    for (int k = 0; k < 9; ++k) S[k] = r.plane_cov[k];
-    for (int k = 0; k < 21; ++k) r.plane_cov[k] = 0.0;
-    for (int k = 0; k < 3; ++k) r.norm[k] = 0.0;
     r.n = n;
-    r.flags = 0;
+    for (int k = 0; k < 3; ++k) r.norm[k] = 0.0;
+    for (int k = 0; k < 21; ++k) r.plane_cov[k] = 0.0;
     if (n <= 0) {
         for (int k = 0; k < 3; ++k) r.mean[k] = 0.0, r.evals[k] = 0.0;
         for (int k = 0; k < 6; ++k) r.cov[k] = 0.0;
-        return;
+        r.flags = 0;
+        return 0;
     }
     const T tn = (T)n;
-    T m[3];  // mean, relative to the first point in FP32C
+    T m[3];
     for (int k = 0; k < 3; ++k) m[k] = (T)S[k] / tn;
     double mean[3];
-    if (MODE == FIT_FP32C) {
-        const double anchor[3] = {(double)a.x[p0], (double)a.y[p0], (double)a.z[p0]};
-        for (int k = 0; k < 3; ++k) mean[k] = anchor[k] + (double)m[k];
-    } else {
-        for (int k = 0; k < 3; ++k) mean[k] = (double)m[k];
-    }
+    for (int k = 0; k < 3; ++k) mean[k] = MODE == FIT_FP32C ? (double)anchor[k] + (double)m[k] : (double)m[k];
     for (int k = 0; k < 3; ++k) r.mean[k] = mean[k];
     if (n < a.min_pts) {
         for (int k = 0; k < 3; ++k) r.evals[k] = 0.0;
         for (int k = 0; k < 6; ++k) r.cov[k] = 0.0;
-        return;
+        r.flags = 0;
+        return 0;
     }
     // C = ppt / n - mean mean^T (upper triangle mirrored)
     constexpr int kU[3][3] = {{3, 4, 5}, {4, 6, 7}, {5, 7, 8}};
@@ -248,7 +234,7 @@ __global__ void k_fit_eig(FitArgs a) {
     int flags = VMP_FIT_FITTED;
     if ((double)ev[0] > a.plane_thresh) {
         r.flags = flags;
-        return;
+        return flags;
     }
     flags |= VMP_FIT_PLANE;
     const T pn[3] = {E[0], E[3], E[6]};
@@ -261,148 +247,194 @@ __global__ void k_fit_eig(FitArgs a) {
     }
     if (flip) flags |= VMP_FIT_FLIPPED;
     for (int k = 0; k < 3; ++k) r.norm[k] = flip ? -(double)pn[k] : (double)pn[k];
-    double* pk = r.plane_cov;
     for (int k = 0; k < 3; ++k) {
-        pk[k] = (double)m[k];
-        pk[3 + k] = (double)pn[k];
-        pk[6 + k] = (double)E[k * 3 + 1];
-        pk[9 + k] = (double)E[k * 3 + 2];
+        kc[k] = m[k];
+        kc[3 + k] = pn[k];
+        kc[6 + k] = E[k * 3 + 1];
+        kc[9 + k] = E[k * 3 + 2];
     }
-    pk[12] = (double)(T(1) / (tn * (ev[0] - ev[1])));
-    pk[13] = (double)(T(1) / (tn * (ev[0] - ev[2])));
-    pk[14] = (double)(T(1) / tn);
+    kc[12] = T(1) / (tn * (ev[0] - ev[1]));
+    kc[13] = T(1) / (tn * (ev[0] - ev[2]));
+    kc[14] = T(1) / tn;
     r.flags = flags;
+    return flags;
 }
 
-// ---------------------------------------------------------------- terms
+// Pass 2 over a plane voxel: the factored J cov J^T terms, reduced across
+// the warp; lane e < 21 forms entry e of the 6x6 and writes it.
 template <int MODE>
-__global__ void __launch_bounds__(kFitWarps * 32) k_fit_terms(FitArgs a) {
+__device__ __forceinline__ void voxel_terms(const FitArgs& a, long long p0, long long p1, float ax, float ay,
+                                            float az, const typename FitTypes<MODE>::T* kc, int lane,
+                                            double* plane_cov) {
     using T = typename FitTypes<MODE>::T;
-    const int lane = threadIdx.x & 31;
-    const long long v = (long long)blockIdx.x * kFitWarps + (threadIdx.x >> 5);
-    if (v >= a.n_vox) return;
-    vmp_fit_rec& r = a.out[v];
-    if (!(r.flags & VMP_FIT_PLANE)) return;  // uniform per warp
-    const double* pk = r.plane_cov;
-    T m[3], nn[3], v1[3], v2[3];
-    for (int k = 0; k < 3; ++k) {
-        m[k] = (T)pk[k];
-        nn[k] = (T)pk[3 + k];
-        v1[k] = (T)pk[6 + k];
-        v2[k] = (T)pk[9 + k];
-    }
-    const T k1 = (T)pk[12], k2 = (T)pk[13], inv_n = (T)pk[14];
-    long long p0, p1;
-    voxel_range(a, v, p0, p1);
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    if (MODE == FIT_FP32C) {
-        ax = a.x[p0];
-        ay = a.y[p0];
-        az = a.z[p0];
-    }
+    const T m[3] = {kc[0], kc[1], kc[2]};
+    const T nn[3] = {kc[3], kc[4], kc[5]};
+    const T v1[3] = {kc[6], kc[7], kc[8]};
+    const T v2[3] = {kc[9], kc[10], kc[11]};
+    const T k1 = kc[12], k2 = kc[13], inv_n = kc[14];
     T acc[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) acc[k] = T(0);
-    for (long long i = p0 + lane; i < p1; i += 128) {
-        float px[4], py[4], pz[4], pc[4][6];
+    auto add = [&](float px, float py, float pz, const float* pc) {
+        T d[3];
+        if constexpr (MODE == FIT_FP32C) {
+            d[0] = (px - ax) - m[0];
+            d[1] = (py - ay) - m[1];
+            d[2] = (pz - az) - m[2];
+        } else {
+            d[0] = (T)px - m[0];
+            d[1] = (T)py - m[1];
+            d[2] = (T)pz - m[2];
+        }
+        const T an = mad(nn[2], d[2], mad(nn[1], d[1], nn[0] * d[0]));
+        const T b1 = mad(v1[2], d[2], mad(v1[1], d[1], v1[0] * d[0]));
+        const T b2 = mad(v2[2], d[2], mad(v2[1], d[1], v2[0] * d[0]));
+        T f1[3], f2[3];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int q = 0; q < 3; ++q) {
+            f1[q] = k1 * mad(an, v1[q], b1 * nn[q]);
+            f2[q] = k2 * mad(an, v2[q], b2 * nn[q]);
+        }
+        const T c00 = (T)pc[0], c01 = (T)pc[1], c02 = (T)pc[2], c11 = (T)pc[3], c12 = (T)pc[4], c22 = (T)pc[5];
+        T g1[3], g2[3];
+        g1[0] = mad(c02, f1[2], mad(c01, f1[1], c00 * f1[0]));
+        g1[1] = mad(c12, f1[2], mad(c11, f1[1], c01 * f1[0]));
+        g1[2] = mad(c22, f1[2], mad(c12, f1[1], c02 * f1[0]));
+        g2[0] = mad(c02, f2[2], mad(c01, f2[1], c00 * f2[0]));
+        g2[1] = mad(c12, f2[2], mad(c11, f2[1], c01 * f2[0]));
+        g2[2] = mad(c22, f2[2], mad(c12, f2[1], c02 * f2[0]));
+        acc[0] += mad(f1[2], g1[2], mad(f1[1], g1[1], f1[0] * g1[0]));
+        acc[1] += mad(f1[2], g2[2], mad(f1[1], g2[1], f1[0] * g2[0]));
+        acc[2] += mad(f2[2], g2[2], mad(f2[1], g2[1], f2[0] * g2[0]));
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            acc[3 + q] += g1[q];
+            acc[6 + q] += g2[q];
+        }
+        acc[9] += c00;
+        acc[10] += c01;
+        acc[11] += c02;
+        acc[12] += c11;
+        acc[13] += c12;
+        acc[14] += c22;
+    };
+    long long i = p0 + lane;
+    for (; i + 32 < p1; i += 64) {  // two points per lane in flight (9 floats each)
+        float px[2], py[2], pz[2], pc[2][6];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
             const long long k = i + 32 * u;
-            const bool ok = k < p1;
-            px[u] = ok ? __ldg(a.x + k) : 0.f;
-            py[u] = ok ? __ldg(a.y + k) : 0.f;
-            pz[u] = ok ? __ldg(a.z + k) : 0.f;
+            px[u] = __ldg(a.x + k);
+            py[u] = __ldg(a.y + k);
+            pz[u] = __ldg(a.z + k);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) pc[u][q] = ok ? __ldg(a.c[q] + k) : 0.f;
+            for (int q = 0; q < 6; ++q) pc[u][q] = __ldg(a.c[q] + k);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (i + 32 * u >= p1) break;
-            T d[3];
-            if constexpr (MODE == FIT_FP32C) {
-                d[0] = (px[u] - ax) - m[0];
-                d[1] = (py[u] - ay) - m[1];
-                d[2] = (pz[u] - az) - m[2];
-            } else {
-                d[0] = (T)px[u] - m[0];
-                d[1] = (T)py[u] - m[1];
-                d[2] = (T)pz[u] - m[2];
-            }
-            const T an = mad(nn[2], d[2], mad(nn[1], d[1], nn[0] * d[0]));
-            const T b1 = mad(v1[2], d[2], mad(v1[1], d[1], v1[0] * d[0]));
-            const T b2 = mad(v2[2], d[2], mad(v2[1], d[1], v2[0] * d[0]));
-            T f1[3], f2[3];
+        for (int u = 0; u < 2; ++u) add(px[u], py[u], pz[u], pc[u]);
+    }
+    for (; i < p1; i += 32) {
+        float pc[6];
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                f1[q] = k1 * mad(an, v1[q], b1 * nn[q]);
-                f2[q] = k2 * mad(an, v2[q], b2 * nn[q]);
-            }
-            const T c00 = (T)pc[u][0], c01 = (T)pc[u][1], c02 = (T)pc[u][2], c11 = (T)pc[u][3],
-                    c12 = (T)pc[u][4], c22 = (T)pc[u][5];
-            T g1[3], g2[3];
-            g1[0] = mad(c02, f1[2], mad(c01, f1[1], c00 * f1[0]));
-            g1[1] = mad(c12, f1[2], mad(c11, f1[1], c01 * f1[0]));
-            g1[2] = mad(c22, f1[2], mad(c12, f1[1], c02 * f1[0]));
-            g2[0] = mad(c02, f2[2], mad(c01, f2[1], c00 * f2[0]));
-            g2[1] = mad(c12, f2[2], mad(c11, f2[1], c01 * f2[0]));
-            g2[2] = mad(c22, f2[2], mad(c12, f2[1], c02 * f2[0]));
-            acc[0] += mad(f1[2], g1[2], mad(f1[1], g1[1], f1[0] * g1[0]));
-            acc[1] += mad(f1[2], g2[2], mad(f1[1], g2[1], f1[0] * g2[0]));
-            acc[2] += mad(f2[2], g2[2], mad(f2[1], g2[1], f2[0] * g2[0]));
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                acc[3 + q] += g1[q];
-                acc[6 + q] += g2[q];
-            }
-            acc[9] += c00;
-            acc[10] += c01;
-            acc[11] += c02;
-            acc[12] += c11;
-            acc[13] += c12;
-            acc[14] += c22;
-        }
+        for (int q = 0; q < 6; ++q) pc[q] = __ldg(a.c[q] + i);
+        add(__ldg(a.x + i), __ldg(a.y + i), __ldg(a.z + i), pc);
     }
     transpose_reduce16(acc, lane);
     // lane e < 21 forms entry e = (i, j), i <= j, row by row
-    int i = 0, j = 0;
+    int ei = 0, ej = 0;
     {
         int e = lane < 21 ? lane : 0, row = 0, len = 6;
         while (e >= len) { e -= len; ++row; --len; }
-        i = row;
-        j = row + e;
+        ei = row;
+        ej = row + e;
     }
     const T s11 = __shfl_sync(0xffffffffu, acc[0], red_lane(0));
     const T s12 = __shfl_sync(0xffffffffu, acc[0], red_lane(1));
     const T s22 = __shfl_sync(0xffffffffu, acc[0], red_lane(2));
-    const int jc = j >= 3 ? j - 3 : j;
+    const int jc = ej >= 3 ? ej - 3 : ej;
     const T g1j = __shfl_sync(0xffffffffu, acc[0], red_lane(3 + jc));
     const T g2j = __shfl_sync(0xffffffffu, acc[0], red_lane(6 + jc));
     int ss = 0;
-    if (i >= 3) {
-        const int a3 = i - 3, b3 = j - 3;  // index in xx xy xz yy yz zz
+    if (ei >= 3) {
+        const int a3 = ei - 3, b3 = ej - 3;  // index in xx xy xz yy yz zz
         ss = a3 == 0 ? b3 : (a3 == 1 ? 2 + b3 : 5);
     }
     const T sij = __shfl_sync(0xffffffffu, acc[0], red_lane(9 + ss));
     if (lane < 21) {
         T val;
-        if (j < 3) {
-            val = s11 * v1[i] * v1[j] + s12 * (v1[i] * v2[j] + v2[i] * v1[j]) + s22 * v2[i] * v2[j];
-        } else if (i < 3) {
-            val = (v1[i] * g1j + v2[i] * g2j) * inv_n;
+        if (ej < 3) {
+            val = s11 * v1[ei] * v1[ej] + s12 * (v1[ei] * v2[ej] + v2[ei] * v1[ej]) + s22 * v2[ei] * v2[ej];
+        } else if (ei < 3) {
+            val = (v1[ei] * g1j + v2[ei] * g2j) * inv_n;
         } else {
             val = sij * inv_n * inv_n;
         }
-        r.plane_cov[lane] = (double)val;
+        plane_cov[lane] = (double)val;
     }
 }
 
-// Measurement hook (vmp_fit_profile): CUDA events around each kernel, the
-// call waits for them and adds up the per-kernel device time.
+// ---------------------------------------------------------------- the fit
+// One warp fits 32 consecutive voxels: their offsets and anchors are loaded
+// by one lane each (coalesced), pass 1 runs voxel by voxel over all lanes and
+// hands each voxel's sums to the lane that owns it, the 32 eigen
+// decompositions run one per lane, and pass 2 runs voxel by voxel again
+// (the points of the 32 voxels were just read: their xyz mostly comes from
+// L2).
+template <int MODE>
+__global__ void __launch_bounds__(kFitWarps * 32, MODE == FIT_FP64 ? 1 : 3) k_fit(FitArgs a) {
+    using T = typename FitTypes<MODE>::T;
+    const int lane = threadIdx.x & 31;
+    const long long v0 = ((long long)blockIdx.x * kFitWarps + (threadIdx.x >> 5)) * 32;
+    if (v0 >= a.n_vox) return;  // uniform per warp
+    const int nb = (int)(a.n_vox - v0 < 32 ? a.n_vox - v0 : 32);
+    long long mp0 = 0, mp1 = 0;
+    float anc[3] = {0.f, 0.f, 0.f};
+    if (lane < nb) {
+        voxel_range(a, v0 + lane, mp0, mp1);
+        if (MODE == FIT_FP32C && mp1 > mp0) {
+            anc[0] = a.x[mp0];
+            anc[1] = a.y[mp0];
+            anc[2] = a.z[mp0];
+        }
+    }
+    double S[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S[k] = 0.0;
+    for (int j = 0; j < nb; ++j) {
+        const long long p0 = __shfl_sync(0xffffffffu, mp0, j), p1 = __shfl_sync(0xffffffffu, mp1, j);
+        const float ax = __shfl_sync(0xffffffffu, anc[0], j), ay = __shfl_sync(0xffffffffu, anc[1], j),
+                    az = __shfl_sync(0xffffffffu, anc[2], j);
+        const double tot = voxel_sums<MODE>(a, p0, p1, ax, ay, az, lane);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const double t = __shfl_sync(0xffffffffu, tot, red_lane(k));
+            if (lane == j) S[k] = t;
+        }
+    }
+    T kc[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) kc[k] = T(0);
+    int fl = 0;
+    if (lane < nb) fl = voxel_finalize<MODE>(a, S, (int)(mp1 - mp0), anc, a.out[v0 + lane], kc);
+    for (int j = 0; j < nb; ++j) {
+        if (!(__shfl_sync(0xffffffffu, fl, j) & VMP_FIT_PLANE)) continue;  // uniform
+        T kj[15];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) kj[k] = __shfl_sync(0xffffffffu, kc[k], j);
+        const long long p0 = __shfl_sync(0xffffffffu, mp0, j), p1 = __shfl_sync(0xffffffffu, mp1, j);
+        const float ax = __shfl_sync(0xffffffffu, anc[0], j), ay = __shfl_sync(0xffffffffu, anc[1], j),
+                    az = __shfl_sync(0xffffffffu, anc[2], j);
+        voxel_terms<MODE>(a, p0, p1, ax, ay, az, kj, lane, a.out[v0 + j].plane_cov);
+    }
+}
+
+// Measurement hook (vmp_fit_profile): CUDA events around the fit kernel; the
+// call waits for them and adds up its device time.
 struct FitProfile {
     std::mutex mu;
     bool on = false;
-    cudaEvent_t ev[4] = {};
-    double ms[3] = {};
+    cudaEvent_t ev[2] = {};
+    double ms = 0.0;
     long long calls = 0;
 };
 FitProfile& fit_profile() {
@@ -412,15 +444,10 @@ FitProfile& fit_profile() {
 
 template <int MODE>
 void launch_mode(const FitArgs& a, cudaStream_t st, cudaEvent_t* ev) {
-    const unsigned wgrid = (unsigned)((a.n_vox + kFitWarps - 1) / kFitWarps);
-    const unsigned tgrid = (unsigned)((a.n_vox + 255) / 256);
+    const unsigned grid = (unsigned)((a.n_vox + 32 * kFitWarps - 1) / (32 * kFitWarps));
     if (ev) cudaEventRecord(ev[0], st);
-    VMP_NOTE_LAUNCH(); k_fit_sums<MODE><<<wgrid, kFitWarps * 32, 0, st>>>(a);
+    VMP_NOTE_LAUNCH(); k_fit<MODE><<<grid, kFitWarps * 32, 0, st>>>(a);
     if (ev) cudaEventRecord(ev[1], st);
-    VMP_NOTE_LAUNCH(); k_fit_eig<MODE><<<tgrid, 256, 0, st>>>(a);
-    if (ev) cudaEventRecord(ev[2], st);
-    VMP_NOTE_LAUNCH(); k_fit_terms<MODE><<<wgrid, kFitWarps * 32, 0, st>>>(a);
-    if (ev) cudaEventRecord(ev[3], st);
 }
 
 bool params_ok(const vmp_fit_params* p) {
@@ -457,12 +484,10 @@ cudaError_t fit_enqueue(const float* xyz, const float* cov, const long long* off
         default: launch_mode<FIT_FP32C>(a, st, ev); break;
     }
     cudaError_t e = cudaGetLastError();
-    if (ev && e == cudaSuccess && (e = cudaEventSynchronize(ev[3])) == cudaSuccess) {
-        for (int k = 0; k < 3; ++k) {
-            float t = 0.f;
-            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
-            prof.ms[k] += t;
-        }
+    if (ev && e == cudaSuccess && (e = cudaEventSynchronize(ev[1])) == cudaSuccess) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[0], ev[1]);
+        prof.ms += t;
         ++prof.calls;
     }
     return e;
@@ -539,7 +564,7 @@ extern "C" vmp_status vmp_fit_profile(int on) {
     FitProfile& p = fit_profile();
     std::lock_guard<std::mutex> lk(p.mu);
     p.on = on != 0;
-    for (double& m : p.ms) m = 0.0;
+    p.ms = 0.0;
     p.calls = 0;
     return VMP_OK;
 }
@@ -547,8 +572,7 @@ extern "C" vmp_status vmp_fit_profile(int on) {
 extern "C" vmp_status vmp_fit_profile_read(double* ms, long long* calls) {
     FitProfile& p = fit_profile();
     std::lock_guard<std::mutex> lk(p.mu);
-    if (ms)
-        for (int k = 0; k < 3; ++k) ms[k] = p.ms[k];
+    if (ms) *ms = p.ms;
     if (calls) *calls = p.calls;
     return VMP_OK;
 }

@@ -51,7 +51,7 @@ __device__ inline void residual_point(int i, const DScan& s, const DMap& m, cons
     m3v(rwl, pl, pw);
     for (int a = 0; a < 3; ++a) pw[a] = pw[a] + pwl[a];
     int64_t key[3];
-    const bool inr = voxel_index(pw, m.voxel_size, key);
+    const bool inr = voxel_index(pw, m.voxel_size, m.voxel_inv, key);
     const uint32_t rec = inr ? map_find(m, pack_key(key[0], key[1], key[2])) : kNoRec;
     const double* cl = s.covl + (size_t)i * 9;
     if (rec != kNoRec) {

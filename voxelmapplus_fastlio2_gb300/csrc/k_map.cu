@@ -41,7 +41,7 @@ __global__ void k_lookup_insert(DMap m, const double* __restrict__ bpts, const i
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double p[3] = {bpts[i * 3], bpts[i * 3 + 1], bpts[i * 3 + 2]};
         int64_t k[3];
-        if (!voxel_index(p, m.voxel_size, k)) {
+        if (!voxel_index(p, m.voxel_size, m.voxel_inv, k)) {
             set_error(m.cnt, E_KEY_RANGE);
             slot_out[i] = kNoRec;
             continue;

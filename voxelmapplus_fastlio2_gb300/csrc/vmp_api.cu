@@ -623,6 +623,11 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     m.chunk_pool = (int)chunks;
     m.q_cap = (uint64_t)(2 * pool + 2 * (long long)max_pts);
     m.voxel_size = cfg.voxel_size;
+    {
+        int e = 0;
+        const double mant = std::frexp(cfg.voxel_size, &e);
+        m.voxel_inv = mant == 0.5 ? std::ldexp(1.0, 1 - e) : 0.0;  // 2^(e-1) -> 2^(1-e)
+    }
     m.update_thresh = cfg.update_size_thresh;
     m.max_thresh = cfg.max_point_thresh;
     m.plane_thresh = cfg.plane_thresh;
