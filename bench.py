@@ -31,7 +31,11 @@ workload, one single-threaded oracle per stream, all host cores.
 
 `--workload urban|room` runs the plain one-stream path alone (value: HBM
 resident with per-step CUDA events and an L2 flush between steps; e2e: from
-pinned host buffers).
+pinned host buffers).  `--workload planefit` is the batched plane fit and its
+precision study (1 M voxels), `--workload corridor` the long-horizon stress
+(16 corridor streams under the LRU cap, drift against the oracle and the
+ground truth), `--workload io` the steps either side of the path (Livox
+decode, output clouds, plane-marker export, STD plane voxels).
 
 Multi-GPU: streams shard by GPU (each rank serves its own streams), no
 collective on the data path; "scaling": "weak".
@@ -74,7 +78,7 @@ def parse():
                     help="timed scans (per stream for the served workload; default 16 there, 60 otherwise)")
     ap.add_argument("--warmup", type=int, default=None, help="warm-up scans (default 3 served, 5 otherwise)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room", "planefit", "corridor"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room", "planefit", "corridor", "io"])
     ap.add_argument("--voxels", type=int, default=1_000_000, help="planefit workload: voxels per batch")
     ap.add_argument("--fit-mode", default="fp32c", choices=["fp64", "fp32", "fp32c"],
                     help="planefit workload: arithmetic mode of the headline value")
@@ -724,6 +728,115 @@ def main_corridor(args, rank, ws, barrier, allmax, dist):
         dist.destroy_process_group()
 
 
+IO_METRIC = "points/s: Livox decode, output clouds, plane-marker export, STD plane voxels (device vs CPU restatement)"
+
+
+def _wall(fn, reps):
+    t = time.perf_counter()
+    out = None
+    for _ in range(reps):
+        out = fn()
+    return (time.perf_counter() - t) / reps, out
+
+
+def main_io(args, rank, ws, barrier, allmax, dist):
+    """The steps either side of the path, through their public entry points
+    with host buffers (copies inside the timing), next to the CPU
+    restatement: livox2pcl on the urban sequence's messages, lidarToBody +
+    lidarToWorld of the undistorted cloud, the plane-marker walk of the map,
+    and STD plane voxels of a 10-scan key cloud."""
+    import oracle
+    from voxelmapplus_fastlio2_gb300 import abi, fit, lio
+    from voxelmapplus_fastlio2_gb300 import build as vbuild
+    if rank != 0:
+        return
+    kind, pts, cfg, seed, uname = workload(args, rank, "urban")
+    K = max(3, min(args.steps, 20))
+    pkgs = make_packages(kind, pts, seed, 2 + K)
+    rng = np.random.default_rng(3)
+    msgs = []
+    for p in pkgs:
+        a = pkg_arrays(p)[0]
+        m = np.zeros(p.n, dtype=abi.livox_dtype())
+        m["x"], m["y"], m["z"] = a[:, 0], a[:, 1], a[:, 2]
+        m["offset_time"] = np.rint(a[:, 3].astype(np.float64) * 1e6).astype(np.uint32)
+        m["reflectivity"] = rng.integers(0, 256, p.n)
+        m["tag"] = rng.choice(np.array([0x00, 0x10, 0x20], dtype=np.uint8), p.n, p=[0.6, 0.35, 0.05])
+        m["line"] = rng.choice(np.array([0, 1, 2, 3, 4], dtype=np.uint8), p.n, p=[0.24] * 4 + [0.04])
+        msgs.append(m)
+    ours = args.impl != "reference"
+    if ours:
+        vbuild.build_all()
+        g = lio.LIOBuilder(cfg)
+        l0 = g.lib.vmp_launch_count()
+    o = oracle.Oracle(cfg)
+    world, comp = [], {}
+    t_dec_g = t_dec_c = t_out_g = t_out_c = 0.0
+    n_dec = 0
+    for k, (p, m) in enumerate(zip(pkgs, msgs)):
+        t0 = time.perf_counter()
+        op, oi = oracle.livox_decode(m, 1, 0.1, 200.0)
+        t_dec_c += time.perf_counter() - t0
+        o.process_points(op, p.t_start, p.t_end, p.imus, p.n_imu, oi)
+        if ours:
+            t0 = time.perf_counter()
+            g.livox_decode(m, 1, 0.1, 200.0, copy_out=False)  # count and last time only, as the node needs
+            t_dec_g += time.perf_counter() - t0
+            g.process_decoded(p.t_start, p.t_end, p.imus, p.n_imu)
+        n_dec += len(op)
+        if k >= 2:
+            t0 = time.perf_counter()
+            cw, _ = o.output_cloud(1)
+            o.output_cloud(0)
+            t_out_c += time.perf_counter() - t0
+            world.append(cw)
+            if ours:
+                t0 = time.perf_counter()
+                g.output_cloud(1)
+                g.output_cloud(0)
+                t_out_g += time.perf_counter() - t0
+    n_in = sum(len(m) for m in msgs)
+    n_out = 2 * sum(len(w) for w in world)
+    key = np.ascontiguousarray(np.concatenate(world[-10:]))
+    comp["livox_decode"] = {"messages": len(msgs), "points_in": n_in, "points_kept": n_dec,
+                            "cpu_points_per_s": n_in / t_dec_c}
+    comp["output_clouds"] = {"points": n_out, "cpu_points_per_s": n_out / t_out_c}
+    mk = np.zeros(100000, dtype=abi.plane_marker_dtype())
+    tc, nm = _wall(lambda: o.lib.orc_map_planes(o.h, mk.ctypes.data_as(C.POINTER(abi.vmp_plane_marker)), 100000), 3)
+    info = abi.vmp_map_info()
+    o.lib.orc_map_info(o.h, C.byref(info))
+    comp["map_planes"] = {"map_voxels": int(info.size), "markers": int(nm), "cpu_ms": 1e3 * tc}
+    so = np.zeros(len(key), dtype=abi.std_voxel_dtype())
+    tc, ns = _wall(lambda: o.lib.orc_std_plane_voxels(key.ctypes.data_as(C.POINTER(C.c_float)), 4, len(key), 1.0, 10,
+                                                        0.01, so.ctypes.data_as(C.POINTER(abi.vmp_std_voxel)),
+                                                        len(key)), 2)
+    comp["std_plane_voxels"] = {"points": int(len(key)), "voxels": int(ns), "cpu_ms": 1e3 * tc}
+    base = {"metric": IO_METRIC, "unit": "points/s", "n_gpus": 1, "steps": K, "warmup": 2, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)"}
+    cfg_line = {"workload": uname + "; Livox messages made from its scans (20 B per point), key cloud = the last "
+                                    "10 world clouds", "components": comp}
+    cpu = {"value": n_in / t_dec_c, "unit": "points/s", "cores": 1, "kind": "port",
+           "sample": f"{len(msgs)} Livox messages, CPU restatement of livox2pcl on 1 thread"}
+    if not ours:
+        print(json.dumps(dict(base, value=cpu["value"], impl="reference", ms_per_step=1e3 * t_dec_c / len(msgs),
+                              config=cfg_line, cpu_baseline=cpu,
+                              e2e={"value": cpu["value"], "unit": "points/s", "h2d_bytes_per_step": 0,
+                                   "d2h_bytes_per_step": 0})))
+        return
+    tg, ng = _wall(lambda: g.map.planes(100000), 5)
+    comp["map_planes"].update({"gpu_ms": 1e3 * tg, "gpu_markers": int(len(ng))})
+    tg, gs = _wall(lambda: fit.std_plane_voxels(key, 1.0, 10, 0.01), 3)
+    comp["std_plane_voxels"].update({"gpu_ms": 1e3 * tg, "gpu_voxels": int(len(gs))})
+    comp["livox_decode"]["gpu_points_per_s"] = n_in / t_dec_g
+    comp["output_clouds"]["gpu_points_per_s"] = n_out / t_out_g
+    v = n_in / t_dec_g
+    print(json.dumps(dict(base, value=v, ms_per_step=1e3 * t_dec_g / len(msgs), config=cfg_line,
+                          e2e={"value": v, "unit": "points/s", "h2d_bytes_per_step": int(20 * n_in / len(msgs)),
+                               "d2h_bytes_per_step": 8},
+                          gpu_launches=int(g.lib.vmp_launch_count() - l0), cpu_baseline=cpu)))
+    g.close()
+
+
 PLANEFIT_METRIC = "voxels/s: batched plane fit (updatePlane over every voxel), FP32 compensated vs FP32 vs FP64"
 PLANEFIT_NAME = ("batched plane fit + precision study: {v} voxels of a 0.5 m grid over +-100 x +-100 x +-10 m, "
                  "points/voxel lognormal (median 40, sigma 1) clipped to [5, 4000], 1 cm normal noise, "
@@ -926,6 +1039,8 @@ def main():
         return main_planefit(args, rank, ws, barrier, allmax, dist)
     if args.workload == "corridor":
         return main_corridor(args, rank, ws, barrier, allmax, dist)
+    if args.workload == "io":
+        return main_io(args, rank, ws, barrier, allmax, dist)
     kind, pts, cfg, seed, wname = workload(args, rank)
     n_init = 2  # IMU_INIT + MAP_INIT packages
     if args.impl == "reference":

@@ -291,6 +291,33 @@ typedef struct vmp_plane_marker {
  * markers written. */
 vmp_status vmp_map_planes(vmp_stream_t s, vmp_plane_marker* out, int max, int* n_out);
 
+/* ---- plane voxels of a key cloud (loop closure) ----
+ * std_desc::STDManager::buildVoxels (std_matcher/src/std_manager/
+ * descriptor.cpp:70-122): the cloud voxelised at voxel_size
+ * (VoxelKey::index: floor(p / voxel_size), descriptor.cpp:44-49), per voxel
+ * the FP64 sum and sum of outer products of its points in cloud order, and
+ * for voxels with more than voxel_min_point points the mean, the eigen
+ * decomposition of C = ppt / n - mean mean^T and the plane test
+ * lambda_min < voxel_plane_thresh.  One record per voxel, in packed-key order
+ * (the reference iterates an unordered_map). */
+typedef struct vmp_std_voxel {
+    int64_t key[3];
+    int32_t n;         /* points in the voxel */
+    int32_t valid;     /* n > voxel_min_point: mean and decomposition formed */
+    int32_t is_plane;  /* valid and lambda_min < voxel_plane_thresh */
+    int32_t pad;
+    double sum[3];
+    double ppt[9];
+    double mean[3];    /* 0 unless valid */
+    double lamdas[3];  /* ascending; 0 unless is_plane */
+    double norms[9];   /* row-major, eigenvectors as columns in lamdas' order; 0 unless is_plane */
+} vmp_std_voxel;
+/* pts: n points of `stride` floats each, x y z first (stride 8 for
+ * pcl::PointXYZI, 4 for vmp_point).  out (host) holds max records; *n_out =
+ * voxels of the cloud.  Allocates and frees device memory per call. */
+vmp_status vmp_std_plane_voxels(const float* pts, int stride, int n, double voxel_size, int voxel_min_point,
+                                double voxel_plane_thresh, vmp_std_voxel* out, int max, int* n_out);
+
 /* The same leaf-centroid downsample for callers that cannot allocate device
  * memory (no counterpart in the reference): a real-time sensor thread that
  * must not call cudaMalloc/cudaFree, or a host framework whose own allocator

@@ -65,6 +65,9 @@ def load():
     lib.orc_output_cloud.restype = C.c_int
     lib.orc_map_planes.argtypes = [vp, P(abi.vmp_plane_marker), C.c_int]
     lib.orc_map_planes.restype = C.c_int
+    lib.orc_std_plane_voxels.argtypes = [P(C.c_float), C.c_int, C.c_int, d, C.c_int, d, P(abi.vmp_std_voxel),
+                                         C.c_int]
+    lib.orc_std_plane_voxels.restype = C.c_int
     lib.orc_fit_planes.argtypes = [P(C.c_float), P(C.c_float), P(C.c_longlong), C.c_int, C.c_longlong, C.c_int, d,
                                    P(abi.vmp_fit_rec), C.c_int]
     lib.orc_downsample.restype = C.c_int

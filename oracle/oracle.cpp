@@ -36,6 +36,8 @@
 #include <cstdio>
 #include <cstring>
 #include <list>
+#include <tuple>
+#include <map>
 #include <memory>
 #include <unordered_map>
 #include <vector>
@@ -1191,6 +1193,55 @@ int orc_map_planes(void* h, vmp_plane_marker* out, int max) {
         quatFromTwoVectors(v3(0, 0, 1), g->plane.norm, o.orientation);
     }
     return count;
+}
+
+// std_desc::STDManager::buildVoxels (std_matcher/src/std_manager/
+// descriptor.cpp:70-122): voxels of the cloud (VoxelKey::index with bias 0,
+// descriptor.cpp:44-49), FP64 sum and outer-product sum in cloud order, and
+// for voxels with more than min_point points the mean, the decomposition of
+// C (eigSym3: the symmetric restatement; the reference's general EigenSolver
+// gives the same eigenvalues of a symmetric matrix up to rounding) and the
+// plane test.  Records in ascending (z, y, x) key order.
+int orc_std_plane_voxels(const float* pts, int stride, int n, double voxel_size, int min_point, double plane_thresh,
+                         vmp_std_voxel* out, int max) {
+    struct Acc { int n = 0; V3 sum = V3::Zero(); M3 ppt = M3::Zero(); };
+    std::map<std::tuple<int64_t, int64_t, int64_t>, Acc> vox;
+    for (int i = 0; i < n; ++i) {
+        const V3 p = v3(pts[(size_t)i * stride], pts[(size_t)i * stride + 1], pts[(size_t)i * stride + 2]);
+        const int64_t kx = (int64_t)std::floor(p[0] / voxel_size + 0.0);
+        const int64_t ky = (int64_t)std::floor(p[1] / voxel_size + 0.0);
+        const int64_t kz = (int64_t)std::floor(p[2] / voxel_size + 0.0);
+        Acc& a = vox[std::make_tuple(kz, ky, kx)];
+        a.n += 1;
+        a.sum += p;
+        a.ppt += p * T(p);
+    }
+    int m = 0;
+    for (auto& kv : vox) {
+        if (m >= max) break;
+        vmp_std_voxel& o = out[m++];
+        std::memset(&o, 0, sizeof(o));
+        o.key[0] = std::get<2>(kv.first);
+        o.key[1] = std::get<1>(kv.first);
+        o.key[2] = std::get<0>(kv.first);
+        const Acc& a = kv.second;
+        o.n = a.n;
+        for (int k = 0; k < 3; ++k) o.sum[k] = a.sum[k];
+        for (int k = 0; k < 9; ++k) o.ppt[k] = a.ppt[k];
+        if (a.n <= min_point) continue;
+        o.valid = 1;
+        const V3 mean = a.sum / static_cast<double>(a.n);
+        const M3 C = a.ppt / static_cast<double>(a.n) - mean * T(mean);
+        V3 ev; M3 E;
+        eigSym3(C, ev, E);
+        for (int k = 0; k < 3; ++k) o.mean[k] = mean[k];
+        if (ev[0] < plane_thresh) {
+            o.is_plane = 1;
+            for (int k = 0; k < 3; ++k) o.lamdas[k] = ev[k];
+            for (int k = 0; k < 9; ++k) o.norms[k] = E[k];
+        }
+    }
+    return (int)vox.size();
 }
 
 }  // extern "C"

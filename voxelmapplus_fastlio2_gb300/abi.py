@@ -181,3 +181,16 @@ def plane_marker_dtype():
     import numpy as np
     return np.dtype([("center", "<f8", (3,)), ("norm", "<f8", (3,)), ("orientation", "<f8", (4,)), ("trace", "<f8"),
                      ("rgb", "u1", (3,)), ("merged", "u1"), ("pad", "<i4")])
+
+
+class vmp_std_voxel(C.Structure):
+    _fields_ = [("key", C.c_int64 * 3), ("n", C.c_int32), ("valid", C.c_int32), ("is_plane", C.c_int32),
+                ("pad", C.c_int32), ("sum", C.c_double * 3), ("ppt", C.c_double * 9), ("mean", C.c_double * 3),
+                ("lamdas", C.c_double * 3), ("norms", C.c_double * 9)]
+
+
+def std_voxel_dtype():
+    import numpy as np
+    return np.dtype([("key", "<i8", (3,)), ("n", "<i4"), ("valid", "<i4"), ("is_plane", "<i4"), ("pad", "<i4"),
+                     ("sum", "<f8", (3,)), ("ppt", "<f8", (9,)), ("mean", "<f8", (3,)), ("lamdas", "<f8", (3,)),
+                     ("norms", "<f8", (9,))])

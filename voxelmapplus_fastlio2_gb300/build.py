@@ -34,6 +34,7 @@ CU_SOURCES = [
     "k_map.cu",
     "k_merge.cu",
     "k_fit.cu",
+    "k_std.cu",
     "vmp_noalloc.cu",
     "vmp_server.cu",
 ]

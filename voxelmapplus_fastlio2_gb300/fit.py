@@ -55,6 +55,22 @@ def fit_planes_device(xyz_ptr, cov_ptr, offsets_ptr, n_vox, n_pts, out_ptr, mode
         raise VmpError(rc, "vmp_fit_planes_device")
 
 
+def std_plane_voxels(pts, voxel_size=1.0, voxel_min_point=10, voxel_plane_thresh=0.01):
+    """STDManager::buildVoxels on the device (vmp_std_plane_voxels): pts is an
+    (n, k) float32 array with x y z in the first three columns (k >= 3).
+    Returns records of abi.std_voxel_dtype() in packed-key order."""
+    pts = np.ascontiguousarray(pts, dtype=np.float32)
+    n, stride = pts.shape
+    cnt = C.c_int()
+    lib = load()
+    out = np.zeros(max(1, n), dtype=abi.std_voxel_dtype())
+    rc = lib.vmp_std_plane_voxels(_ptr(pts), stride, n, voxel_size, voxel_min_point, voxel_plane_thresh, _ptr(out),
+                                  n, C.byref(cnt))
+    if rc != abi.VMP_OK:
+        raise VmpError(rc, "vmp_std_plane_voxels")
+    return out[: cnt.value]
+
+
 # ---------------------------------------------------------------- workload
 def synth_voxels(n_vox, seed=0, median=40.0, sigma=1.0, n_min=5, n_max=4000, nonplanar=0.1, noise=0.01,
                  voxel=0.5, extent=(400, 400, 40), chunk=100_000):

@@ -166,20 +166,24 @@ class LIOBuilder:
                                                   C.c_void_p(d_imus), n_imu, C.byref(res)))
         return res
 
-    def livox_decode(self, livox, filter_num=1, range_min=0.5, range_max=20.0):
+    def livox_decode(self, livox, filter_num=1, range_min=0.5, range_max=20.0, copy_out=True):
         """livox2pcl on the device (src/utils.cpp:3-28).  livox: numpy array of
         abi.livox_dtype().  Returns (points (m, 4) float32: x y z t_ms,
-        intensity (m,), last point's t_ms); the cloud stays on the device for
-        process_decoded."""
+        intensity (m,), last point's t_ms) -- with copy_out=False only the
+        count and the last time are read back (the node's use); the cloud
+        stays on the device for process_decoded."""
         livox = np.ascontiguousarray(livox, dtype=abi.livox_dtype())
         n = len(livox)
-        out = np.zeros((max(1, n), 4), dtype=np.float32)
-        inten = np.zeros(max(1, n), dtype=np.float32)
+        out = np.zeros((max(1, n), 4), dtype=np.float32) if copy_out else None
+        inten = np.zeros(max(1, n), dtype=np.float32) if copy_out else None
         m = C.c_int()
         last = C.c_float()
         check(self.h, self.lib.vmp_livox_decode(self.h, C.c_void_p(livox.ctypes.data), n, filter_num, range_min,
-                                                range_max, C.c_void_p(out.ctypes.data), C.c_void_p(inten.ctypes.data),
+                                                range_max, C.c_void_p(out.ctypes.data) if copy_out else None,
+                                                C.c_void_p(inten.ctypes.data) if copy_out else None,
                                                 C.byref(m), C.byref(last)))
+        if not copy_out:
+            return m.value, last.value
         return out[: m.value], inten[: m.value], last.value
 
     def process_decoded(self, t_start, t_end, imus, n_imu):
