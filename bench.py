@@ -462,7 +462,7 @@ def run_served(args, streams, pkgs, workers, phases, barrier, keep_results=False
             if keep_results:
                 out[ph]["results"] = [(sids.index(r.stream_id), r.cookie, np.array(r.result.x.pos[:]),
                                        np.array(r.result.x.rot[:]).reshape(3, 3), r.result.evicted,
-                                       r.result.map_size) for r in res]
+                                       r.result.map_size, np.array(r.result.P[:])) for r in res]
             if ph == "device":
                 del dev
     finally:
@@ -470,10 +470,12 @@ def run_served(args, streams, pkgs, workers, phases, barrier, keep_results=False
     return out
 
 
-def run_cpu_served(streams, pkgs, warmup, steps, threads, stream_ids):
+def run_cpu_served(streams, pkgs, warmup, steps, threads, stream_ids, collect=None):
     """The CPU oracle on the served workload: the listed streams' packages,
     streams in parallel on `threads` host threads (one oracle per stream, as
-    the reference runs one single-threaded node per sensor)."""
+    the reference runs one single-threaded node per sensor).  With a dict
+    `collect`, the timed scans' results are stored in it by (stream, package
+    index)."""
     from concurrent.futures import ThreadPoolExecutor
     import oracle
 
@@ -488,14 +490,36 @@ def run_cpu_served(streams, pkgs, warmup, steps, threads, stream_ids):
 
     def timed(j):
         i = stream_ids[j]
-        for p in pkgs[i][2 + warmup:2 + warmup + steps]:
-            ors[j].process(p)
+        for k, p in enumerate(pkgs[i][2 + warmup:2 + warmup + steps]):
+            r = ors[j].process(p)
+            if collect is not None:
+                collect[(i, 2 + warmup + k)] = r
 
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
         list(ex.map(timed, range(len(stream_ids))))
     wall = time.perf_counter() - t0
     return len(stream_ids) * steps / wall, wall
+
+
+def pose_errors(gpu, cpu):
+    """Per-scan errors of served results against the oracle's: position (m),
+    rotation angle (rad, by atan2) and the covariance P (max abs difference
+    over max abs entry).  gpu: {(stream, package): (pos, rot, P)}."""
+    dp, da, dP = [], [], []
+    for key, ro in cpu.items():
+        if key not in gpu:
+            continue
+        pos, rot, P = gpu[key]
+        dp.append(float(np.linalg.norm(pos - np.array(ro.x.pos[:]))))
+        Rd = rot.T @ np.array(ro.x.rot[:]).reshape(3, 3)
+        sk = 0.5 * np.linalg.norm([Rd[2, 1] - Rd[1, 2], Rd[0, 2] - Rd[2, 0], Rd[1, 0] - Rd[0, 1]])
+        da.append(float(np.arctan2(sk, (np.trace(Rd) - 1.0) / 2.0)))
+        Po = np.array(ro.P[:])
+        dP.append(float(np.max(np.abs(P - Po)) / max(float(np.max(np.abs(Po))), 1e-300)))
+    if not dp:
+        return None
+    return {"scans": len(dp), "pos_m_max": max(dp), "rot_rad_max": max(da), "P_rel_max": max(dP)}
 
 
 def dist_setup(args, backend=None):
@@ -590,7 +614,10 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
     vbuild.build_all()
     pkgs = make_serve_packages(streams, 2 + W + 2 * K + L)
     workers = args.workers or min(32, len(streams))
-    served = run_served(args, streams, pkgs, workers, ["device", "host", "open"], barrier)
+    served = run_served(args, streams, pkgs, workers, ["device", "host", "open"], barrier, keep_results=True)
+    gpu_res = {(r[0], r[1]): (r[2], r[3], r[6]) for r in served["device"].pop("results")}
+    for ph in ("host", "open"):
+        served[ph].pop("results", None)
     plain_mix = run_served(args, streams, pkgs, 1, ["device"], barrier)
     # plain one-stream urban block (per-phase profile: the kernel roofline)
     kind, pts, ucfg, seed, uname = workload(args, rank, "urban")
@@ -631,7 +658,9 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         ids = list(range(min(4, len(streams))))
         cpk = [pkgs[i][:2 + W + K] if i in ids else [] for i in range(len(streams))]
-        v1, wall = run_cpu_served(streams, cpk, W, K, 1, ids)
+        cres = {}
+        v1, wall = run_cpu_served(streams, cpk, W, K, 1, ids, collect=cres)
+        line["pose_vs_oracle"] = pose_errors(gpu_res, cres)
         line["cpu_baseline"] = {"value": v1, "unit": "scans/s", "cores": 1, "kind": "port",
                                 "sample": f"{K} mapping scans of each of streams {ids} (rays/scan "
                                           f"{[streams[i][1] for i in ids]}) after {W} warm-up scans; CPU "

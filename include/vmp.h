@@ -318,6 +318,11 @@ typedef struct vmp_std_voxel {
 vmp_status vmp_std_plane_voxels(const float* pts, int stride, int n, double voxel_size, int voxel_min_point,
                                 double voxel_plane_thresh, vmp_std_voxel* out, int max, int* n_out);
 
+/* Test hook: a[i] / b[i] computed on the device by the reciprocal-and-
+ * correction path the kernels use for divisions that share a divisor, and by
+ * the FP64 division (host arrays of n; the two must agree bit for bit). */
+vmp_status vmp_test_division(const double* a, const double* b, int n, double* by_recip, double* by_div);
+
 /* The same leaf-centroid downsample for callers that cannot allocate device
  * memory (no counterpart in the reference): a real-time sensor thread that
  * must not call cudaMalloc/cudaFree, or a host framework whose own allocator

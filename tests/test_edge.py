@@ -127,3 +127,29 @@ def test_residual_reduce_empty(lio_mod):
     H, b, eff = g.residual_reduce(x, np.eye(23) * 1e-3, np.zeros((0, 3)), np.zeros((0, 9)))
     assert eff == 0 and not np.any(H) and not np.any(b)
     g.close()
+
+
+@pytest.mark.gpu
+def test_shared_divisor_division_is_exact():
+    """The kernels divide by a shared divisor through its reciprocal and
+    Markstein's correction; it must equal the FP64 division bit for bit --
+    random operands over wide exponent ranges, the covariance-term operands
+    (differences of nearby coordinates over n (l0 - lm)), signed zeros,
+    exact quotients and divisors at the range limits."""
+    from voxelmapplus_fastlio2_gb300._lib import load
+    rng = np.random.default_rng(17)
+    n = 1 << 20
+    a = rng.uniform(1, 2, n) * 2.0 ** rng.integers(-60, 60, n) * rng.choice([-1, 1], n)
+    b = rng.uniform(1, 2, n) * 2.0 ** rng.integers(-60, 60, n) * rng.choice([-1, 1], n)
+    m = n // 4  # the plane-covariance operands
+    a[:m] = rng.normal(0, 0.2, m)
+    b[:m] = rng.integers(10, 400, m) * -rng.uniform(1e-4, 2e-2, m)
+    a[m:m + 8] = [0.0, -0.0, 0.0, -0.0, 3.0, -7.5, 1e-300, 6.0]
+    b[m:m + 8] = [2.0, 2.0, -2.0, -2.0, 1.5, 2.5, 1e-289, 1e291]
+    a[m + 8:m + 1000] = b[m + 8:m + 1000] * rng.integers(-50, 50, 992)  # exact quotients
+    by_recip = np.zeros(n)
+    by_div = np.zeros(n)
+    dp = lambda x: C.c_void_p(x.ctypes.data)
+    rc = load().vmp_test_division(dp(a), dp(b), n, dp(by_recip), dp(by_div))
+    assert rc == 0
+    assert np.array_equal(by_recip.view(np.uint64), by_div.view(np.uint64))

@@ -11,7 +11,8 @@ STATUS_NAMES = {
     4: "VMP_ERR_HASH_FULL", 5: "VMP_ERR_TIMEOUT", 6: "VMP_ERR_CUDA", 7: "VMP_ERR_KEY_RANGE",
     8: "VMP_ERR_STATE", 9: "VMP_ERR_CAPACITY",
 }
-VMP_ERR_INVALID_ARG, VMP_ERR_ADMISSION_DENIED, VMP_ERR_CAPACITY = 1, 3, 9
+VMP_ERR_INVALID_ARG, VMP_ERR_OUT_OF_MEMORY, VMP_ERR_ADMISSION_DENIED = 1, 2, 3
+VMP_ERR_HASH_FULL, VMP_ERR_TIMEOUT, VMP_ERR_CUDA, VMP_ERR_KEY_RANGE, VMP_ERR_STATE, VMP_ERR_CAPACITY = 4, 5, 6, 7, 8, 9
 IMU_INIT, MAP_INIT, LIO_MAPPING = 0, 1, 2
 
 

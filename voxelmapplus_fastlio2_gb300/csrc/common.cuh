@@ -231,6 +231,26 @@ __device__ inline bool voxel_index(const double p[3], double vs, double inv, int
     return ok;
 }
 
+// --------------------------------------------------------------- division
+// a / b, correctly rounded, from y = RN(1 / b) by Markstein's correction
+// (P. W. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q = RN(a y) is
+// within one ulp of a / b, the remainder r = a - b q is exact by FMA, and
+// RN(q + r y) is RN(a / b).  Three FP64 instructions instead of a division
+// sequence, for divisions that share a divisor.  Valid while a / b and y
+// stay in the normal range (callers check the divisor with div_recip_ok);
+// a zero dividend keeps the sign rule of a / b.
+__host__ __device__ inline bool div_recip_ok(double b) {
+    const double ab = b < 0 ? -b : b;
+    return ab > 1e-290 && ab < 1e290;
+}
+__device__ __forceinline__ double div_by_recip(double a, double b, double y) {
+    const double q = a * y;
+    const double r = __fma_rn(-q, b, a);
+    const double q2 = __fma_rn(r, y, q);
+    return a == 0.0 ? q : q2;
+}
+
 // --------------------------------------------------------------- small FP64 algebra
 // Row-major, products summed k = 0..K-1 left to right (no FMA).
 template <int R, int K, int C>

@@ -261,7 +261,7 @@ __global__ void k_undistort(const DFilter* __restrict__ f, const DPose* __restri
     if (npose < 2) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 q = cloud[i];
-        double tau = (double)q.w / double(1000);
+        const double tau = div_by_recip((double)q.w, 1000.0, 1.0 / 1000.0);  // q.w / 1000, correctly rounded
         // head = largest h in [0, npose-2] with offset[h] < tau
         int lo = 0, hi = npose - 2, h = -1;
         while (lo <= hi) {

@@ -268,6 +268,8 @@ struct RefitConst {
     double evecs[9];
     double M1[9], M2[9];
     double den1, den2, inv_n;
+    double rden1, rden2;  // RN(1 / den1), RN(1 / den2)
+    bool recip_ok;        // both divisors in the range where div_by_recip is exact
 };
 __device__ inline void refit_const(const double* mean, int n, const double* ev, const double* evecs, RefitConst& k) {
     const double pn[3] = {evecs[0], evecs[3], evecs[6]};
@@ -282,6 +284,9 @@ __device__ inline void refit_const(const double* mean, int n, const double* ev, 
     k.den1 = (double)n * (ev[0] - ev[1]);
     k.den2 = (double)n * (ev[0] - ev[2]);
     k.inv_n = 1.0 / (double)n;
+    k.recip_ok = div_recip_ok(k.den1) && div_recip_ok(k.den2);
+    k.rden1 = k.recip_ok ? 1.0 / k.den1 : 0.0;
+    k.rden2 = k.recip_ok ? 1.0 / k.den2 : 0.0;
 }
 
 // J cov J^T is symmetric: its 21 upper-triangle entries (row-major over the
@@ -298,8 +303,19 @@ __device__ inline void plane_cov_term(const double* p, const double* cov, const 
     const double d[3] = {p[0] - k.mean[0], p[1] - k.mean[1], p[2] - k.mean[2]};
     double F1[3], F2[3];
     {
-        const double a[3] = {d[0] / k.den1, d[1] / k.den1, d[2] / k.den1};
-        const double b[3] = {d[0] / k.den2, d[1] / k.den2, d[2] / k.den2};
+        // d / den, correctly rounded (the reference's division)
+        double a[3], b[3];
+        if (k.recip_ok) {
+            for (int c = 0; c < 3; ++c) {
+                a[c] = div_by_recip(d[c], k.den1, k.rden1);
+                b[c] = div_by_recip(d[c], k.den2, k.rden2);
+            }
+        } else {
+            for (int c = 0; c < 3; ++c) {
+                a[c] = d[c] / k.den1;
+                b[c] = d[c] / k.den2;
+            }
+        }
         for (int j = 0; j < 3; ++j) {
             F1[j] = (a[0] * k.M1[j] + a[1] * k.M1[3 + j]) + a[2] * k.M1[6 + j];
             F2[j] = (b[0] * k.M2[j] + b[1] * k.M2[3 + j]) + b[2] * k.M2[6 + j];
@@ -365,6 +381,9 @@ struct RefitSnap {
     double evecs[9];
     double M1[9], M2[9];  // RefitConst of a plane refit
     double den1, den2, inv_n;
+    double rden1, rden2;  // RN(1 / den): the divisions of the terms by the reciprocal (div_by_recip)
+    int recip_ok;
+    int pad2;
 };
 struct CovSeg {
     uint32_t seg;
@@ -648,6 +667,9 @@ __global__ void k_refit_eig(DMap m, SegScratch ss) {
         sn.den1 = kc.den1;
         sn.den2 = kc.den2;
         sn.inv_n = kc.inv_n;
+        sn.rden1 = kc.rden1;
+        sn.rden2 = kc.rden2;
+        sn.recip_ok = kc.recip_ok ? 1 : 0;
         const int off = atomicAdd(ss.d_n_terms, sn.npts);
         if (off + sn.npts <= ss.term_cap) {  // else k_seg_cov forms these terms itself
             sn.toff = off;
@@ -662,6 +684,9 @@ __device__ inline void snap_const(const RefitSnap& sn, RefitConst& k) {
     k.den1 = sn.den1;
     k.den2 = sn.den2;
     k.inv_n = sn.inv_n;
+    k.rden1 = sn.rden1;
+    k.rden2 = sn.rden2;
+    k.recip_ok = sn.recip_ok != 0;
 }
 
 // The point's source: batch segment (build) or slab prefix.

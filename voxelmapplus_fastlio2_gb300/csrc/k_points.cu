@@ -187,7 +187,12 @@ __device__ inline void normalize3(double* v) {
     double n = dot3(v, v);
     if (n > 0.0) {
         double r = sqrt(n);
-        v[0] = v[0] / r; v[1] = v[1] / r; v[2] = v[2] / r;
+        if (div_recip_ok(r)) {  // the three divisions by r, correctly rounded
+            const double y = 1.0 / r;
+            v[0] = div_by_recip(v[0], r, y); v[1] = div_by_recip(v[1], r, y); v[2] = div_by_recip(v[2], r, y);
+        } else {
+            v[0] = v[0] / r; v[1] = v[1] / r; v[2] = v[2] / r;
+        }
     }
 }
 

@@ -104,6 +104,15 @@ __global__ void k_export(DMap m, vmp_voxel* out, int* d_count, int max) {
         for (int k = 0; k < 36; ++k) v.cov[k] = c.cov[k];
     }
 }
+// Test hook: the shared-divisor division against the FP64 division, per pair.
+__global__ void k_div_check(const double* a, const double* b, int n, double* by_recip, double* by_div) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double y = 1.0 / b[i];
+        by_recip[i] = div_recip_ok(b[i]) ? div_by_recip(a[i], b[i], y) : __ddiv_rn(a[i], b[i]);
+        by_div[i] = __ddiv_rn(a[i], b[i]);
+    }
+}
+
 // ---- voxel-map export for visualisation (voxel2MarkerArray, utils.cpp:154-208)
 // Frozen planes (is_plane && !update_enable) with their LRU stamps, as sort
 // keys that order the most recently touched first (complemented halves).
@@ -1257,6 +1266,30 @@ vmp_status vmp_map_export(vmp_stream_t s, vmp_voxel* out, long long max, long lo
     long long n = std::min<long long>(max, (long long)all.size());
     if (n > 0) std::memcpy(out, all.data(), sizeof(vmp_voxel) * (size_t)n);
     if (n_out) *n_out = (long long)all.size();
+    return VMP_OK;
+}
+
+// Test hook: a[i] / b[i] by the reciprocal-and-correction path the kernels
+// use for shared divisors and by the FP64 division (host arrays of n).
+vmp_status vmp_test_division(const double* a, const double* b, int n, double* by_recip, double* by_div) {
+    if (n < 0 || (n > 0 && (!a || !b || !by_recip || !by_div))) return VMP_ERR_INVALID_ARG;
+    if (n == 0) return VMP_OK;
+    double* d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 4 * (size_t)n) != cudaSuccess) return VMP_ERR_OUT_OF_MEMORY;
+    cudaError_t e = cudaMemcpy(d, a, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        VMP_NOTE_LAUNCH();
+        k_div_check<<<std::min(1216, (n + 255) / 256), 256>>>(d, d + n, n, d + 2 * (size_t)n, d + 3 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(by_recip, d + 2 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(by_div, d + 3 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return VMP_ERR_CUDA;
+    }
     return VMP_OK;
 }
 
