@@ -21,6 +21,8 @@
 //   6. LRU: each touched voxel's stamp = global index of its last touching
 //      point; evictions take the least recent untouched voxels in creation
 //      order.
+#include <mutex>
+#include <vector>
 #include "kernels.cuh"
 
 namespace vmp {
@@ -32,6 +34,28 @@ static int grid_for_map(int n) {
     int b = (n + kMapThreads - 1) / kMapThreads;
     if (b > 152 * 8) b = 152 * 8;
     return b < 1 ? 1 : b;
+}
+
+// RN(1 / k) for k = 1 .. kRecipTable - 1 (the running mean's divisors n + 1),
+// written once per device from the host's correctly rounded divisions.
+constexpr int kRecipTable = 4096;
+__device__ double g_recip[kRecipTable];
+
+cudaError_t map_recip_table_init() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return cudaSuccess;
+    std::vector<double> t(kRecipTable, 0.0);
+    for (int k = 1; k < kRecipTable; ++k) t[k] = 1.0 / (double)k;
+    e = cudaMemcpyToSymbol(g_recip, t.data(), sizeof(double) * kRecipTable);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
 }
 
 // ---------------------------------------------------------------- lookup / insert
@@ -527,7 +551,12 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             ++nref;
         };
         auto add_point = [&](const double* p) {
-            if (q < 3) mean_l = mean_l + (p[q] - mean_l) / ((double)n + 1.0);
+            // (p - mean) / (n + 1): the divisor's reciprocal from the table
+            // (small counts), the division itself otherwise
+            if (q < 3) {
+                const double num = p[q] - mean_l, den = (double)n + 1.0;
+                mean_l = mean_l + (n + 1 < kRecipTable ? div_by_recip(num, den, __ldg(g_recip + n + 1)) : num / den);
+            }
             if (q < 9) ppt_l = ppt_l + p[q / 3] * p[q % 3];
             n += 1;
         };
@@ -652,8 +681,11 @@ __global__ void k_refit_eig(DMap m, SegScratch ss) {
         RefitSnap& sn = ss.snaps[si];
         const double dn = (double)sn.n;
         double C[9], ev[3], evecs[9];
+        // ppt / n - mean mean^T; the nine divisions by n share the divisor
+        const double rn = 1.0 / dn;
         for (int k = 0; k < 3; ++k)
-            for (int l = 0; l < 3; ++l) C[k * 3 + l] = sn.ppt[k * 3 + l] / dn - sn.mean[k] * sn.mean[l];
+            for (int l = 0; l < 3; ++l)
+                C[k * 3 + l] = div_by_recip(sn.ppt[k * 3 + l], dn, rn) - sn.mean[k] * sn.mean[l];
         eig_sym3<double>(C, ev, evecs);
         for (int k = 0; k < 3; ++k) sn.ev[k] = ev[k];
         for (int k = 0; k < 9; ++k) sn.evecs[k] = evecs[k];

@@ -161,5 +161,8 @@ int merge_rounds_read(void* scratch, cudaStream_t st);
 // Many streams from now on (a server exists): cooperative merge launches use
 // half the SMs and run several at once instead of one at a time on all SMs.
 void merge_set_throughput_mode();
+// Writes the reciprocal table of the voxel state machine on the current
+// device (once per device; before any stream of the device runs a map batch).
+cudaError_t map_recip_table_init();
 
 }  // namespace vmp

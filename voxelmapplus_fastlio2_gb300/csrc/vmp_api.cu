@@ -657,6 +657,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     m.cnt = s->cnt;
     CREATE_TRY(cudaMemset(s->cnt, 0, sizeof(Counters)));
     CREATE_TRY(map_scratch_alloc(s->ms, max_pts, m.rec_pool, cfg.reserved[1]));
+    CREATE_TRY(map_recip_table_init());
     // queue compaction scratch
     const int qmax = (int)std::min<uint64_t>(m.q_cap, 0x7FFFFFF0ull);
     CREATE_TRY(dalloc(s, &s->qc_flag, qmax));
