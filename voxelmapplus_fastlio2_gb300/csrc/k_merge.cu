@@ -577,16 +577,19 @@ void merge_scratch_free(void* p) {
     delete ms;
 }
 
-constexpr int kMaxCoopSlots = 8;
+constexpr int kMaxCoopSlots = 64;
 static std::mutex g_coop_mu;
 static std::vector<cudaEvent_t> g_coop_done;  // completion of the last launches, one per slot
 static unsigned long long g_coop_next = 0;
 static int g_coop_slots = 1;
 static bool g_coop_throughput = false;
+static int g_coop_throughput_refs = 0;
 
-void merge_set_throughput_mode() {
+void merge_set_throughput_mode(bool on) {
     std::lock_guard<std::mutex> lk(g_coop_mu);
-    g_coop_throughput = true;
+    g_coop_throughput_refs += on ? 1 : -1;
+    if (g_coop_throughput_refs < 0) g_coop_throughput_refs = 0;
+    g_coop_throughput = g_coop_throughput_refs > 0;
 }
 
 // The merge calls of one batch: the cooperative fixed point, then the replay
@@ -606,11 +609,14 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     if ((e = cudaMemsetAsync(&g.ctl->converged, 0, sizeof(int) * 3 + sizeof(unsigned int), st)) != cudaSuccess) return e;
     if (g.coop_capacity > 0) {
         // Launch sizing (process-wide): alone, one launch at a time on the
-        // whole device; once a server runs many streams, half the SMs per
-        // launch and at most capacity / grid launches on the device at once
-        // (launch i waits for launch i - slots; on a switch, for all
-        // earlier ones).  Their CTAs then always fit co-resident, so no
-        // launch can wait for CTAs that the others hold while they wait.
+        // whole device; once a server runs many streams, 1/16 of the SMs per
+        // launch (a batch's merge calls are few: small grids spend less on
+        // grid barriers and leave the device to the other streams; measured
+        // best among 1/2 .. 1/152 on 64 streams) and at most capacity / grid
+        // launches (<= 64) on the device at once (launch i waits for launch
+        // i - slots; on a switch, for all earlier ones).  Their CTAs then
+        // always fit co-resident, so no launch can wait for CTAs that the
+        // others hold while they wait.
         std::lock_guard<std::mutex> lk(g_coop_mu);
         if (g_coop_done.empty()) {
             g_coop_done.assign(kMaxCoopSlots, nullptr);
@@ -622,7 +628,7 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
         }
         int grid = g.coop_capacity, slots = 1;
         if (g_coop_throughput) {
-            grid = g.sms / 2 > 0 ? g.sms / 2 : 1;
+            grid = g.sms / 16 > 0 ? g.sms / 16 : 1;
             if (grid > g.coop_capacity) grid = g.coop_capacity;
             slots = g.coop_capacity / grid;
             if (slots < 1) slots = 1;

@@ -158,9 +158,10 @@ void merge_scratch_free(void* p);
 cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, int mode, int* rounds_out,
                              cudaStream_t st);
 int merge_rounds_read(void* scratch, cudaStream_t st);
-// Many streams from now on (a server exists): cooperative merge launches use
-// half the SMs and run several at once instead of one at a time on all SMs.
-void merge_set_throughput_mode();
+// While at least one multi-worker server exists (on: one more, off: one
+// fewer), cooperative merge launches use 1/16 of the SMs and run several at
+// once instead of one at a time on all SMs.
+void merge_set_throughput_mode(bool on);
 // Writes the reciprocal table of the voxel state machine on the current
 // device (once per device; before any stream of the device runs a map batch).
 cudaError_t map_recip_table_init();

@@ -24,7 +24,7 @@
 #include "vmp.h"
 
 namespace vmp {
-void merge_set_throughput_mode();
+void merge_set_throughput_mode(bool on);
 }
 
 namespace {
@@ -147,13 +147,15 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
     // if the process has not created its CUDA context yet; a caller's own
     // setting wins.
     setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
-    // cooperative merges of many streams: half the device each, several at once
-    vmp::merge_set_throughput_mode();
     vmp_server_t sv = new (std::nothrow) vmp_server_s();
     if (!sv) return VMP_ERR_OUT_OF_MEMORY;
     sv->cfg = cfg;
     sv->slots.resize(cfg.max_streams);
     sv->workers.reserve(cfg.workers);
+    // cooperative merges of several streams at once: small grids, many in
+    // flight (a one-worker server runs one package at a time: whole-device
+    // merges, as a single stream)
+    if (cfg.workers > 1) vmp::merge_set_throughput_mode(true);
     for (int i = 0; i < cfg.workers; ++i) sv->workers.emplace_back([sv] { sv->worker(); });
     *out = sv;
     return VMP_OK;
@@ -169,6 +171,7 @@ vmp_status vmp_server_destroy(vmp_server_t sv) {
     for (auto& t : sv->workers) t.join();
     for (auto& s : sv->slots)
         if (s.h) vmp_destroy(s.h);
+    if (sv->cfg.workers > 1) vmp::merge_set_throughput_mode(false);
     delete sv;
     return VMP_OK;
 }
