@@ -59,7 +59,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "scans/s & p99 scan latency: 64-stream served vs plain 1-stream GPU vs CPU ref"
 
-# SURVEY 8(d)-style algorithmic bytes per unit for each profiled phase:
+# Algorithmic (minimum unique) bytes per unit of work for each profiled phase:
 # (bytes per unit, unit name).  Units are the points the phase processes.
 ALGO_BYTES = {
     "residual": (64.0, "downsampled point x IEKF iteration"),   # 16 B point + 16 B slot + 32 B plane record
@@ -678,7 +678,7 @@ CORRIDOR_NAME = ("long-horizon stress: {s} independent streams, each a 1 km corr
 
 
 def main_corridor(args, rank, ws, barrier, allmax, dist):
-    """configs[4]-style long-horizon stress: many corridor streams served
+    """Long-horizon stress (1 km corridors): many corridor streams served
     with the LRU cap in force; throughput, latency, eviction counts, and the
     drift of stream 0 against the oracle and against the ground truth."""
     from voxelmapplus_fastlio2_gb300 import abi, synth
@@ -885,7 +885,7 @@ def planefit_bytes(off, rec):
 
 
 def main_planefit(args, rank, ws, barrier, allmax, dist):
-    """configs[2]-style batched plane fitting: value = voxels/s of the chosen
+    """Batched plane fitting (1 M voxels): value = voxels/s of the chosen
     mode with the batch resident in HBM; e2e = the host-buffer call
     (vmp_fit_planes) with the copies inside; precision of all three modes
     against the oracle (FP64, the reference's sequential arithmetic)."""
