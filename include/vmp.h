@@ -476,7 +476,9 @@ typedef struct vmp_server_config {
     int max_streams;            /* stream slots (default 64) */
     int workers;                /* host threads driving streams concurrently (default 32) */
     int queue_depth;            /* queued packages per stream before vmp_submit answers VMP_ERR_CAPACITY (default 64) */
-    int reserved[7];
+    int autotune;               /* 1 (default): tune the launch shape of the served merge resolution online */
+    int merge_grid_divisor;     /* served merge launches use SMs / divisor CTAs (0: 16); autotune's start */
+    int reserved[5];
 } vmp_server_config;
 
 typedef struct vmp_server_result {
@@ -490,6 +492,11 @@ typedef struct vmp_server_result {
 } vmp_server_result;
 
 void vmp_server_config_default(vmp_server_config* c);
+/* The autotuner's state: the merge grid divisor in use, the windows of 128
+ * completed packages measured so far and the best rate seen (packages/s).
+ * The divisor changes only the launch shape of a deterministic fixed point:
+ * results are the same under every setting. */
+vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long* windows, double* best_rate);
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out);
 /* Waits for the packages that are running; queued ones are dropped. */
 vmp_status vmp_server_destroy(vmp_server_t sv);

@@ -32,11 +32,11 @@ def _key(res):
             bytes(res.P))
 
 
-def _run_server(streams, workers, concurrent):
+def _run_server(streams, workers, concurrent, **server_kw):
     """streams: list of (kind, packages).  concurrent=False submits one
     stream's next package only after the previous stream's finished."""
     from voxelmapplus_fastlio2_gb300.serve import Server
-    srv = Server(hbm_budget_bytes=150e9, max_streams=len(streams), workers=workers)
+    srv = Server(hbm_budget_bytes=150e9, max_streams=len(streams), workers=workers, **server_kw)
     try:
         sids = [srv.open_stream(_cfg(kind)) for kind, _ in streams]
         out = {sid: [] for sid in sids}
@@ -109,5 +109,29 @@ def test_admission_by_budget_and_release():
         srv.close_stream(a)
         c = srv.open_stream(_cfg(synth.KIND_ROOM))  # the freed budget admits a new stream
         assert srv.info()["streams_open"] == 2 and c != b
+    finally:
+        srv.close()
+
+
+def test_merge_launch_shape_does_not_change_results():
+    """The served merge resolution runs on grids of SMs / divisor CTAs (the
+    autotuner's knob): every divisor gives the same results and maps."""
+    streams = []
+    for i in range(4):
+        kind = synth.KIND_ROOM if i % 2 == 0 else synth.KIND_URBAN
+        streams.append((kind, _packages(kind, 0x5EED0000 + 200 + i, [6000, 30000, 10000, 20000][i], 7)))
+    runs = [_run_server(streams, workers=4, concurrent=True, autotune=False, merge_grid_divisor=d)
+            for d in (2, 16, 152)]
+    for res, maps in runs[1:]:
+        assert [[k for _, k in r] for r in res] == [[k for _, k in r] for r in runs[0][0]]
+        assert maps == runs[0][1]
+
+
+def test_autotuner_reports_state():
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    srv = Server(hbm_budget_bytes=150e9, max_streams=2, workers=2)
+    try:
+        t = srv.tuning()
+        assert t["merge_grid_divisor"] in (4, 8, 16, 32, 64) and t["windows"] == 0
     finally:
         srv.close()

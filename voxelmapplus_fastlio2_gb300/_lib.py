@@ -71,6 +71,7 @@ def _declare(lib):
         "vmp_server_stream": ([vp, C.c_int, P(vp)], st),
         "vmp_server_info": ([vp, P(C.c_longlong), P(C.c_int), P(C.c_int), P(C.c_int)], st),
         "vmp_server_last_error": ([vp], C.c_char_p),
+        "vmp_server_tuning": ([vp, P(C.c_int), P(C.c_longlong), P(d)], st),
         "vmp_fit_planes": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp], st),
         "vmp_fit_planes_device": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp, vp], st),
         "vmp_fit_profile": ([C.c_int], st),

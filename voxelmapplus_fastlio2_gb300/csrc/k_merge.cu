@@ -584,6 +584,12 @@ static unsigned long long g_coop_next = 0;
 static int g_coop_slots = 1;
 static bool g_coop_throughput = false;
 static int g_coop_throughput_refs = 0;
+static int g_coop_divisor = 16;
+
+void merge_set_grid_divisor(int d) {
+    std::lock_guard<std::mutex> lk(g_coop_mu);
+    g_coop_divisor = d < 1 ? 1 : (d > 1024 ? 1024 : d);
+}
 
 void merge_set_throughput_mode(bool on) {
     std::lock_guard<std::mutex> lk(g_coop_mu);
@@ -609,10 +615,10 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     if ((e = cudaMemsetAsync(&g.ctl->converged, 0, sizeof(int) * 3 + sizeof(unsigned int), st)) != cudaSuccess) return e;
     if (g.coop_capacity > 0) {
         // Launch sizing (process-wide): alone, one launch at a time on the
-        // whole device; once a server runs many streams, 1/16 of the SMs per
-        // launch (a batch's merge calls are few: small grids spend less on
-        // grid barriers and leave the device to the other streams; measured
-        // best among 1/2 .. 1/152 on 64 streams) and at most capacity / grid
+        // whole device; once a server runs many streams, SMs / divisor CTAs
+        // per launch (a batch's merge calls are few: small grids spend less
+        // on grid barriers and leave the device to the other streams; the
+        // server's autotuner picks the divisor, 16 by default) and at most capacity / grid
         // launches (<= 64) on the device at once (launch i waits for launch
         // i - slots; on a switch, for all earlier ones).  Their CTAs then
         // always fit co-resident, so no launch can wait for CTAs that the
@@ -628,7 +634,7 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
         }
         int grid = g.coop_capacity, slots = 1;
         if (g_coop_throughput) {
-            grid = g.sms / 16 > 0 ? g.sms / 16 : 1;
+            grid = g.sms / g_coop_divisor > 0 ? g.sms / g_coop_divisor : 1;
             if (grid > g.coop_capacity) grid = g.coop_capacity;
             slots = g.coop_capacity / grid;
             if (slots < 1) slots = 1;

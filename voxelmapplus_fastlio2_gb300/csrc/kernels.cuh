@@ -162,6 +162,8 @@ int merge_rounds_read(void* scratch, cudaStream_t st);
 // fewer), cooperative merge launches use 1/16 of the SMs and run several at
 // once instead of one at a time on all SMs.
 void merge_set_throughput_mode(bool on);
+// Served merge launches use SMs / d CTAs (process-wide; 16 by default).
+void merge_set_grid_divisor(int d);
 // Writes the reciprocal table of the voxel state machine on the current
 // device (once per device; before any stream of the device runs a map batch).
 cudaError_t map_recip_table_init();

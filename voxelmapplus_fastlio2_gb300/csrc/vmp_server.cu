@@ -25,6 +25,7 @@
 
 namespace vmp {
 void merge_set_throughput_mode(bool on);
+void merge_set_grid_divisor(int d);
 }
 
 namespace {
@@ -52,8 +53,76 @@ struct Slot {
 
 }  // namespace
 
+// Online autotuner of the served merge launch shape, a hill climb over the
+// grid divisors kCand: a window of completed packages at the current divisor
+// (the first packages after a switch are not counted), then one at each
+// neighbour; the fastest of the three becomes current.  When the current one
+// wins, it is kept for kExploit windows before its neighbours are measured
+// again (the stream mix may have changed).  It starts at 16 (measured best
+// on 64 mixed streams) and climbs first after kFirst windows, so short runs
+// pay nothing for the exploration.
+struct MergeTuner {
+    static constexpr int kWindow = 128, kSettle = 16, kExploit = 32, kN = 5;
+    static constexpr int kCand[kN] = {4, 8, 16, 32, 64};
+    static constexpr int kFirst = 8;  // windows at the starting divisor before the first climb
+    int idx = 2;             // current candidate
+    int probe = 3;           // 0: current, 1: idx + 1, 2: idx - 1, 3: exploiting
+    int exploit_left = kFirst;
+    int seen = 0;            // packages completed in the window (settling first)
+    double t_begin = 0.0;
+    double rate[3] = {};     // current, upper, lower
+    long long windows = 0;
+    double best = 0.0;
+
+    int cur() const {
+        const int i = probe == 1 ? idx + 1 : (probe == 2 ? idx - 1 : idx);
+        return kCand[i];
+    }
+    // the next probe that has a candidate, from `p` on
+    int next_probe(int p) const {
+        if (p == 1 && idx + 1 >= kN) p = 2;
+        if (p == 2 && idx - 1 < 0) p = 3;
+        return p;
+    }
+    // called under the server lock at every completion; returns the divisor
+    // to switch to, or 0
+    int on_done(double now_ms) {
+        ++seen;
+        if (seen == kSettle) t_begin = now_ms;
+        if (seen < kSettle + kWindow) return 0;
+        const double r = kWindow / ((now_ms - t_begin) * 1e-3);
+        seen = 0;
+        ++windows;
+        if (r > best) best = r;
+        if (probe == 3) {
+            if (--exploit_left > 0) return 0;
+            rate[0] = r;  // the current one, freshly measured
+            probe = next_probe(1);
+            return probe == 3 ? 0 : cur();
+        }
+        rate[probe] = r;
+        probe = next_probe(probe + 1);
+        if (probe < 3) return cur();
+        int pick = 0;  // decide among current / upper / lower
+        if (idx + 1 < kN && rate[1] > rate[pick]) pick = 1;
+        if (idx - 1 >= 0 && rate[2] > rate[pick]) pick = 2;
+        if (pick == 0) {
+            exploit_left = kExploit;
+        } else {
+            idx += pick == 1 ? 1 : -1;
+            rate[0] = rate[pick];
+            probe = next_probe(1);
+            if (probe == 3) exploit_left = kExploit;
+        }
+        return cur();
+    }
+};
+constexpr int MergeTuner::kCand[MergeTuner::kN];
+
 struct vmp_server_s {
     vmp_server_config cfg{};
+    MergeTuner tuner;
+    int fixed_divisor = 16;
     std::mutex mu;
     std::condition_variable cv_work;  // workers: a package is ready / stop
     std::condition_variable cv_done;  // pollers, close / destroy: a package finished
@@ -116,6 +185,10 @@ struct vmp_server_s {
             lk.lock();
             sl.busy = false;
             --running;
+            if (cfg.autotune && cfg.workers > 1) {
+                const int d = tuner.on_done(r.end_ms);
+                if (d > 0) vmp::merge_set_grid_divisor(d);
+            }
             done.push_back(r);
             cv_done.notify_all();
             cv_work.notify_all();
@@ -132,6 +205,8 @@ void vmp_server_config_default(vmp_server_config* c) {
     c->max_streams = 64;
     c->workers = 32;
     c->queue_depth = 64;
+    c->autotune = 1;
+    c->merge_grid_divisor = 16;
 }
 
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
@@ -155,9 +230,31 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
     // cooperative merges of several streams at once: small grids, many in
     // flight (a one-worker server runs one package at a time: whole-device
     // merges, as a single stream)
-    if (cfg.workers > 1) vmp::merge_set_throughput_mode(true);
+    if (cfg.workers > 1) {
+        vmp::merge_set_throughput_mode(true);
+        const int d0 = cfg.merge_grid_divisor > 0 ? cfg.merge_grid_divisor : 16;
+        vmp::merge_set_grid_divisor(d0);
+        if (cfg.autotune) {  // the climb starts at the candidate nearest the configured divisor
+            int bi = 0;
+            for (int i = 1; i < MergeTuner::kN; ++i)
+                if (std::abs(MergeTuner::kCand[i] - d0) < std::abs(MergeTuner::kCand[bi] - d0)) bi = i;
+            sv->tuner.idx = bi;
+            vmp::merge_set_grid_divisor(sv->tuner.cur());
+        }
+        sv->fixed_divisor = d0;
+    }
     for (int i = 0; i < cfg.workers; ++i) sv->workers.emplace_back([sv] { sv->worker(); });
     *out = sv;
+    return VMP_OK;
+}
+
+vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long* windows, double* best_rate) {
+    if (!sv) return VMP_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (merge_grid_divisor)
+        *merge_grid_divisor = sv->cfg.autotune && sv->cfg.workers > 1 ? sv->tuner.cur() : sv->fixed_divisor;
+    if (windows) *windows = sv->tuner.windows;
+    if (best_rate) *best_rate = sv->tuner.best;
     return VMP_OK;
 }
 

@@ -15,7 +15,8 @@ from .lio import LIOBuilder
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes=150e9, max_streams=64, workers=32, queue_depth=64):
+    def __init__(self, hbm_budget_bytes=150e9, max_streams=64, workers=32, queue_depth=64, autotune=True,
+                 merge_grid_divisor=16):
         self.lib = load()
         cfg = abi.vmp_server_config()
         self.lib.vmp_server_config_default(C.byref(cfg))
@@ -23,6 +24,8 @@ class Server:
         cfg.max_streams = int(max_streams)
         cfg.workers = int(workers)
         cfg.queue_depth = int(queue_depth)
+        cfg.autotune = 1 if autotune else 0
+        cfg.merge_grid_divisor = int(merge_grid_divisor)
         h = C.c_void_p()
         code = self.lib.vmp_server_create(C.byref(cfg), C.byref(h))
         if code != abi.VMP_OK:
@@ -79,6 +82,12 @@ class Server:
                                              C.byref(running)), "info")
         return {"budget_used": used.value, "streams_open": n_open.value, "queued": queued.value,
                 "running": running.value}
+
+    def tuning(self):
+        """The online autotuner's state (vmp_server_tuning)."""
+        d, w, r = C.c_int(), C.c_longlong(), C.c_double()
+        self._check(self.lib.vmp_server_tuning(self.h, C.byref(d), C.byref(w), C.byref(r)), "vmp_server_tuning")
+        return {"merge_grid_divisor": d.value, "windows": w.value, "best_rate": r.value}
 
     def close(self):
         if getattr(self, "h", None):
