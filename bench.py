@@ -465,6 +465,7 @@ def run_served(args, streams, pkgs, workers, phases, barrier, keep_results=False
                                        r.result.map_size, np.array(r.result.P[:])) for r in res]
             if ph == "device":
                 del dev
+        out["tuning"] = srv.tuning()
     finally:
         srv.close()
     return out
@@ -641,7 +642,7 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(C.sizeof(abi.vmp_result)),
                     "latency_ms": hv["latency_ms"]},
             "served": {"streams": args.streams, "workers": workers, "hbm_budget_gb": args.hbm_budget_gb,
-                       "budget_used_gb": served["budget_used_gb"],
+                       "budget_used_gb": served["budget_used_gb"], "autotuner": served["tuning"],
                        "device_resident": dv, "host_buffers": hv,
                        "open_loop_10hz": served["open"]},
             "plain_1stream": {
