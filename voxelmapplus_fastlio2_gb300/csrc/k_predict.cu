@@ -14,13 +14,13 @@
 //   * the covariance chain P = F P F^T + G Q G^T computes only the 11 rows /
 //     columns of F that are not identity rows, summing each entry's
 //     structural non-zero terms in k order -- the same value as the dense
-//     product -- one warp per row group with the lanes over the other index;
+//     product -- one warp per row with the lanes over the other index;
 //     the G Q G^T blocks (Q diagonal) are precomputed per step.
 #include "kernels.cuh"
 
 namespace vmp {
 
-constexpr int kPredThreads = 128;  // one warp per SM sub-partition
+constexpr int kPredThreads = 352;  // 11 warps: one per active F row / column of the covariance chain
 
 // F row / column groups that are not identity: {0,1,2}, {3,4,5}, {12,13,14}, {21,22}.
 __device__ inline bool f_row_active(int i) { return i < 6 || (i >= 12 && i < 15) || i >= 21; }
@@ -104,8 +104,9 @@ __device__ inline double fpft_entry_s(const StepSm& d, const double* NM, const d
     return r[21] * NM[a * 2 + 0] + r[22] * NM[a * 2 + 1];
 }
 
-// Row (half 1) / column (half 2) groups per warp, balanced by FP64 cost.
-__constant__ int kGroupStart[5] = {0, 2, 4, 6, 11};
+// Row (half 1) / column (half 2) of each warp: the 11 active indices, one per
+// warp, so that a step's dependent chain is one entry's sum.
+__constant__ int kGroupStart[12] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11};
 __constant__ int kGroupIdx[11] = {12, 3, 13, 4, 14, 5, 0, 1, 2, 21, 22};
 
 // B = G Q G^T entry (i, j) for the step, 0 where structurally zero.
