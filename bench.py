@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
                     help="timed scans (per stream for the served workload; default 16 there, 60 otherwise)")
-    ap.add_argument("--warmup", type=int, default=None, help="warm-up scans (default 3 served, 5 otherwise)")
+    ap.add_argument("--warmup", type=int, default=None, help="warm-up scans (default 10 served, 3 corridor, 5 otherwise)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="serve", choices=["serve", "urban", "room", "planefit", "corridor", "io"])
     ap.add_argument("--voxels", type=int, default=1_000_000, help="planefit workload: voxels per batch")
