@@ -385,7 +385,9 @@ vmp_status vmp_fit_planes_device(const float* xyz, const float* cov, const long 
                                  long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out,
                                  void* cuda_stream);
 /* Host-buffer form: copies in, fits, copies the records out and returns
- * after they arrived (allocates and frees device memory per call). */
+ * after they arrived.  The copies of one quarter of the voxels overlap the fit
+ * of the previous quarter; the device buffers are kept for the next call
+ * (grown when a call needs more) and calls are serialised. */
 vmp_status vmp_fit_planes(const float* xyz, const float* cov, const long long* offsets, int n_vox,
                           long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out);
 /* Measurement hook: while on, every fit call records CUDA events around its

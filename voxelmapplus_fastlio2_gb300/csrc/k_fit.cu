@@ -113,9 +113,6 @@ __device__ __forceinline__ void transpose_reduce16(V (&v)[16], int lane) {
 __host__ __device__ constexpr int red_lane(int k) {
     return (((k >> 3) & 1) << 4) | (((k >> 2) & 1) << 3) | (((k >> 1) & 1) << 2) | ((k & 1) << 1);
 }
-__device__ __forceinline__ int red_index(int lane) {
-    return (((lane >> 4) & 1) << 3) | (((lane >> 3) & 1) << 2) | (((lane >> 2) & 1) << 1) | ((lane >> 1) & 1);
-}
 
 template <int MODE> struct FitTypes;
 template <> struct FitTypes<FIT_FP64> { using T = double; using Acc = double; };
@@ -509,6 +506,59 @@ extern "C" vmp_status vmp_fit_planes_device(const float* xyz, const float* cov, 
     return VMP_OK;
 }
 
+namespace vmp {
+namespace {
+// Device buffers and streams of the host-buffer entry point, kept between
+// calls (grown when a call needs more): the copies of one chunk of voxels
+// overlap the fit of the previous chunk and the copy-back of the one before.
+struct FitHostCache {
+    std::mutex mu;
+    float* d_pts = nullptr;
+    long long* d_off = nullptr;
+    vmp_fit_rec* d_out = nullptr;
+    size_t cap_pts = 0, cap_vox = 0;
+    cudaStream_t s_in = nullptr, s_fit = nullptr, s_out = nullptr;
+    static constexpr int kChunks = 4;
+    cudaEvent_t in_done[kChunks] = {}, fit_done[kChunks] = {};
+    bool ready = false;
+};
+FitHostCache& fit_host_cache() {
+    static FitHostCache c;
+    return c;
+}
+cudaError_t fit_host_prepare(FitHostCache& c, size_t n_pts, size_t n_vox) {
+    cudaError_t e = cudaSuccess;
+    if (!c.ready) {
+        for (cudaStream_t* st : {&c.s_in, &c.s_fit, &c.s_out})
+            if ((e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        for (int k = 0; k < FitHostCache::kChunks; ++k) {
+            if ((e = cudaEventCreateWithFlags(&c.in_done[k], cudaEventDisableTiming)) != cudaSuccess) return e;
+            if ((e = cudaEventCreateWithFlags(&c.fit_done[k], cudaEventDisableTiming)) != cudaSuccess) return e;
+        }
+        c.ready = true;
+    }
+    if (n_pts > c.cap_pts) {
+        if (c.d_pts) cudaFree(c.d_pts);
+        c.d_pts = nullptr;
+        c.cap_pts = 0;
+        if ((e = cudaMalloc((void**)&c.d_pts, sizeof(float) * 9 * n_pts)) != cudaSuccess) return e;
+        c.cap_pts = n_pts;
+    }
+    if (n_vox > c.cap_vox) {
+        if (c.d_off) cudaFree(c.d_off);
+        if (c.d_out) cudaFree(c.d_out);
+        c.d_off = nullptr;
+        c.d_out = nullptr;
+        c.cap_vox = 0;
+        if ((e = cudaMalloc((void**)&c.d_off, sizeof(long long) * (n_vox + 1))) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&c.d_out, sizeof(vmp_fit_rec) * n_vox)) != cudaSuccess) return e;
+        c.cap_vox = n_vox;
+    }
+    return e;
+}
+}  // namespace
+}  // namespace vmp
+
 extern "C" vmp_status vmp_fit_planes(const float* xyz, const float* cov, const long long* offsets, int n_vox,
                                      long long n_pts, const vmp_fit_params* params, vmp_fit_rec* out) {
     if (!params_ok(params) || n_vox < 0 || n_pts < 0) return VMP_ERR_INVALID_ARG;
@@ -517,47 +567,47 @@ extern "C" vmp_status vmp_fit_planes(const float* xyz, const float* cov, const l
     if (offsets[0] != 0 || offsets[n_vox] != n_pts) return VMP_ERR_INVALID_ARG;
     for (int v = 0; v < n_vox; ++v)
         if (offsets[v + 1] < offsets[v]) return VMP_ERR_INVALID_ARG;
-    cudaStream_t st = nullptr;
-    float* d_pts = nullptr;
-    long long* d_off = nullptr;
-    vmp_fit_rec* d_out = nullptr;
-    vmp_status rc = VMP_OK;
-    const size_t pts_bytes = sizeof(float) * 9 * (size_t)(n_pts > 0 ? n_pts : 1);
-    do {
-        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { rc = VMP_ERR_CUDA; break; }
-        if (cudaMalloc((void**)&d_pts, pts_bytes) != cudaSuccess ||
-            cudaMalloc((void**)&d_off, sizeof(long long) * ((size_t)n_vox + 1)) != cudaSuccess ||
-            cudaMalloc((void**)&d_out, sizeof(vmp_fit_rec) * (size_t)n_vox) != cudaSuccess) {
-            rc = VMP_ERR_OUT_OF_MEMORY;
-            break;
+    FitHostCache& c = fit_host_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    cudaError_t e = fit_host_prepare(c, (size_t)(n_pts > 0 ? n_pts : 1), (size_t)n_vox);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? VMP_ERR_OUT_OF_MEMORY : VMP_ERR_CUDA;
+    }
+    const size_t N = (size_t)n_pts;
+    float* d_xyz = c.d_pts;
+    float* d_cov = c.d_pts + 3 * N;
+    const int K = n_vox >= 4096 ? FitHostCache::kChunks : 1;
+    // the chunk's voxels [v[k], v[k+1]) own points [offsets[v[k]], offsets[v[k+1]])
+    int vb[FitHostCache::kChunks + 1];
+    for (int k = 0; k <= K; ++k) vb[k] = (int)((long long)n_vox * k / K);
+    e = cudaMemcpyAsync(c.d_off, offsets, sizeof(long long) * ((size_t)n_vox + 1), cudaMemcpyHostToDevice, c.s_in);
+    for (int k = 0; k < K && e == cudaSuccess; ++k) {
+        const size_t p0 = (size_t)offsets[vb[k]], p1 = (size_t)offsets[vb[k + 1]];
+        for (int q = 0; q < 9 && e == cudaSuccess && p1 > p0; ++q) {
+            const float* src = (q < 3 ? xyz + (size_t)q * N : cov + (size_t)(q - 3) * N) + p0;
+            float* dst = (q < 3 ? d_xyz + (size_t)q * N : d_cov + (size_t)(q - 3) * N) + p0;
+            e = cudaMemcpyAsync(dst, src, sizeof(float) * (p1 - p0), cudaMemcpyHostToDevice, c.s_in);
         }
-        float* d_xyz = d_pts;
-        float* d_cov = d_pts + 3 * (size_t)n_pts;
-        if (n_pts > 0 &&
-            (cudaMemcpyAsync(d_xyz, xyz, sizeof(float) * 3 * (size_t)n_pts, cudaMemcpyHostToDevice, st) !=
-                 cudaSuccess ||
-             cudaMemcpyAsync(d_cov, cov, sizeof(float) * 6 * (size_t)n_pts, cudaMemcpyHostToDevice, st) !=
-                 cudaSuccess)) {
-            rc = VMP_ERR_CUDA;
-            break;
-        }
-        if (cudaMemcpyAsync(d_off, offsets, sizeof(long long) * ((size_t)n_vox + 1), cudaMemcpyHostToDevice, st) !=
-                cudaSuccess ||
-            fit_enqueue(d_xyz, d_cov, d_off, n_vox, n_pts, params, d_out, st) != cudaSuccess ||
-            cudaMemcpyAsync(out, d_out, sizeof(vmp_fit_rec) * (size_t)n_vox, cudaMemcpyDeviceToHost, st) !=
-                cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess) {
-            rc = VMP_ERR_CUDA;
-            break;
-        }
-    } while (false);
-    if (rc != VMP_OK) cudaGetLastError();
-    if (st) cudaStreamSynchronize(st);
-    if (d_pts) cudaFree(d_pts);
-    if (d_off) cudaFree(d_off);
-    if (d_out) cudaFree(d_out);
-    if (st) cudaStreamDestroy(st);
-    return rc;
+        if (e == cudaSuccess) e = cudaEventRecord(c.in_done[k], c.s_in);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c.s_fit, c.in_done[k], 0);
+        if (e == cudaSuccess)
+            e = fit_enqueue(d_xyz, d_cov, c.d_off + vb[k], vb[k + 1] - vb[k], n_pts, params, c.d_out + vb[k], c.s_fit);
+        if (e == cudaSuccess) e = cudaEventRecord(c.fit_done[k], c.s_fit);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c.s_out, c.fit_done[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(out + vb[k], c.d_out + vb[k], sizeof(vmp_fit_rec) * (size_t)(vb[k + 1] - vb[k]),
+                                cudaMemcpyDeviceToHost, c.s_out);
+    }
+    const cudaError_t e2 = cudaStreamSynchronize(c.s_out);
+    cudaStreamSynchronize(c.s_in);
+    cudaStreamSynchronize(c.s_fit);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return VMP_ERR_CUDA;
+    }
+    return VMP_OK;
 }
 
 extern "C" vmp_status vmp_fit_profile(int on) {
