@@ -571,10 +571,18 @@ def roofline_of(prof):
     bytes_per_launch = per_unit * prof[dom]["items"] / launches
     peak, peak_src = load_peaks()
     achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    phases = {}
+    for k, (pu, _) in ALGO_BYTES.items():  # every phase with a byte count, the dominant one included
+        nl = max(1, prof[k]["launches"])
+        ms = prof[k]["ms"] / nl
+        if ms > 0:
+            a = pu * prof[k]["items"] / nl / (ms * 1e-3) / 1e9
+            phases[k] = {"achieved": a, "frac": a / peak, "avg_launch_ms": ms}
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": load_traffic(dom, prof[dom]["items"] / launches),
             "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
-            "bytes_per_unit": per_unit, "unit_of_work": unit_name, "peak_source": peak_src}
+            "bytes_per_unit": per_unit, "unit_of_work": unit_name, "peak_source": peak_src,
+            "phases": phases}
 
 
 SERVE_NAME = ("64 independent streams, each its own seeded scene and trajectory (even: 20x20x5 m room, "
