@@ -353,6 +353,10 @@ struct vmp_stream_s {
     int cloud_n = 0;     // points of the last processed scan's undistorted cloud
     bool blocking_wait = false;  // vmp_set_wait_mode
     cudaEvent_t done_ev = nullptr;
+    // the IMU predict chain runs beside the time sort (they share no data):
+    // forked onto st_side and joined before the undistortion
+    cudaStream_t st_side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
     // the stream's own CUDA stream, resolved after the call's final sync
     struct ProfRec { int slot; int items_kind; cudaEvent_t a, b; };
@@ -517,6 +521,9 @@ vmp_status vmp_destroy(vmp_stream_t s) {
     }
     if (s->h_hdr) cudaFreeHost(s->h_hdr);
     if (s->done_ev) cudaEventDestroy(s->done_ev);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->st_side) cudaStreamDestroy(s->st_side);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return VMP_OK;
@@ -555,6 +562,9 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     } while (0)
     CREATE_TRY(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
     CREATE_TRY(cudaEventCreateWithFlags(&s->done_ev, cudaEventBlockingSync | cudaEventDisableTiming));
+    CREATE_TRY(cudaStreamCreateWithFlags(&s->st_side, cudaStreamNonBlocking));
+    CREATE_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    CREATE_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
     const int max_pts = cfg.max_scan_points;
     const int max_imu = cfg.max_imu_per_scan;
     s->sin_deg = std::sin(cfg.angle_cov * 0.017453293);  // pcl_macros.h DEG2RAD
@@ -900,12 +910,21 @@ static vmp_status finish_result_host(vmp_stream_t s, int n_raw, vmp_result* out)
 static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     const vmp_config& cfg = s->cfg;
     cudaStream_t st = s->st;
-    s->pbeg();
-    launch_time_sort(s->s, nb, s->ss, st);
-    s->pend(VMP_PROF_TIME_SORT, 0);
-    s->pbeg();
-    launch_predict_chain2(s->f, s->s, st);
-    s->pend(VMP_PROF_PREDICT, -1);
+    if (s->prof_on) {  // one phase after the other, each timed on the stream
+        s->pbeg();
+        launch_time_sort(s->s, nb, s->ss, st);
+        s->pend(VMP_PROF_TIME_SORT, 0);
+        s->pbeg();
+        launch_predict_chain2(s->f, s->s, st);
+        s->pend(VMP_PROF_PREDICT, -1);
+    } else {  // the predict chain beside the time sort
+        cudaEventRecord(s->ev_fork, st);
+        cudaStreamWaitEvent(s->st_side, s->ev_fork, 0);
+        launch_predict_chain2(s->f, s->s, s->st_side);
+        cudaEventRecord(s->ev_join, s->st_side);
+        launch_time_sort(s->s, nb, s->ss, st);
+        cudaStreamWaitEvent(st, s->ev_join, 0);
+    }
     s->pbeg();
     launch_undistort(s->f, s->s, nb, st);
     s->pend(VMP_PROF_UNDISTORT, 0);
