@@ -323,6 +323,11 @@ vmp_status vmp_std_plane_voxels(const float* pts, int stride, int n, double voxe
  * the FP64 division (host arrays of n; the two must agree bit for bit). */
 vmp_status vmp_test_division(const double* a, const double* b, int n, double* by_recip, double* by_div);
 
+/* Test hook: lio::calcBodyCov (commons.cpp:18-45) of n points on the device
+ * (host arrays; pts_out receives the points after the z == 0 fix). */
+vmp_status vmp_test_body_cov(const double* pts, int n, double range_inc, double degree_inc, double* pts_out,
+                             double* cov);
+
 /* The same leaf-centroid downsample for callers that cannot allocate device
  * memory (no counterpart in the reference): a real-time sensor thread that
  * must not call cudaMalloc/cudaFree, or a host framework whose own allocator

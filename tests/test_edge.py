@@ -153,3 +153,23 @@ def test_shared_divisor_division_is_exact():
     rc = load().vmp_test_division(dp(a), dp(b), n, dp(by_recip), dp(by_div))
     assert rc == 0
     assert np.array_equal(by_recip.view(np.uint64), by_div.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_body_cov_bit_exact(oracle_lib):
+    """calcBodyCov on the device (normalisations through one reciprocal per
+    vector with Markstein's correction) against the oracle, bit for bit,
+    including points with z == 0 (fixed to 0.001 in place, as the reference)."""
+    from voxelmapplus_fastlio2_gb300._lib import load
+    rng = np.random.default_rng(23)
+    n = 50000
+    pts = rng.normal(0, 8, (n, 3))
+    pts[::97, 2] = 0.0
+    pts[::89] = pts[::89].astype(np.float32).astype(np.float64)
+    gp, gc = np.zeros((n, 3)), np.zeros((n, 9))
+    op, oc = np.zeros((n, 3)), np.zeros((n, 9))
+    dp = lambda x: C.c_void_p(x.ctypes.data)
+    assert load().vmp_test_body_cov(dp(pts), n, 0.04, 0.1, dp(gp), dp(gc)) == 0
+    oracle_lib.orc_calc_body_cov(_dp(pts), n, 0.04, 0.1, _dp(op), _dp(oc))
+    assert np.array_equal(gp, op)
+    assert np.array_equal(gc.view(np.uint64), oc.view(np.uint64))

@@ -10,6 +10,8 @@
 //                                                                  lio_builder.cpp:155-163, 185-211, 231-246
 // The sorts are stable, so equal keys keep their input order (the reference's
 // std::sort leaves that order unspecified).
+#include <cmath>
+
 #include "kernels.cuh"
 
 namespace vmp {
@@ -239,6 +241,18 @@ void launch_body_cov(DScan& s, int n_max, double range_inc, double sin_deg, cuda
     VMP_NOTE_LAUNCH(); k_body_cov<<<grid_for(n_max), kPtThreads, 0, st>>>(s.down, s.d_n_down, range_inc, sin_deg, s.pl, s.covl);
 }
 
+// Test hook: calcBodyCov on the device for explicit points.
+__global__ void k_body_cov_check(const double* pts, int n, double range_inc, double sin_deg, double* pts_out,
+                                 double* cov) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double pb[3] = {pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]};
+        double c[9];
+        calc_body_cov(pb, range_inc, sin_deg, c);
+        for (int k = 0; k < 3; ++k) pts_out[i * 3 + k] = pb[k];
+        for (int k = 0; k < 9; ++k) cov[i * 9 + k] = c[k];
+    }
+}
+
 // ---------------------------------------------------------------- map batch
 __global__ void k_map_batch(const DFilter* __restrict__ f, const float4* __restrict__ pts, const int* d_n,
                             const double* __restrict__ pl, const double* __restrict__ covl, int full,
@@ -386,3 +400,29 @@ void launch_output_cloud(const DFilter* f, const DScan& s, int n, int frame, flo
 }
 
 }  // namespace vmp
+
+// Test hook (host arrays): lio::calcBodyCov (commons.cpp:18-45) of n points on
+// the device, with the angle noise in degrees as vmp_config.angle_cov.
+extern "C" vmp_status vmp_test_body_cov(const double* pts, int n, double range_inc, double degree_inc,
+                                        double* pts_out, double* cov) {
+    if (n < 0 || (n > 0 && (!pts || !pts_out || !cov))) return VMP_ERR_INVALID_ARG;
+    if (n == 0) return VMP_OK;
+    double* d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 15 * (size_t)n) != cudaSuccess) return VMP_ERR_OUT_OF_MEMORY;
+    const double sin_deg = std::sin(degree_inc * 0.017453293);  // as vmp_create forms it
+    cudaError_t e = cudaMemcpy(d, pts, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        VMP_NOTE_LAUNCH();
+        vmp::k_body_cov_check<<<(n + 255) / 256 < 1216 ? (n + 255) / 256 : 1216, 256>>>(
+            d, n, range_inc, sin_deg, d + 3 * (size_t)n, d + 6 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(pts_out, d + 3 * (size_t)n, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(cov, d + 6 * (size_t)n, sizeof(double) * 9 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return VMP_ERR_CUDA;
+    }
+    return VMP_OK;
+}
