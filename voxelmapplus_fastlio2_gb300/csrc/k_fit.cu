@@ -378,7 +378,7 @@ __device__ __forceinline__ void voxel_terms(const FitArgs& a, long long p0, long
 // (the points of the 32 voxels were just read: their xyz mostly comes from
 // L2).
 template <int MODE>
-__global__ void __launch_bounds__(kFitWarps * 32, MODE == FIT_FP64 ? 1 : 3) k_fit(FitArgs a) {
+__global__ void __launch_bounds__(kFitWarps * 32, MODE == FIT_FP64 ? 1 : 4) k_fit(FitArgs a) {
     using T = typename FitTypes<MODE>::T;
     const int lane = threadIdx.x & 31;
     const long long v0 = ((long long)blockIdx.x * kFitWarps + (threadIdx.x >> 5)) * 32;
