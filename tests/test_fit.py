@@ -187,3 +187,18 @@ def test_fit_device_entry_matches_host_entry():
     torch.cuda.synchronize()
     dev = d_out.cpu().numpy().view(abi.fit_rec_dtype()).reshape(-1)
     assert dev.tobytes() == host.tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [fit.FP64, fit.FP32, fit.FP32C])
+def test_fit_record_depends_only_on_its_voxel(mode):
+    """A voxel's record is the same whatever voxels share its warp: the
+    batch shifted by 13 voxels (other warp groups) gives the same bytes."""
+    xyz, cov, off = fit.synth_voxels(3000, seed=43)
+    full = fit.fit_planes(xyz, cov, off, mode=mode)
+    s = 13
+    sub_off = np.ascontiguousarray(off[s:] - off[s])
+    sub_xyz = np.ascontiguousarray(xyz[:, off[s]:])
+    sub_cov = np.ascontiguousarray(cov[:, off[s]:])
+    part = fit.fit_planes(sub_xyz, sub_cov, sub_off, mode=mode)
+    assert part.tobytes() == full[s:].tobytes()

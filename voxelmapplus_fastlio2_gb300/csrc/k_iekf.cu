@@ -54,14 +54,20 @@ __device__ inline void residual_point(int i, const DScan& s, const DMap& m, cons
     const bool inr = voxel_index(pw, m.voxel_size, m.voxel_inv, key);
     const uint32_t rec = inr ? map_find(m, pack_key(key[0], key[1], key[2])) : kNoRec;
     const double* cl = s.covl + (size_t)i * 9;
+    // u = R^T n and r_cov = u^T S u of a plane found in this call: the
+    // accumulation below uses the same values (same operations), so they are
+    // formed once; a miss recomputes them from the stored normal
+    double u[3], r_cov = 0.0, n[3], r = 0.0;
+    bool fresh = false;
+    int valid = 0;
     if (rec != kNoRec) {
         const RecHot hot = m.hot[rec];
         if (hot.flags & F_PLANE) {
-            const double* n = hot.norm;
+            for (int c = 0; c < 3; ++c) n[c] = hot.norm[c];
             const double p2m[3] = {pw[0] - hot.mean[0], pw[1] - hot.mean[1], pw[2] - hot.mean[2]};
-            const double r = dot3(n, p2m);
-            // u = R^T n ; v = n x p_l
-            double u[3], v[3], su[3], pv[3], pn[3];
+            r = dot3(n, p2m);
+            // v = n x p_l
+            double v[3], su[3], pv[3], pn[3];
             for (int c = 0; c < 3; ++c) u[c] = fma(rwl[6 + c], n[2], fma(rwl[3 + c], n[1], rwl[c] * n[0]));
             v[0] = fma(n[1], pl[2], -n[2] * pl[1]);
             v[1] = fma(n[2], pl[0], -n[0] * pl[2]);
@@ -75,20 +81,30 @@ __device__ inline void residual_point(int i, const DScan& s, const DMap& m, cons
             const double t2 = fma(v[2], pv[2], fma(v[1], pv[1], v[0] * pv[0]));
             const double t3 = fma(n[2], pn[2], fma(n[1], pn[1], n[0] * pn[0]));
             const double sigma = t1 + t2 + t3;
-            s.rvalid[i] = fabs(r) < 3.0 * sqrt(sigma) ? 1 : 0;
+            r_cov = t1;
+            fresh = true;
+            valid = fabs(r) < 3.0 * sqrt(sigma) ? 1 : 0;
+            s.rvalid[i] = valid;
             s.rnorm[i * 3] = n[0]; s.rnorm[i * 3 + 1] = n[1]; s.rnorm[i * 3 + 2] = n[2];
             s.rres[i] = r;
         } else {
             s.rvalid[i] = 0;
         }
+    } else {
+        // a miss keeps the record of the previous iteration / scan
+        valid = s.rvalid[i];
+        if (valid) {
+            for (int c = 0; c < 3; ++c) n[c] = s.rnorm[i * 3 + c];
+            r = s.rres[i];
+        }
     }
-    if (!s.rvalid[i]) return;  // a miss keeps the record of the previous iteration / scan
-    const double n[3] = {s.rnorm[i * 3], s.rnorm[i * 3 + 1], s.rnorm[i * 3 + 2]};
-    const double r = s.rres[i];
-    double u[3], su[3];
-    for (int c = 0; c < 3; ++c) u[c] = fma(rwl[6 + c], n[2], fma(rwl[3 + c], n[1], rwl[c] * n[0]));
-    for (int c = 0; c < 3; ++c) su[c] = fma(cl[c * 3 + 2], u[2], fma(cl[c * 3 + 1], u[1], cl[c * 3] * u[0]));
-    const double r_cov = fma(u[2], su[2], fma(u[1], su[1], u[0] * su[0]));
+    if (!valid) return;
+    if (!fresh) {
+        double su[3];
+        for (int c = 0; c < 3; ++c) u[c] = fma(rwl[6 + c], n[2], fma(rwl[3 + c], n[1], rwl[c] * n[0]));
+        for (int c = 0; c < 3; ++c) su[c] = fma(cl[c * 3 + 2], u[2], fma(cl[c * 3 + 1], u[1], cl[c * 3] * u[0]));
+        r_cov = fma(u[2], su[2], fma(u[1], su[1], u[0] * su[0]));
+    }
     const double w = r_cov < 0.0002 ? 5000 : 1.0 / r_cov;
     // J = [n, (-rot^T n) x q, ...]  with q = rot_ext p_l + pos_ext
     double J[NJ], q[3], v1[3];
