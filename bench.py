@@ -838,9 +838,22 @@ def main_io(args, rank, ws, barrier, allmax, dist):
     n_in = sum(len(m) for m in msgs)
     n_out = 2 * sum(len(w) for w in world)
     key = np.ascontiguousarray(np.concatenate(world[-10:]))
+    # back to back (the timings inside the sequence above interleave the
+    # CPU restatement's scans, during which the GPU idles and clocks down):
+    # both output clouds of the last scan, then every message decoded again
+    R = len(world)
+    n_out_b = 2 * R * len(world[-1])
+    tc_out, _ = _wall(lambda: (o.output_cloud(1), o.output_cloud(0)), R)
+    tc_dec, _ = _wall(lambda: [oracle.livox_decode(m, 1, 0.1, 200.0) for m in msgs], 1)
     comp["livox_decode"] = {"messages": len(msgs), "points_in": n_in, "points_kept": n_dec,
-                            "cpu_points_per_s": n_in / t_dec_c}
-    comp["output_clouds"] = {"points": n_out, "cpu_points_per_s": n_out / t_out_c}
+                            "cpu_points_per_s": n_in / tc_dec, "cpu_points_per_s_in_sequence": n_in / t_dec_c}
+    comp["output_clouds"] = {"points": n_out_b, "cpu_points_per_s": n_out_b / (R * tc_out),
+                             "cpu_points_per_s_in_sequence": n_out / t_out_c}
+    if ours:
+        g.output_cloud(1)
+        tg_out, _ = _wall(lambda: (g.output_cloud(1), g.output_cloud(0)), R)
+        g.livox_decode(msgs[0], 1, 0.1, 200.0, copy_out=False)
+        tg_dec, _ = _wall(lambda: [g.livox_decode(m, 1, 0.1, 200.0, copy_out=False) for m in msgs], 1)
     mk = np.zeros(100000, dtype=abi.plane_marker_dtype())
     tc, nm = _wall(lambda: o.lib.orc_map_planes(o.h, mk.ctypes.data_as(C.POINTER(abi.vmp_plane_marker)), 100000), 3)
     info = abi.vmp_map_info()
@@ -855,10 +868,10 @@ def main_io(args, rank, ws, barrier, allmax, dist):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)"}
     cfg_line = {"workload": uname + "; Livox messages made from its scans (20 B per point), key cloud = the last "
                                     "10 world clouds", "components": comp}
-    cpu = {"value": n_in / t_dec_c, "unit": "points/s", "cores": 1, "kind": "port",
-           "sample": f"{len(msgs)} Livox messages, CPU restatement of livox2pcl on 1 thread"}
+    cpu = {"value": n_in / tc_dec, "unit": "points/s", "cores": 1, "kind": "port",
+           "sample": f"{len(msgs)} Livox messages back to back, CPU restatement of livox2pcl on 1 thread"}
     if not ours:
-        print(json.dumps(dict(base, value=cpu["value"], impl="reference", ms_per_step=1e3 * t_dec_c / len(msgs),
+        print(json.dumps(dict(base, value=cpu["value"], impl="reference", ms_per_step=1e3 * tc_dec / len(msgs),
                               config=cfg_line, cpu_baseline=cpu,
                               e2e={"value": cpu["value"], "unit": "points/s", "h2d_bytes_per_step": 0,
                                    "d2h_bytes_per_step": 0})))
@@ -867,10 +880,11 @@ def main_io(args, rank, ws, barrier, allmax, dist):
     comp["map_planes"].update({"gpu_ms": 1e3 * tg, "gpu_markers": int(len(ng))})
     tg, gs = _wall(lambda: fit.std_plane_voxels(key, 1.0, 10, 0.01), 3)
     comp["std_plane_voxels"].update({"gpu_ms": 1e3 * tg, "gpu_voxels": int(len(gs))})
-    comp["livox_decode"]["gpu_points_per_s"] = n_in / t_dec_g
-    comp["output_clouds"]["gpu_points_per_s"] = n_out / t_out_g
-    v = n_in / t_dec_g
-    print(json.dumps(dict(base, value=v, ms_per_step=1e3 * t_dec_g / len(msgs), config=cfg_line,
+    comp["livox_decode"].update({"gpu_points_per_s": n_in / tg_dec, "gpu_points_per_s_in_sequence": n_in / t_dec_g})
+    comp["output_clouds"].update({"gpu_points_per_s": n_out_b / (R * tg_out),
+                                  "gpu_points_per_s_in_sequence": n_out / t_out_g})
+    v = n_in / tg_dec
+    print(json.dumps(dict(base, value=v, ms_per_step=1e3 * tg_dec / len(msgs), config=cfg_line,
                           e2e={"value": v, "unit": "points/s", "h2d_bytes_per_step": int(20 * n_in / len(msgs)),
                                "d2h_bytes_per_step": 8},
                           gpu_launches=int(g.lib.vmp_launch_count() - l0), cpu_baseline=cpu)))
