@@ -189,16 +189,24 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per unit of
+# work of each profiled phase, from ncu captures on GB300: one steady scan of
+# the urban block at 50k rays for the scan phases, k_fit<FP32C> on 200 000
+# voxels / 13.16 M points for the fit.  The traffic grows in proportion to
+# the units, so a launch's traffic is this times its units.
+TRAFFIC_PER_UNIT = {
+    "residual": 151.0,   # per downsampled point x IEKF iteration
+    "map_state": 996.0,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov
+    "undistort": 17.3,   # per raw point
+    "fit_fp32c": 51.5,   # per point
+}
+
+
 def load_traffic(phase, units_per_launch):
-    """DRAM bytes per launch of the phase from the committed ncu summary
-    (profiles/traffic.json holds bytes per unit of work)."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
-    try:
-        with open(path) as f:
-            t = json.load(f).get(phase)
-        return None if t is None else float(t["bytes_per_unit"]) * units_per_launch
-    except Exception:
-        return None
+    """DRAM bytes per launch of the phase (TRAFFIC_PER_UNIT x units), or None
+    where no capture covers it."""
+    t = TRAFFIC_PER_UNIT.get(phase)
+    return None if t is None else t * units_per_launch
 
 
 def pkg_arrays(p):
