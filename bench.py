@@ -109,12 +109,13 @@ def workload(args, rank, name=None):
     from voxelmapplus_fastlio2_gb300 import abi, synth
     if (name or args.workload) == "urban":
         kind, pts, leaf, cap, iters = synth.KIND_URBAN, 200000, 0.1, 4000000, 4
-        name = "urban block 100x100x20 m, spinning 128-beam, 200k rays/scan"
+        name = "urban block 100x100x20 m, spinning 128-beam, {}k rays/scan"
     else:
         kind, pts, leaf, cap, iters = synth.KIND_ROOM, 20000, 0.2, 100000, 5
-        name = "room 20x20x5 m, rosette, 20k rays/scan"
+        name = "room 20x20x5 m, rosette, {}k rays/scan"
     if args.points:
         pts = args.points
+    name = name.format(f"{pts / 1000:g}")
     if getattr(args, "map_capacity", None):
         cap = args.map_capacity
     cfg = abi.default_config(scan_resolution=leaf, map_capacity=cap, ieskf_max_iter=iters,
@@ -200,6 +201,34 @@ TRAFFIC_PER_UNIT = {
     "undistort": 17.3,   # per raw point
     "fit_fp32c": 51.5,   # per point
 }
+
+
+# FP64 warp instructions (ncu sm__inst_executed_pipe_fp64.sum) per unit of
+# work of the FP64-bound phases, from the same urban-block capture (one
+# steady scan, 50k rays).  These phases are bound by the FP64 pipe, not by
+# HBM: an FP64 warp instruction holds an SM sub-partition's FP64 pipe for 64
+# cycles whatever its active lanes (a dependent-DFMA micro-probe on this
+# GB300), so the pipe's peak is 4 x SMs x clock / 64 warp instructions/s.
+FP64_PER_UNIT = {
+    "residual": 5.81,   # per downsampled point x IEKF iteration
+    "undistort": 7.11,  # per raw point
+    "body_cov": 6.97,   # per downsampled point
+    "map_batch": 6.66,  # per batch point
+    "map_state": 20.2,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov
+}
+FP64_CYCLES_PER_WARP_INSTR = 64
+
+
+def fp64_peak():
+    """FP64 warp instructions/s of the whole GPU at its maximum SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        mhz = 2070.0
+    return 4 * sms * mhz * 1e6 / FP64_CYCLES_PER_WARP_INSTR
 
 
 def load_traffic(phase, units_per_launch):
@@ -586,11 +615,25 @@ def roofline_of(prof):
         if ms > 0:
             a = pu * prof[k]["items"] / nl / (ms * 1e-3) / 1e9
             phases[k] = {"achieved": a, "frac": a / peak, "avg_launch_ms": ms}
+    # the same phases against the FP64 pipe, which is what bounds them
+    p64 = fp64_peak()
+    f64 = {}
+    for k, per in FP64_PER_UNIT.items():
+        nl = max(1, prof[k]["launches"])
+        ms = prof[k]["ms"] / nl
+        if ms > 0 and prof[k]["items"] > 0:
+            a = per * prof[k]["items"] / nl / (ms * 1e-3)
+            f64[k] = {"achieved": a, "frac": a / p64, "avg_launch_ms": ms, "instr_per_unit": per}
+    fp64 = {"bound": "fp64", "unit": "FP64 warp instructions/s", "peak": p64,
+            "peak_source": "4 x SMs x max SM clock / 64 cycles per FP64 warp instruction (micro-probe)",
+            "phases": f64}
+    if dom in f64:
+        fp64.update({"kernel": dom, "achieved": f64[dom]["achieved"], "frac": f64[dom]["frac"]})
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": load_traffic(dom, prof[dom]["items"] / launches),
             "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
             "bytes_per_unit": per_unit, "unit_of_work": unit_name, "peak_source": peak_src,
-            "phases": phases}
+            "phases": phases, "fp64": fp64}
 
 
 SERVE_NAME = ("64 independent streams, each its own seeded scene and trajectory (even: 20x20x5 m room, "

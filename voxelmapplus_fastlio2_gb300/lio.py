@@ -174,8 +174,8 @@ class LIOBuilder:
         stays on the device for process_decoded."""
         livox = np.ascontiguousarray(livox, dtype=abi.livox_dtype())
         n = len(livox)
-        out = np.zeros((max(1, n), 4), dtype=np.float32) if copy_out else None
-        inten = np.zeros(max(1, n), dtype=np.float32) if copy_out else None
+        out = np.empty((max(1, n), 4), dtype=np.float32) if copy_out else None
+        inten = np.empty(max(1, n), dtype=np.float32) if copy_out else None
         m = C.c_int()
         last = C.c_float()
         check(self.h, self.lib.vmp_livox_decode(self.h, C.c_void_p(livox.ctypes.data), n, filter_num, range_min,
@@ -197,8 +197,8 @@ class LIOBuilder:
         undistorted cloud: (points (n, 4) float32, intensity (n,))."""
         n = C.c_int()
         check(self.h, self.lib.vmp_output_cloud(self.h, frame, None, None, 0, C.byref(n)))
-        out = np.zeros((max(1, n.value), 4), dtype=np.float32)
-        inten = np.zeros(max(1, n.value), dtype=np.float32)
+        out = np.empty((max(1, n.value), 4), dtype=np.float32)
+        inten = np.empty(max(1, n.value), dtype=np.float32)
         check(self.h, self.lib.vmp_output_cloud(self.h, frame, C.c_void_p(out.ctypes.data),
                                                 C.c_void_p(inten.ctypes.data), n.value, C.byref(n)))
         return out[: n.value], inten[: n.value]
