@@ -81,6 +81,14 @@ def test_livox_decode_matches_oracle(filter_num):
     # an empty decode leaves nothing to process
     e, _, _ = g.livox_decode(a[:0], filter_num, 0.5, 20.0)
     assert len(e) == 0
+    # a message whose points all fail the line test keeps none
+    b = a.copy()
+    b["line"] = 4
+    e, _, _ = g.livox_decode(b, filter_num, 0.5, 20.0)
+    assert len(e) == 0 and len(oracle.livox_decode(b, filter_num, 0.5, 20.0)[0]) == 0
+    # and the next message decodes as before
+    pts2, _, last2 = g.livox_decode(a, filter_num, 0.5, 20.0)
+    assert pts2.tobytes() == opts.tobytes() and last2 == last
     g.close()
 
 

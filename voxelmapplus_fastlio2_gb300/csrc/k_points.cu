@@ -341,26 +341,57 @@ __global__ void k_livox_keep(const vmp_livox_point* __restrict__ in, int n, cons
         keep[i] = k;
     }
 }
+// filter_num == 1 (every point that passes the line / tag test goes on to
+// the range test): both tests in one pass, one scan instead of two.
+__global__ void k_livox_keep1(const vmp_livox_point* __restrict__ in, int n, double rmin2, double rmax2,
+                              uint32_t* __restrict__ keep, int* d_n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_n = n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const vmp_livox_point p = in[i];
+        uint32_t k = 0;
+        if (livox_line_tag_ok(p)) {
+            const float sq = p.x * p.x + p.y * p.y + p.z * p.z;
+            const double d = (double)sq;
+            k = (d > rmin2 && d < rmax2) ? 1u : 0u;
+        }
+        keep[i] = k;
+    }
+}
+// The kept points in order; the thread of the last one also writes its time
+// (ms, as float bits) to *last_t_bits, so the host reads count and time at once.
 __global__ void k_livox_scatter(const vmp_livox_point* __restrict__ in, int n, const uint32_t* __restrict__ keep,
-                                const uint32_t* __restrict__ pos, float4* __restrict__ raw, float* __restrict__ raw_int) {
+                                const uint32_t* __restrict__ pos, const int* __restrict__ d_total,
+                                float4* __restrict__ raw, float* __restrict__ raw_int, int* last_t_bits) {
+    const uint32_t total = (uint32_t)*d_total;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!keep[i]) continue;
         const vmp_livox_point p = in[i];
         const uint32_t o = pos[i];
-        raw[o] = make_float4(p.x, p.y, p.z, (float)p.offset_time / 1000000.0f);  // ns -> ms
+        const float t = (float)p.offset_time / 1000000.0f;  // ns -> ms
+        raw[o] = make_float4(p.x, p.y, p.z, t);
         raw_int[o] = (float)p.reflectivity;
+        if (o + 1u == total) *last_t_bits = __float_as_int(t);
     }
 }
 
 void launch_livox_decode(DScan& s, const vmp_livox_point* d_in, int n, int filter_num, double range_min,
                          double range_max, ScanScratch& sc, cudaStream_t st) {
     const int g = grid_for(n);
-    VMP_NOTE_LAUNCH(); k_livox_valid<<<g, kPtThreads, 0, st>>>(d_in, n, s.flags, s.d_n_in);
-    exclusive_scan_u32(s.flags, s.scan_out, s.d_n_in, s.d_n_in + 1, sc, st);
-    VMP_NOTE_LAUNCH(); k_livox_keep<<<g, kPtThreads, 0, st>>>(d_in, n, s.flags, s.scan_out, (unsigned)filter_num,
-                                                             range_min * range_min, range_max * range_max, s.sort_k);
+    if (filter_num == 1) {
+        VMP_NOTE_LAUNCH();
+        k_livox_keep1<<<g, kPtThreads, 0, st>>>(d_in, n, range_min * range_min, range_max * range_max, s.sort_k,
+                                                s.d_n_in);
+    } else {
+        VMP_NOTE_LAUNCH(); k_livox_valid<<<g, kPtThreads, 0, st>>>(d_in, n, s.flags, s.d_n_in);
+        exclusive_scan_u32(s.flags, s.scan_out, s.d_n_in, s.d_n_in + 1, sc, st);
+        VMP_NOTE_LAUNCH();
+        k_livox_keep<<<g, kPtThreads, 0, st>>>(d_in, n, s.flags, s.scan_out, (unsigned)filter_num,
+                                               range_min * range_min, range_max * range_max, s.sort_k);
+    }
     exclusive_scan_u32(s.sort_k, s.sort_v, s.d_n_in, s.d_n_raw, sc, st);
-    VMP_NOTE_LAUNCH(); k_livox_scatter<<<g, kPtThreads, 0, st>>>(d_in, n, s.sort_k, s.sort_v, s.raw, s.raw_int);
+    VMP_NOTE_LAUNCH();
+    k_livox_scatter<<<g, kPtThreads, 0, st>>>(d_in, n, s.sort_k, s.sort_v, s.d_n_raw, s.raw, s.raw_int,
+                                              s.d_n_in + 3);
 }
 
 // ---------------------------------------------------------------- output clouds

@@ -1138,16 +1138,16 @@ vmp_status vmp_livox_decode(vmp_stream_t s, const vmp_livox_point* pts, int n, i
     s->io_h2d += (long long)sizeof(vmp_livox_point) * n;
     launch_livox_decode(s->s, d_in, n, filter_num, range_min, range_max, s->sc, s->st);
     VMP_TRY(cudaGetLastError(), "livox decode");
+    // the count and the last kept point's time (written by the scatter) in one read
     VMP_TRY(cudaMemcpyAsync(s->h_int, s->s.d_n_raw, sizeof(int), cudaMemcpyDeviceToHost, s->st), "count");
+    VMP_TRY(cudaMemcpyAsync(s->h_int + 1, s->s.d_n_in + 3, sizeof(int), cudaMemcpyDeviceToHost, s->st), "last time");
     VMP_TRY(cudaStreamSynchronize(s->st), "livox decode");
     const int m = s->h_int[0];
     *n_out = m;
     s->decoded_n = m;
     if (m > 0) {
-        if (last_t_ms) {
-            VMP_TRY(cudaMemcpyAsync(last_t_ms, reinterpret_cast<const float*>(s->s.raw + (m - 1)) + 3, sizeof(float),
-                                    cudaMemcpyDefault, s->st), "last time");
-        }
+        if (last_t_ms) std::memcpy(last_t_ms, s->h_int + 1, sizeof(float));
+        if (!out && !intensity) return VMP_OK;
         if (out)
             VMP_TRY(cudaMemcpyAsync(out, s->s.raw, sizeof(vmp_point) * (size_t)m, cudaMemcpyDefault, s->st), "cloud");
         if (intensity)
