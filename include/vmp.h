@@ -450,6 +450,12 @@ vmp_status vmp_set_graphs(vmp_stream_t s, int on);
 /* Test hook: batches that the LRU eviction had to split (an evicted voxel
  * touched again later in the same batch). */
 long long vmp_eviction_splits(vmp_stream_t s);
+/* Test hook: the bounded wait of the merge resolution's grid barrier.  Two
+ * CTAs meet at one barrier; with skip set the second never arrives, the
+ * first gives up after spin_limit polls (a 64 ns sleep each), records the failure
+ * and returns -- no fault, the context stays usable.  timed_out = 1 when the
+ * wait ran out; ms = device time of the launch. */
+vmp_status vmp_test_barrier_timeout(int skip, long long spin_limit, int* timed_out, double* ms);
 /* Device memory a stream holds (all of it is allocated by vmp_create). */
 long long vmp_device_bytes(vmp_stream_t s);
 /* How vmp_process waits for its result: 0 (default) polls, lowest latency;

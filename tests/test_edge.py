@@ -173,3 +173,21 @@ def test_body_cov_bit_exact(oracle_lib):
     oracle_lib.orc_calc_body_cov(_dp(pts), n, 0.04, 0.1, _dp(op), _dp(oc))
     assert np.array_equal(gp, op)
     assert np.array_equal(gc.view(np.uint64), oc.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_grid_barrier_wait_is_bounded():
+    """The merge resolution's grid barrier gives up instead of hanging: with
+    one CTA that never arrives the other's wait runs out (a status the host
+    reads, no fault), the context stays usable, and with both CTAs arriving
+    nothing times out."""
+    from voxelmapplus_fastlio2_gb300._lib import load
+    lib = load()
+    to, ms = C.c_int(-1), C.c_double(0.0)
+    assert lib.vmp_test_barrier_timeout(1, 100_000, C.byref(to), C.byref(ms)) == 0
+    assert to.value == 1
+    assert ms.value < 2000.0  # 1e5 polls with a 64 ns sleep each: milliseconds, not a hang
+    to.value = -1
+    assert lib.vmp_test_barrier_timeout(0, 100_000_000, C.byref(to), C.byref(ms)) == 0
+    assert to.value == 0
+    assert ms.value < 100.0

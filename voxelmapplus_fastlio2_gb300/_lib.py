@@ -78,6 +78,7 @@ def _declare(lib):
         "vmp_map_planes": ([vp, vp, C.c_int, P(C.c_int)], st),
         "vmp_test_division": ([vp, vp, C.c_int, vp, vp], st),
         "vmp_test_body_cov": ([vp, C.c_int, d, d, vp, vp], st),
+        "vmp_test_barrier_timeout": ([C.c_int, C.c_longlong, P(C.c_int), P(d)], st),
         "vmp_std_plane_voxels": ([vp, C.c_int, C.c_int, d, C.c_int, d, vp, C.c_int, P(C.c_int)], st),
         "vmp_livox_decode": ([vp, vp, C.c_int, C.c_int, d, d, vp, vp, P(C.c_int), P(C.c_float)], st),
         "vmp_process_decoded": ([vp, d, d, P(abi.vmp_imu), C.c_int, P(abi.vmp_result)], st),

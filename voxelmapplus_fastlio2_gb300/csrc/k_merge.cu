@@ -225,7 +225,7 @@ __global__ void k_merge_sequential(DMap m, const uint32_t* __restrict__ ev_list,
 // gives up after kBarrierSpinLimit polls, records the failure and lets every
 // later barrier pass at once, so the kernel always ends; the replay then
 // produces the result.
-__device__ void grid_barrier(MergeCtl* c) {
+__device__ void grid_barrier(MergeCtl* c, long long spin_limit = kBarrierSpinLimit) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int* vgen = &c->bar_gen;
@@ -242,7 +242,7 @@ __device__ void grid_barrier(MergeCtl* c) {
                 while (*vgen == g) {
                     if (*verr) break;
                     __nanosleep(64);
-                    if (++spins > kBarrierSpinLimit) {
+                    if (++spins > spin_limit) {
                         atomicExch(&c->wait_error, 1);
                         break;
                     }
@@ -672,3 +672,51 @@ int merge_rounds_read(void* scratch, cudaStream_t st) {
 }
 
 }  // namespace vmp
+
+// ------------------------------------------------------------ test hook
+// The barrier's failure path without a fault: with skip set, CTA 1 returns
+// without arriving, so CTA 0's wait runs out after spin_limit polls, records
+// wait_error and returns; without skip both arrive (cooperative launch, so
+// both CTAs are resident).  The kernel always ends.
+namespace vmp {
+namespace {
+__global__ void k_barrier_probe(MergeCtl* c, int skip, long long spin_limit) {
+    if (skip && blockIdx.x == 1) return;
+    grid_barrier(c, spin_limit);
+}
+}  // namespace
+}  // namespace vmp
+
+extern "C" vmp_status vmp_test_barrier_timeout(int skip, long long spin_limit, int* timed_out, double* ms) {
+    using namespace vmp;
+    if (!timed_out || spin_limit < 1) return VMP_ERR_INVALID_ARG;
+    MergeCtl* c = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaMalloc((void**)&c, sizeof(MergeCtl));
+    if (e == cudaSuccess) e = cudaMemset(c, 0, sizeof(MergeCtl));
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    if (e == cudaSuccess) e = cudaEventRecord(a, 0);
+    if (e == cudaSuccess) {
+        void* args[] = {(void*)&c, (void*)&skip, (void*)&spin_limit};
+        e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(2), dim3(32), args, 0, 0);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    MergeCtl h{};
+    if (e == cudaSuccess) e = cudaMemcpy(&h, c, sizeof(MergeCtl), cudaMemcpyDeviceToHost);
+    float t = 0.f;
+    if (e == cudaSuccess && ms) {
+        cudaEventElapsedTime(&t, a, b);
+        *ms = t;
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (c) cudaFree(c);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return VMP_ERR_CUDA;
+    }
+    *timed_out = h.wait_error;
+    return VMP_OK;
+}
