@@ -36,10 +36,10 @@ static int grid_for_map(int n) {
     return b < 1 ? 1 : b;
 }
 
-// RN(1 / k) for k = 1 .. kRecipTable - 1 (the running mean's divisors n + 1),
-// written once per device from the host's correctly rounded divisions.
+// (k, RN(1 / k)) for k = 1 .. kRecipTable - 1 (the running mean's divisors
+// n + 1), written once per device from the host's correctly rounded divisions.
 constexpr int kRecipTable = 4096;
-__device__ double g_recip[kRecipTable];
+__device__ double2 g_div[kRecipTable];
 
 cudaError_t map_recip_table_init() {
     static std::mutex mu;
@@ -50,9 +50,9 @@ cudaError_t map_recip_table_init() {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(mu);
     if (done[dev]) return cudaSuccess;
-    std::vector<double> t(kRecipTable, 0.0);
-    for (int k = 1; k < kRecipTable; ++k) t[k] = 1.0 / (double)k;
-    e = cudaMemcpyToSymbol(g_recip, t.data(), sizeof(double) * kRecipTable);
+    std::vector<double2> t(kRecipTable, make_double2(0.0, 0.0));
+    for (int k = 1; k < kRecipTable; ++k) t[k] = make_double2((double)k, 1.0 / (double)k);
+    e = cudaMemcpyToSymbol(g_div, t.data(), sizeof(double2) * kRecipTable);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) done[dev] = true;
     return e;
@@ -452,6 +452,10 @@ struct SegScratch {
 // voxels.  Collective steps (chunk allocation, the loop test) run on the
 // whole warp with per-group predicates.
 constexpr int kGroupLanes = 10;
+// Lane 3 + e of a chain holds the distinct ppt entry e = (i, j), i <= j:
+// i, j, i * 3 + j and j * 3 + i as 4-bit fields e of these constants.
+constexpr unsigned kPptI = 0x211000u, kPptJ = 0x221210u, kPptIdx = 0x854210u, kPptMir = 0x874630u;
+__device__ __forceinline__ int ppt_field(unsigned packed, int e) { return (int)((packed >> (4 * e)) & 15u); }
 constexpr int kGroups = 3;
 
 // Slab append for the groups with `app` (all lanes call it).
@@ -496,6 +500,9 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
     const int gi = g < kGroups ? g : 0;
     const int gbase = gi * kGroupLanes;
     const unsigned gmask = ((1u << kGroupLanes) - 1u) << gbase;
+    const int pe = q >= 3 && q < 9 ? q - 3 : 0;
+    const int p_i = ppt_field(kPptI, pe), p_j = ppt_field(kPptJ, pe);
+    const int p_idx = ppt_field(kPptIdx, pe), p_mir = ppt_field(kPptMir, pe);
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int nseg = *d_n_seg;
@@ -527,7 +534,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             newly = Cc.newly;
             nslab = Cc.nslab;
             if (q < 3) mean_l = H.mean[q];
-            if (q < 9) ppt_l = Cc.ppt[q];
+            if (q >= 3 && q < 9) ppt_l = Cc.ppt[p_idx];
             for (int k = q; k < kMaxChunks; k += kGroupLanes) chunks[k] = Cc.chunks[k];
         }
         __syncwarp();
@@ -539,7 +546,10 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             flags |= F_INIT;
             RefitSnap& sn = ss.snaps[b + nref];
             if (q < 3) sn.mean[q] = mean_l;
-            if (q < 9) sn.ppt[q] = ppt_l;
+            if (q >= 3 && q < 9) {  // ppt is symmetric: entry and mirror
+                sn.ppt[p_idx] = ppt_l;
+                sn.ppt[p_mir] = ppt_l;
+            }
             if (q == 0) {
                 sn.n = n;
                 sn.npts = npts;
@@ -551,13 +561,26 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             ++nref;
         };
         auto add_point = [&](const double* p) {
-            // (p - mean) / (n + 1): the divisor's reciprocal from the table
-            // (small counts), the division itself otherwise
-            if (q < 3) {
-                const double num = p[q] - mean_l, den = (double)n + 1.0;
-                mean_l = mean_l + (n + 1 < kRecipTable ? div_by_recip(num, den, __ldg(g_recip + n + 1)) : num / den);
+            // addToPlane: lanes 0-2 mean += (p - mean) / (n + 1), the division
+            // through the tabled RN(1 / (n + 1)) with Markstein's correction;
+            // lanes 3-8 the six distinct entries of ppt += p p^T (p_i - 0 is
+            // p_i exactly).  One FP64 instruction sequence serves both roles.
+            const int np1 = n + 1;
+            if (q < 9 && np1 < kRecipTable) {
+                const bool ml = q < 3;
+                const double2 dr = __ldg(g_div + np1);  // (n + 1, RN(1 / (n + 1)))
+                const int pi = ml ? q : p_i, pj = p_j;
+                const double a = p[pi] - (ml ? mean_l : 0.0);
+                const double prod = a * (ml ? dr.y : p[pj]);
+                const double r = __fma_rn(-prod, dr.x, a);
+                const double q2 = __fma_rn(r, dr.y, prod);
+                const double inc = ml ? (a == 0.0 ? prod : q2) : prod;
+                const double v = (ml ? mean_l : ppt_l) + inc;
+                if (ml) mean_l = v; else ppt_l = v;
+            } else if (q < 9) {
+                if (q < 3) mean_l = mean_l + (p[q] - mean_l) / ((double)n + 1.0);
+                else ppt_l = ppt_l + p[p_i] * p[p_j];
             }
-            if (q < 9) ppt_l = ppt_l + p[q / 3] * p[q % 3];
             n += 1;
         };
         if (build) {
@@ -664,7 +687,10 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
                 Cc.stamp = base + sv[e - 1];
             }
             if (q < 3) H.mean[q] = mean_l;
-            if (q < 9) Cc.ppt[q] = ppt_l;
+            if (q >= 3 && q < 9) {
+                Cc.ppt[p_idx] = ppt_l;
+                Cc.ppt[p_mir] = ppt_l;
+            }
             for (int t = q; t < kMaxChunks; t += kGroupLanes) Cc.chunks[t] = chunks[t];
         }
         __syncwarp();
