@@ -376,9 +376,10 @@ __device__ inline void plane_cov_term(const double* p, const double* cov, const 
 // ---------------------------------------------------------------- voxel state machine
 // VoxelGrid::pushPoint / addPoint / updatePlane (voxel_map.cpp:29-136) for
 // every touched voxel of a batch, in three kernels:
-//   k_seg_chain  one warp per voxel: the points in order -- addToPlane with
-//                the three coordinates of the mean and the nine of ppt on
-//                separate lanes, slab appends, the integer state machine --
+//   k_seg_chain  three voxels per warp, ten lanes each: the points in order
+//                -- addToPlane with the three coordinates of the mean and the
+//                six distinct entries of ppt on separate lanes, slab
+//                appends, the integer state machine --
 //                recording a snapshot (n, mean, ppt, slab length) at every
 //                updatePlane call that reaches the eigen decomposition;
 //   k_refit_eig  one thread per snapshot: the 3x3 eigen decomposition and the
