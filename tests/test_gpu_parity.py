@@ -335,20 +335,26 @@ def test_process_sequence_room(lio_mod, oracle_lib):
         assert np.max(np.abs(Pg - Po)) <= 1e-8 * np.max(np.abs(Po)), k
 
 
-def test_graph_and_direct_launches_agree(lio_mod):
+@pytest.mark.parametrize("evicting", [False, True])
+def test_graph_and_direct_launches_agree(lio_mod, evicting):
     """The steady-state scan as captured graphs and as direct launches: the
     same kernels with the same grids, so the same bits -- every result, and
-    the map at the end (two urban streams of different scan sizes, so that
-    several size classes are captured)."""
+    the map at the end.  Urban scans (several size classes captured) with
+    room to grow; corridor scans at a 2500-voxel capacity, where every scan's
+    map update may evict and only the scan front runs as a graph."""
     from voxelmapplus_fastlio2_gb300 import abi as A
     out = []
     for graphs in (1, 0):
-        seq = synth.Sequence(synth.KIND_URBAN, points_per_scan=30000)
-        cfg = A.default_config(scan_resolution=0.1, map_capacity=300000, max_scan_points=40000, ieskf_max_iter=4)
+        if evicting:
+            seq = synth.Sequence(synth.KIND_CORRIDOR, points_per_scan=8000)
+            cfg = A.default_config(scan_resolution=0.2, max_scan_points=16384, map_capacity=2500)
+        else:
+            seq = synth.Sequence(synth.KIND_URBAN, points_per_scan=30000)
+            cfg = A.default_config(scan_resolution=0.1, map_capacity=300000, max_scan_points=40000, ieskf_max_iter=4)
         g = lio_mod.LIOBuilder(cfg)
         g.lib.vmp_set_graphs(g.h, graphs)
         res = []
-        for k in range(12):
+        for k in range(30 if evicting else 12):
             r = g.process(seq.next())
             res.append((r.lio_status, r.iters, r.effect_num, r.n_down, r.map_size, bytes(r.x), bytes(r.P)))
         v, n = g.map.export()

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <new>
 #include <string>
 #include <vector>
@@ -72,9 +73,6 @@ __global__ void k_read_hm(const DFilter* f, double* H, double* b, int* eff) {
     for (int e = threadIdx.x; e < 144; e += blockDim.x) H[e] = f->Hm[e];
     if (threadIdx.x < 12) b[threadIdx.x] = f->bm[threadIdx.x];
     if (threadIdx.x == 0) *eff = f->effect_num;
-}
-__global__ void k_valid_bytes(const uint8_t* v, int n, uint8_t* out) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v[i];
 }
 
 // Export of live records (device -> vmp_voxel).
@@ -343,8 +341,11 @@ struct vmp_stream_s {
     // captured graphs of the steady-state scan, per size class: g1 = time
     // sort .. voxel state machine, g2 = LRU queue .. result copy (the merge
     // resolution runs between them)
-    struct ScanGraphs { int nb; cudaGraphExec_t g1, g2; long long k1, k2; };
-    std::vector<ScanGraphs> graphs;
+    // g1 / g2: the steady scan around the merge resolution; g0: the scan
+    // front alone (time sort to map batch), for scans whose map update may
+    // evict and therefore runs its map part with host decisions
+    struct ScanGraphs { int nb; cudaGraphExec_t g1, g2, g0; long long k1, k2, k0; };
+    std::deque<ScanGraphs> graphs;
     bool use_graphs = true;
     // vmp_map_planes scratch (allocated by its first call)
     SortScratch vis_ss{};
@@ -518,6 +519,7 @@ vmp_status vmp_destroy(vmp_stream_t s) {
     for (auto& gp : s->graphs) {
         if (gp.g1) cudaGraphExecDestroy(gp.g1);
         if (gp.g2) cudaGraphExecDestroy(gp.g2);
+        if (gp.g0) cudaGraphExecDestroy(gp.g0);
     }
     if (s->h_hdr) cudaFreeHost(s->h_hdr);
     if (s->done_ev) cudaEventDestroy(s->done_ev);
@@ -957,11 +959,46 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     s->pend(VMP_PROF_MAP_BATCH, 1);
 }
 
+// The graphs of size class nb (an empty entry on first use).
+static vmp_stream_s::ScanGraphs* graphs_for(vmp_stream_t s, int nb) {
+    for (auto& g : s->graphs)
+        if (g.nb == nb) return &g;
+    s->graphs.push_back(vmp_stream_s::ScanGraphs{nb, nullptr, nullptr, nullptr, 0, 0, 0});
+    return &s->graphs.back();
+}
+
+// The scan front (time sort to map batch) of size class nb as one graph
+// launch; captured on first use.  The same kernels and grids as the direct
+// launches.
+static vmp_status launch_front_graph(vmp_stream_t s, int nb) {
+    vmp_stream_s::ScanGraphs* gp = graphs_for(s, nb);
+    if (!gp->g0) {
+        long long launches = 0;
+        set_capture_launch_counter(&launches);
+        cudaError_t e = cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_scan_front(s, nb, false);
+            cudaGraph_t g = nullptr;
+            e = cudaStreamEndCapture(s->st, &g);
+            if (e == cudaSuccess) {
+                e = cudaGraphInstantiate(&gp->g0, g, 0);
+                cudaGraphDestroy(g);
+                gp->k0 = launches;
+            }
+        }
+        set_capture_launch_counter(nullptr);
+        if (e != cudaSuccess) return cuda_fail(s, e, "scan front graph capture");
+    }
+    VMP_TRY(cudaGraphLaunch(gp->g0, s->st), "scan front graph");
+    g_launch_count.fetch_add(gp->k0, std::memory_order_relaxed);
+    return VMP_OK;
+}
+
 // Captures the two graphs of a steady-state scan of size class nb.
 static vmp_status capture_scan_graphs(vmp_stream_t s, int nb, vmp_stream_s::ScanGraphs& gp) {
     cudaStream_t st = s->st;
     MapScratch& ms = s->ms;
-    gp = {nb, nullptr, nullptr, 0, 0};
+    gp.nb = nb;
     for (int part = 0; part < 2; ++part) {
         long long launches = 0;
         set_capture_launch_counter(&launches);
@@ -1000,15 +1037,10 @@ static vmp_status capture_scan_graphs(vmp_stream_t s, int nb, vmp_stream_s::Scan
 static vmp_status process_graph(vmp_stream_t s, int n, int nb, vmp_result* out) {
     cudaStream_t st = s->st;
     map_maintenance(s);  // host-decided rehash / queue compaction, before the graph
-    vmp_stream_s::ScanGraphs* gp = nullptr;
-    for (auto& g : s->graphs)
-        if (g.nb == nb) gp = &g;
-    if (!gp) {
-        vmp_stream_s::ScanGraphs g{};
-        vmp_status v = capture_scan_graphs(s, nb, g);
+    vmp_stream_s::ScanGraphs* gp = graphs_for(s, nb);
+    if (!gp->g1) {
+        vmp_status v = capture_scan_graphs(s, nb, *gp);
         if (v != VMP_OK) return v;
-        s->graphs.push_back(g);
-        gp = &s->graphs.back();
     }
     VMP_TRY(cudaGraphLaunch(gp->g1, st), "scan graph");
     g_launch_count.fetch_add(gp->k1, std::memory_order_relaxed);
@@ -1098,7 +1130,12 @@ static vmp_status process_impl(vmp_stream_t s, const vmp_point* pts, int n, doub
         s->lio_status = VMP_LIO_MAPPING;
         return finish_result(s, n, out);
     }
-    enqueue_scan_front(s, nb, false);
+    if (s->use_graphs && !s->prof_on) {  // the map update below may evict: only the front as a graph
+        v = launch_front_graph(s, nb);
+        if (v != VMP_OK) return v;
+    } else {
+        enqueue_scan_front(s, nb, false);
+    }
     VMP_TRY(cudaGetLastError(), "scan launch");
     s->cur_batch_kind = 1;
     v = map_apply(s, s->s.bpts, s->s.bcov, s->s.d_n_batch, -1, nb, false);
