@@ -239,8 +239,19 @@ inline void calcBodyCov(V3& pb, double range_inc, double degree_inc, M3& cov) {
     N(0, 0) = b1[0]; N(0, 1) = b2[0];
     N(1, 0) = b1[1]; N(1, 1) = b2[1];
     N(2, 0) = b1[2]; N(2, 1) = b2[2];
-    M32 A = (range * dh) * N;
-    cov = (d * range_var) * T(d) + (A * dvar) * T(A);
+    // A = (range [d]x) N and A dvar, without the products with the zero
+    // diagonal of [d]x and the zero off-diagonal of dvar: the dense sums less
+    // their +-0 terms (the same values up to the sign of an exact zero; the
+    // device evaluates it alike)
+    M32 A, AD;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 2; ++j) {
+            const int k0 = i == 0 ? 1 : 0, k1 = i == 2 ? 1 : 2;
+            A(i, j) = (range * dh(i, k0)) * N(k0, j) + (range * dh(i, k1)) * N(k1, j);
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 2; ++j) AD(i, j) = A(i, j) * dvar(j, j);
+    cov = (d * range_var) * T(d) + AD * T(A);
 }
 
 // ---------------------------------------------------------------- VoxelMap
@@ -666,9 +677,9 @@ struct LIOBuilder {  // lio_builder.h:56-83
         for (int i = 0; i < 3; ++i) t[i] = (float)p[i];
     }
 
+    // lio_builder.cpp:200-203, 241-243; [p]x P_rr [p]x^T through hatSandwich
     M3 worldCov(const M3& r_wl, const M3& cov_l, const V3& p_l) const {
-        M3 cm = hat(p_l);
-        return r_wl * cov_l * T(r_wl) + cm * kf.P_.block<3, 3>(3, 3) * T(cm) + kf.P_.block<3, 3>(0, 0);
+        return r_wl * cov_l * T(r_wl) + hatSandwich(p_l, kf.P_.block<3, 3>(3, 3)) + kf.P_.block<3, 3>(0, 0);
     }
 
     std::vector<float> next_intensity;  // intensities of the next package's points (else 0)

@@ -277,6 +277,23 @@ __device__ inline void hat3(const double* w, double* m) {
     m[3] = w[2]; m[4] = 0; m[5] = -w[0];
     m[6] = -w[1]; m[7] = w[0]; m[8] = 0;
 }
+// [p]x M [p]x^T as ([p]x M) [p]x^T, products summed k = 0..2 left to right,
+// without the products with [p]x's zero diagonal: the dense sums less their
+// +-0 terms (the same values up to the sign of an exact zero).
+__device__ inline void hat_sandwich(const double* p, const double* M, double* out) {
+    double h[9], T[9];
+    hat3(p, h);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const int k0 = i == 0 ? 1 : 0, k1 = i == 2 ? 1 : 2;  // the two k != i
+            T[i * 3 + j] = h[i * 3 + k0] * M[k0 * 3 + j] + h[i * 3 + k1] * M[k1 * 3 + j];
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const int k0 = j == 0 ? 1 : 0, k1 = j == 2 ? 1 : 2;  // the two k != j
+            out[i * 3 + j] = T[i * 3 + k0] * h[j * 3 + k0] + T[i * 3 + k1] * h[j * 3 + k1];
+        }
+}
 __device__ inline void eye3(double* m) {
     for (int i = 0; i < 9; ++i) m[i] = (i % 4 == 0) ? 1.0 : 0.0;
 }

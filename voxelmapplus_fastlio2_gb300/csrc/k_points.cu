@@ -212,11 +212,17 @@ __device__ void calc_body_cov(double* pb, double range_inc, double s, double* co
     double b2[3] = {b1[1] * d[2] - b1[2] * d[1], b1[2] * d[0] - b1[0] * d[2], b1[0] * d[1] - b1[1] * d[0]};
     normalize3(b2);
     double N[6] = {b1[0], b2[0], b1[1], b2[1], b1[2], b2[2]};
-    double rdh[9];
-    for (int i = 0; i < 9; ++i) rdh[i] = range * dh[i];
+    // A = (range [d]x) N and A dvar without the products with the zero
+    // diagonal of [d]x and the zero off-diagonal of dvar: the dense sums less
+    // their +-0 terms (the oracle evaluates it alike)
     double A[6], AD[6], AT[6], C1[9], C2[9], dr[3];
-    mm<3, 3, 2>(rdh, N, A);
-    mm<3, 2, 2>(A, dvar, AD);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 2; ++j) {
+            const int k0 = i == 0 ? 1 : 0, k1 = i == 2 ? 1 : 2;
+            A[i * 2 + j] = (range * dh[i * 3 + k0]) * N[k0 * 2 + j] + (range * dh[i * 3 + k1]) * N[k1 * 2 + j];
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 2; ++j) AD[i * 2 + j] = A[i * 2 + j] * dvar[j * 3];
     tr<3, 2>(A, AT);
     mm<3, 2, 3>(AD, AT, C2);
     for (int i = 0; i < 3; ++i) dr[i] = d[i] * range_var;
@@ -288,14 +294,11 @@ __global__ void k_map_batch(const DFilter* __restrict__ f, const float4* __restr
             for (int a = 0; a < 3; ++a) pb[a] = pl[i * 3 + a];
             for (int a = 0; a < 9; ++a) cl[a] = covl[i * 9 + a];
         }
-        double T1[9], T2[9], rT[9], cm[9], cmT[9], T3[9], T4[9];
+        double T1[9], T2[9], rT[9], T4[9];
         mm<3, 3, 3>(rwl, cl, T1);
         tr<3, 3>(rwl, rT);
         mm<3, 3, 3>(T1, rT, T2);
-        hat3(pb, cm);
-        mm<3, 3, 3>(cm, prr, T3);
-        tr<3, 3>(cm, cmT);
-        mm<3, 3, 3>(T3, cmT, T4);
+        hat_sandwich(pb, prr, T4);
         for (int k = 0; k < 9; ++k) bcov[i * 9 + k] = (T2[k] + T4[k]) + ppp[k];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *d_n_batch = n;
