@@ -212,7 +212,7 @@ TRAFFIC_PER_UNIT = {
 FP64_PER_UNIT = {
     "residual": 5.81,   # per downsampled point x IEKF iteration
     "undistort": 7.11,  # per raw point
-    "body_cov": 6.97,   # per downsampled point
+    "body_cov": 6.22,   # per downsampled point
     "map_batch": 5.57,  # per batch point
     "map_state": 18.3,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov
 }
