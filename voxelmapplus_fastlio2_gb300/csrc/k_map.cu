@@ -206,55 +206,119 @@ __global__ void k_fill_u32(uint32_t* p, const int* d_n, uint32_t v) {
 }
 
 // ---------------------------------------------------------------- eviction
-// Sequential walk over the creations of this batch that overflow the
-// capacity (exact LRU semantics): the victim of a creation at point c is the
+// Walk over the creations of this batch that overflow the capacity (exact
+// LRU semantics): the victim of a creation at point c is the
 // least recently used voxel that no point before c touched in this batch.
 // A victim that a later point of the batch touches would be re-created by the
 // reference; the walk then reports the first such point (split_at) and the
 // host applies the batch in two parts.
-__global__ void k_evict_walk(DMap m, const uint32_t* __restrict__ new_pos, uint32_t* victims, const int* d_n) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// The walk is a scan, 1024 queue entries per step in one CTA: an entry is
+// stale (its voxel dead or touched again since), live and untouched in this
+// batch, or live and touched in this batch.  Before the first split every
+// victim is a live untouched entry, so the creation an entry meets is j0 plus
+// the count of live untouched entries before it (a block prefix sum); a
+// touched entry is skipped if its first touch precedes that creation and is
+// the split point otherwise.  The assignments equal the one-entry-at-a-time
+// walk's.
+constexpr int kWalkThreads = 1024;
+__global__ void __launch_bounds__(kWalkThreads) k_evict_walk(DMap m, const uint32_t* __restrict__ new_pos,
+                                                              uint32_t* victims, const int* d_n) {
+    __shared__ int s_wsum[kWalkThreads / 32];
+    __shared__ int s_split_t, s_last_t;
     Counters* c = m.cnt;
-    const unsigned long long batch_end = c->batch_base + (unsigned long long)*d_n;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const unsigned long long base = c->batch_base;
+    const unsigned long long batch_end = base + (unsigned long long)*d_n;
     const int n_new = c->n_new;
     const long long size_before = c->size - n_new;
-    const unsigned long long base = c->batch_base;
-    c->n_evict = 0;
-    c->split_at = -1;
+    const unsigned long long q_head = c->q_head, q_tail = c->q_tail;
+    __syncthreads();  // every thread has read the counters before they change
+    if (t == 0) {
+        c->n_evict = 0;
+        c->split_at = -1;
+    }
     long long j0 = m.capacity - size_before;  // creations j >= j0 evict
     if (j0 < 0) j0 = 0;
-    if (j0 >= n_new) return;
-    unsigned long long q = c->q_head;
-    int ne = 0;
-    long long split = -1;
-    for (long long j = j0; j < n_new; ++j) {
-        const unsigned long long cg = base + new_pos[j];
-        uint32_t victim = kNoRec;
-        while (q < c->q_tail) {
-            uint32_t r = m.q_rec[q % m.q_cap];
-            uint64_t st = m.q_stamp[q % m.q_cap];
-            ++q;
-            if (!(m.hot[r].flags & F_ALIVE) || m.cold[r].stamp != st) continue;
-            uint64_t tf = m.cold[r].touch_first_g;
-            // a stamp past this batch's points is left by the rolled-back
-            // first pass of a batch that was split: not a touch of this batch
-            bool touched_here = (tf != kNever) && tf >= base && tf < batch_end;
-            if (touched_here && tf < cg) continue;  // moved to the front before this creation
-            victim = r;
-            if (touched_here) split = (long long)(tf - base);  // re-created later by the reference
+    if (j0 >= n_new) return;  // uniform
+    const int need = (int)(n_new - j0);
+    unsigned long long q0 = q_head;
+    int assigned = 0;  // victims assigned before q0
+    int ne = -1;       // victims of the batch once known
+    unsigned long long q_end = q_tail;
+    for (;;) {
+        const unsigned long long qi = q0 + (unsigned long long)t;
+        int kind = 0;  // 0 stale or past the tail, 1 live untouched, 2 live touched in this batch
+        uint32_t r = 0;
+        uint64_t tf = kNever;
+        if (qi < q_tail) {
+            r = m.q_rec[qi % m.q_cap];
+            const uint64_t st = m.q_stamp[qi % m.q_cap];
+            if ((m.hot[r].flags & F_ALIVE) && m.cold[r].stamp == st) {
+                tf = m.cold[r].touch_first_g;
+                // a stamp past this batch's points is left by the rolled-back
+                // first pass of a batch that was split: not a touch of this batch
+                kind = (tf != kNever && tf >= base && tf < batch_end) ? 2 : 1;
+            }
+        }
+        // exclusive prefix count of live untouched entries over the block
+        const int f = kind == 1 ? 1 : 0;
+        int inc = f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) s_wsum[w] = inc;
+        if (t == 0) {
+            s_split_t = kWalkThreads;
+            s_last_t = -1;
+        }
+        __syncthreads();
+        if (w == 0) {
+            int x = s_wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += v;
+            }
+            s_wsum[lane] = x;  // inclusive over warps
+        }
+        __syncthreads();
+        const int total = s_wsum[kWalkThreads / 32 - 1];
+        const int a = assigned + (w > 0 ? s_wsum[w - 1] : 0) + inc - f;  // creation offset this entry meets
+        if (kind == 2 && a < need && tf >= base + new_pos[j0 + a]) atomicMin(&s_split_t, t);
+        __syncthreads();
+        const int ts = s_split_t;
+        if (kind == 1 && t < ts && a < need) {
+            victims[a] = r;
+            if (a == need - 1) s_last_t = t;
+        }
+        __syncthreads();
+        if (ts < kWalkThreads) {  // re-created later by the reference: split the batch here
+            if (t == ts) c->split_at = (int)(tf - base);
+            return;
+        }
+        if (s_last_t >= 0) {  // every creation has its victim
+            ne = need;
+            q_end = q0 + (unsigned long long)s_last_t + 1ull;
             break;
         }
-        if (split >= 0) break;
-        if (victim == kNoRec) { set_error(c, E_CAPACITY); break; }
-        victims[ne++] = victim;
+        assigned += total;
+        q0 += kWalkThreads;
+        if (q0 >= q_tail) {  // the queue ran out before every creation had a victim
+            if (t == 0) set_error(c, E_CAPACITY);
+            ne = assigned;
+            q_end = q_tail;
+            break;
+        }
+        __syncthreads();  // s_wsum and the flags are reused by the next step
     }
-    if (split >= 0) {
-        c->split_at = (int)split;
-        return;
+    __syncthreads();  // the victims written above are visible to the block
+    for (int v = t; v < ne; v += kWalkThreads) m.cold[victims[v]].evict_g = base + new_pos[j0 + v];
+    if (t == 0) {
+        c->q_head = q_end;
+        c->n_evict = ne;
     }
-    for (int v = 0; v < ne; ++v) m.cold[victims[v]].evict_g = base + new_pos[j0 + v];
-    c->q_head = q;
-    c->n_evict = ne;
 }
 
 // Undoes the creations of an aborted batch (the batch is split and re-applied).
@@ -976,7 +1040,7 @@ void launch_map_phase_a(DMap& m, MapScratch& ms, const double* bpts, int n_max, 
 }
 // Eviction walk (only when the batch can overflow the capacity).
 void launch_map_walk(DMap& m, MapScratch& ms, cudaStream_t st) {
-    VMP_NOTE_LAUNCH(); k_evict_walk<<<1, 32, 0, st>>>(m, ms.new_pos, ms.victims, ms.d_n);
+    VMP_NOTE_LAUNCH(); k_evict_walk<<<1, kWalkThreads, 0, st>>>(m, ms.new_pos, ms.victims, ms.d_n);
 }
 void launch_map_rollback(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
     VMP_NOTE_LAUNCH(); k_rollback<<<grid_for_map(n_max), kMapThreads, 0, st>>>(m, ms.slot, ms.flag, ms.d_n);
