@@ -23,7 +23,9 @@ HBM budget, served by libvmp's server (vmp_submit / vmp_poll).
   plain_1stream  the same streams and packages with one package on the GPU
             at a time (one worker), and the one-stream urban block (200k
             rays, 4 M voxel capacity) with its per-phase CUDA-event profile,
-            which gives the kernel roofline;
+            which gives the kernel roofline: HBM bytes of the dominant phase
+            against the measured copy bandwidth, and (roofline.fp64) the
+            FP64-bound phases against the FP64 pipe's issue rate;
   cpu_baseline  the CPU oracle (restated reference, one thread as the
             reference's MP_PROC_NUM=1) on a bounded sample of the streams.
 `--impl reference` runs the CPU restatement on all streams of the served
