@@ -522,6 +522,16 @@ vmp_status vmp_submit(vmp_server_t sv, int stream_id, const vmp_scan* scan, cons
  * the buffers must stay valid until the package's result is polled. */
 vmp_status vmp_submit_device(vmp_server_t sv, int stream_id, const vmp_point* d_pts, int n, double t_start,
                              double t_end, const vmp_imu* d_imus, int n_imu, long long cookie);
+/* A raw Livox CustomMsg point array as the package (the node's lidarCB +
+ * syncPackage + process, lio_node.cpp:121-148, 171): copied like vmp_submit;
+ * the worker decodes it on the device (vmp_livox_decode: livox2pcl,
+ * utils.cpp:3-28), takes the scan's end time as t_start + (last kept point's
+ * time in ms) / 1000 (lio_node.cpp:146) and processes the decoded cloud
+ * (vmp_process_decoded).  A message that keeps no point gives
+ * VMP_ERR_INVALID_ARG in its result. */
+vmp_status vmp_submit_livox(vmp_server_t sv, int stream_id, const vmp_livox_point* pts, int n, int filter_num,
+                            double range_min, double range_max, double t_start, const vmp_imu* imus, int n_imu,
+                            long long cookie);
 /* Moves up to max finished results to out (completion order), waiting up to
  * timeout_ms for the first one; returns how many, or -1 on a bad argument. */
 int vmp_poll(vmp_server_t sv, vmp_server_result* out, int max, int timeout_ms);

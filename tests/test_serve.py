@@ -135,3 +135,57 @@ def test_autotuner_reports_state():
         assert t["merge_grid_divisor"] in (4, 8, 16, 32, 64) and t["windows"] == 0
     finally:
         srv.close()
+
+
+def _livox(rng, pkg):
+    pts = pkg.points_np()
+    a = np.zeros(pkg.n, dtype=abi.livox_dtype())
+    a["x"], a["y"], a["z"] = pts[:, 0], pts[:, 1], pts[:, 2]
+    a["offset_time"] = np.rint(pts[:, 3].astype(np.float64) * 1e6).astype(np.uint32)
+    a["reflectivity"] = rng.integers(0, 256, pkg.n)
+    a["tag"] = rng.choice(np.array([0x00, 0x10, 0x20], dtype=np.uint8), pkg.n, p=[0.6, 0.35, 0.05])
+    a["line"] = rng.choice(np.array([0, 1, 2, 3, 4], dtype=np.uint8), pkg.n, p=[0.24, 0.24, 0.24, 0.24, 0.04])
+    return a
+
+
+def test_served_livox_messages_match_direct_decode():
+    """Raw Livox messages submitted to the server (decoded by the worker, end
+    time from the last kept point) give the results of vmp_livox_decode +
+    vmp_process_decoded on a stream of one's own, bit for bit, with four
+    streams' messages in flight together."""
+    from voxelmapplus_fastlio2_gb300 import lio
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    rng = np.random.default_rng(11)
+    streams = []
+    for s in range(4):
+        pk = _packages(synth.KIND_ROOM, 0x5EED0000 + 300 + s, 6000, 12)
+        streams.append([(p, _livox(rng, p)) for p in pk])
+    cfg = _cfg(synth.KIND_ROOM)
+    direct = []
+    for msgs in streams:
+        g = lio.LIOBuilder(cfg)
+        res = []
+        for p, a in msgs:
+            n, last = g.livox_decode(a, 2, 0.1, 100.0, copy_out=False)
+            res.append(_key(g.process_decoded(p.t_start, p.t_start + float(last) / 1000.0, p.imus, p.n_imu)))
+        direct.append(res)
+        g.close()
+    srv = Server(hbm_budget_bytes=50e9, max_streams=4, workers=4)
+    try:
+        sids = [srv.open_stream(cfg) for _ in streams]
+        for k in range(12):
+            for sid, msgs in zip(sids, streams):
+                p, a = msgs[k]
+                srv.submit_livox(sid, a, p.t_start, p.imus, p.n_imu, filter_num=2, range_min=0.1, range_max=100.0,
+                                 cookie=k)
+        got = {}
+        while sum(len(v) for v in got.values()) < 12 * len(sids):
+            for r in srv.poll(timeout_ms=1000):
+                assert r.status == abi.VMP_OK
+                got.setdefault(r.stream_id, []).append((r.cookie, _key(r.result)))
+        for i, sid in enumerate(sids):
+            seq = sorted(got[sid])
+            assert [c for c, _ in seq] == list(range(12))
+            assert [k for _, k in seq] == direct[i]
+    finally:
+        srv.close()

@@ -67,6 +67,7 @@ def _declare(lib):
         "vmp_server_close_stream": ([vp, C.c_int], st),
         "vmp_submit": ([vp, C.c_int, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, C.c_longlong], st),
         "vmp_submit_device": ([vp, C.c_int, vp, C.c_int, d, d, vp, C.c_int, C.c_longlong], st),
+        "vmp_submit_livox": ([vp, C.c_int, vp, C.c_int, C.c_int, d, d, d, P(abi.vmp_imu), C.c_int, C.c_longlong], st),
         "vmp_poll": ([vp, P(abi.vmp_server_result), C.c_int, C.c_int], C.c_int),
         "vmp_server_stream": ([vp, C.c_int, P(vp)], st),
         "vmp_server_info": ([vp, P(C.c_longlong), P(C.c_int), P(C.c_int), P(C.c_int)], st),

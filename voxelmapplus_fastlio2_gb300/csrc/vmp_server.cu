@@ -34,6 +34,11 @@ struct Package {
     long long cookie = 0;
     std::vector<vmp_point> pts;
     std::vector<vmp_imu> imus;
+    // vmp_submit_livox: the raw message, decoded by the worker
+    std::vector<vmp_livox_point> livox;
+    bool is_livox = false;
+    int filter_num = 1;
+    double range_min = 0.0, range_max = 0.0;
     // vmp_submit_device: the caller's device buffers
     const vmp_point* d_pts = nullptr;
     const vmp_imu* d_imus = nullptr;
@@ -175,7 +180,18 @@ struct vmp_server_s {
             r.stream_id = id;
             r.submit_ms = p.submit_ms;
             r.start_ms = now_ms();
-            if (p.d_pts) {
+            if (p.is_livox) {
+                int m = 0;
+                float last_t = 0.f;
+                r.status = vmp_livox_decode(h, p.livox.data(), (int)p.livox.size(), p.filter_num, p.range_min,
+                                            p.range_max, nullptr, nullptr, &m, &last_t);
+                if (r.status == VMP_OK && m <= 0) r.status = VMP_ERR_INVALID_ARG;
+                if (r.status == VMP_OK) {
+                    const double t_end = p.t_start + (double)last_t / 1000.0;  // lio_node.cpp:146
+                    r.status = vmp_process_decoded(h, p.t_start, t_end, p.imus.data(), (int)p.imus.size(),
+                                                   &r.result);
+                }
+            } else if (p.d_pts) {
                 r.status = vmp_process_device(h, p.d_pts, p.n, p.t_start, p.t_end, p.d_imus, p.n_imu, &r.result);
             } else {
                 vmp_scan scan{p.pts.data(), (int)p.pts.size(), p.t_start, p.t_end};
@@ -361,6 +377,22 @@ vmp_status vmp_submit(vmp_server_t sv, int id, const vmp_scan* scan, const vmp_i
     p.imus.assign(imus, imus + n_imu);
     p.t_start = scan->t_start;
     p.t_end = scan->t_end;
+    return enqueue(sv, id, std::move(p));
+}
+
+vmp_status vmp_submit_livox(vmp_server_t sv, int id, const vmp_livox_point* pts, int n, int filter_num,
+                            double range_min, double range_max, double t_start, const vmp_imu* imus, int n_imu,
+                            long long cookie) {
+    if (!sv || n < 0 || (n > 0 && !pts) || filter_num < 1 || n_imu <= 0 || !imus) return VMP_ERR_INVALID_ARG;
+    Package p;
+    p.cookie = cookie;
+    p.is_livox = true;
+    p.livox.assign(pts, pts + n);
+    p.imus.assign(imus, imus + n_imu);
+    p.filter_num = filter_num;
+    p.range_min = range_min;
+    p.range_max = range_max;
+    p.t_start = t_start;
     return enqueue(sv, id, std::move(p));
 }
 

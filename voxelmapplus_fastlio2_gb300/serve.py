@@ -52,6 +52,16 @@ class Server:
         scan = pkg.scan()
         self._check(self.lib.vmp_submit(self.h, int(sid), C.byref(scan), pkg.imus, pkg.n_imu, int(cookie)), "submit")
 
+    def submit_livox(self, sid, livox, t_start, imus, n_imu, filter_num=1, range_min=0.5, range_max=20.0, cookie=0):
+        """A raw Livox message (numpy array of abi.livox_dtype()) as the
+        package: decoded on the device by the worker, the scan's end time
+        taken from its last kept point (vmp_submit_livox)."""
+        import numpy as np
+        livox = np.ascontiguousarray(livox, dtype=abi.livox_dtype())
+        self._check(self.lib.vmp_submit_livox(self.h, int(sid), C.c_void_p(livox.ctypes.data), len(livox),
+                                              int(filter_num), float(range_min), float(range_max), float(t_start),
+                                              imus, int(n_imu), int(cookie)), "submit_livox")
+
     def submit_device(self, sid, d_pts, n, t_start, t_end, d_imus, n_imu, cookie=0):
         """A package already in device memory (pointers stay valid until polled)."""
         self._check(self.lib.vmp_submit_device(self.h, int(sid), C.c_void_p(d_pts), int(n), float(t_start),
