@@ -566,8 +566,8 @@ def pose_errors(gpu, cpu):
 
 def dist_setup(args, backend=None):
     """One process per GPU (torchrun): rank, world size, a barrier and a max
-    over ranks.  NCCL on GPU machines; gloo (CPU tensors) where no GPU is
-    visible, which is how the multi-rank path is tested here."""
+    over ranks.  NCCL where GPUs are visible; gloo (CPU tensors) where none
+    is, which is how the multi-rank path is tested on CPU."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws <= 1:
