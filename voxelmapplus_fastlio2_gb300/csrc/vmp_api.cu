@@ -761,29 +761,30 @@ static vmp_status map_apply(vmp_stream_t s, const double* bpts, const double* bc
         s->h_size += n_upper;  // upper bound until the next counter read
         return VMP_OK;
     }
-    // eviction possible: know n exactly, then walk
-    int n = n_host;
-    if (d_n_src) {
-        VMP_TRY(cudaMemcpyAsync(s->h_int, d_n_src, sizeof(int), cudaMemcpyDeviceToHost, s->st), "read n");
-        s->io_d2h += (long long)sizeof(int);
-        VMP_TRY(cudaStreamSynchronize(s->st), "sync");
-        n = s->h_int[0];
-        VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(ms.d_n, n);
-    }
-    if (n <= 0) return VMP_OK;
-    launch_map_phase_a(m, ms, bpts, n, s->st);
-    launch_map_segments(m, ms, n, s->st);
+    // eviction possible: the walk runs on the device; its counters (a split?)
+    // and the batch size come back in one read, the only host round trip of
+    // a batch that does not split (the kernels take n from the device and
+    // n_upper bounds their grids, as above)
+    launch_map_phase_a(m, ms, bpts, n_upper, s->st);
+    launch_map_segments(m, ms, n_upper, s->st);
     launch_map_walk(m, ms, s->st);
+    VMP_TRY(cudaMemcpyAsync(s->h_int, ms.d_n, sizeof(int), cudaMemcpyDeviceToHost, s->st), "read n");
+    s->io_d2h += (long long)sizeof(int);
     vmp_status st = read_counters(s);
     if (st != VMP_OK) return st;
+    const int n = s->h_int[0];
+    if (n <= 0) return VMP_OK;
     const int split = s->h_cnt->split_at;
     if (split < 0) {
-        launch_map_phase_b(m, ms, bpts, bcov, n, build, s->st);
+        launch_map_phase_b(m, ms, bpts, bcov, n_upper, build, s->st);
         VMP_TRY(cudaGetLastError(), "map update launch");
-        return read_counters(s);
+        // at most the capacity once the walk evicted for it; every caller
+        // reads the counters with its result
+        s->h_size = m.capacity;
+        return VMP_OK;
     }
     ++s->eviction_splits;
-    launch_map_rollback(m, ms, n, s->st);
+    launch_map_rollback(m, ms, n_upper, s->st);
     st = read_counters(s);
     if (st != VMP_OK) return st;
     if (split <= 0 || split >= n) return fail(s, VMP_ERR_STATE, "eviction split outside the batch");
