@@ -197,6 +197,11 @@ vmp_status vmp_map_update(vmp_stream_t s, const double* pts, const double* cov, 
 vmp_status vmp_map_info_get(vmp_stream_t s, vmp_map_info* info);
 /* Copies up to max voxels, most recently used first (LRU order). */
 vmp_status vmp_map_export(vmp_stream_t s, vmp_voxel* out, long long max, long long* n_out);
+/* The keys of VoxelMap::featmap in the order of VoxelMap::cache
+ * (voxel_map.h:124-125; front = most recently used): keys[i*3+0..2] for up
+ * to max voxels, *n_out = live voxels.  24 bytes per voxel instead of a full
+ * vmp_voxel, for per-scan key-set checks of large maps. */
+vmp_status vmp_map_keys(vmp_stream_t s, int64_t* keys, long long max, long long* n_out);
 /* Replaces the map by the given voxels (LRU order as listed, first = most
  * recent) and their buffered points (pts/cov of all voxels concatenated in
  * voxel order, vox[i].n_temp each). */
@@ -331,15 +336,20 @@ vmp_status vmp_test_body_cov(const double* pts, int n, double range_inc, double 
 /* The same leaf-centroid downsample for callers that cannot allocate device
  * memory (no counterpart in the reference): a real-time sensor thread that
  * must not call cudaMalloc/cudaFree, or a host framework whose own allocator
- * owns the GPU's memory.  d_in / d_out are device buffers the caller owns
- * (d_out holds up to n points); *n_out (host) receives the output count.  The
- * working memory is a fixed 2 MiB __device__ array inside libvmp, held by
- * every GPU that loads the library until exit; at most 65536 input points
- * (VMP_ERR_CAPACITY above that).  The call allocates nothing.  Its first call
- * on a device resolves the array's device address, so make that first call
- * before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race and must be serialised by the caller.  cuda_stream may be
- * NULL (default stream); the call returns after that stream finished. */
+ * owns the GPU's memory.  d_in / d_out are device (or managed) buffers the
+ * caller owns, each 16-byte aligned, and they must not overlap (d_out holds
+ * up to n points; an in-place call is rejected); *n_out (host) receives the
+ * output count.  Host pointers, misaligned or overlapping buffers give
+ * VMP_ERR_INVALID_ARG before anything is launched.  The working memory is a
+ * fixed 2 MiB __device__ array inside libvmp, held by every GPU that loads
+ * the library until exit; at most 65536 input points (VMP_ERR_CAPACITY above
+ * that).  The call allocates nothing.  Its first call on a device resolves
+ * the array's device address, so make that first call before any stream
+ * capture; the address is kept for the process, so cudaDeviceReset while
+ * libvmp is loaded is not supported.  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  cuda_stream
+ * may be NULL (default stream); the call returns after that stream
+ * finished. */
 vmp_status vmp_downsample_noalloc(const vmp_point* d_in, int n, double leaf, vmp_point* d_out, int* n_out,
                                   void* cuda_stream);
 

@@ -46,6 +46,9 @@ def load():
     lib.orc_map_info.argtypes = [vp, P(abi.vmp_map_info)]
     lib.orc_map_export.argtypes = [vp, P(abi.vmp_voxel), C.c_longlong]
     lib.orc_map_export.restype = C.c_longlong
+    lib.orc_map_keys.argtypes = [vp, P(C.c_int64), C.c_longlong]
+    lib.orc_map_keys.restype = C.c_longlong
+    lib.orc_residual_valid.argtypes = [vp, P(C.c_ubyte), C.c_int]
     lib.orc_map_export_points.argtypes = [vp, P(d), P(d), C.c_longlong]
     lib.orc_map_export_points.restype = C.c_longlong
     lib.orc_map_import.argtypes = [vp, P(abi.vmp_voxel), C.c_longlong, P(d), P(d), C.c_longlong]
@@ -115,6 +118,21 @@ class Oracle:
         res = abi.vmp_result()
         self.lib.orc_process(self.h, C.byref(scan), imus, n_imu, C.byref(res))
         return res
+
+    def map_keys(self):
+        """Keys of all voxels in cache order (front = most recently used)."""
+        import numpy as np
+        n = self.lib.orc_map_keys(self.h, None, 0)
+        out = np.zeros((max(1, n), 3), dtype=np.int64)
+        self.lib.orc_map_keys(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)), n)
+        return out[:n]
+
+    def residual_valid(self, n):
+        """is_valid of the first n residual_info entries (the last match set)."""
+        import numpy as np
+        v = np.zeros(max(1, n), dtype=np.uint8)
+        self.lib.orc_residual_valid(self.h, v.ctypes.data_as(C.POINTER(C.c_ubyte)), n)
+        return v[:n]
 
     def output_cloud(self, frame):
         import numpy as np

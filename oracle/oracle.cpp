@@ -572,6 +572,7 @@ struct LIOBuilder {  // lio_builder.h:56-83
     int threads = 1;
     int last_effect = 0;
     int no_effect_flag = 0;
+    long long last_evicted_total = 0;
 
     explicit LIOBuilder(const vmp_config& c) { loadConfig(c); }
 
@@ -856,10 +857,11 @@ int orc_process(void* h, const vmp_scan* scan, const vmp_imu* imus, int n_imu, v
         out->n_down = (int)b->lidar_cloud.size();
         out->flags = b->no_effect_flag;
         out->map_size = (long long)b->map->featmap.size();
-        out->evicted = b->map->evicted;
+        out->evicted = b->map->evicted - b->last_evicted_total;  // this scan's evictions
         stateToC(b->kf.x_, &out->x);
         for (int i = 0; i < 529; ++i) out->P[i] = b->kf.P_[i];
     }
+    b->last_evicted_total = b->map->evicted;
     return 0;
 }
 
@@ -912,6 +914,24 @@ long long orc_map_export(void* h, vmp_voxel* out, long long max) {
         ++n;
     }
     return n;
+}
+// Keys of featmap in cache order (voxel_map.h:124-125), front first.
+long long orc_map_keys(void* h, int64_t* keys, long long max) {
+    LIOBuilder* b = (LIOBuilder*)h;
+    long long n = 0;
+    for (auto& k : b->map->cache) {
+        if (n >= max) break;
+        keys[3 * n] = k.x; keys[3 * n + 1] = k.y; keys[3 * n + 2] = k.z;
+        ++n;
+    }
+    return (long long)b->map->cache.size();
+}
+// ResidualData::is_valid of the first n entries of residual_info
+// (lio_builder.cpp:25, 260-274): the match set of the last iteration,
+// stale entries included.
+void orc_residual_valid(void* h, unsigned char* valid, int n) {
+    LIOBuilder* b = (LIOBuilder*)h;
+    for (int i = 0; i < n; ++i) valid[i] = i < (int)b->residual_info.size() ? b->residual_info[i].is_valid : 0;
 }
 long long orc_map_export_points(void* h, double* pts, double* cov, long long max_points) {
     LIOBuilder* b = (LIOBuilder*)h;

@@ -272,7 +272,12 @@ def test_residual_reduce_matches_oracle(lio_mod, oracle_lib):
         oracle_lib.orc_destroy(o)
 
 
-def test_ieskf_predict_bit_exact(lio_mod, oracle_lib):
+def test_ieskf_predict_matches_oracle(lio_mod, oracle_lib):
+    """20 single IESKF::predict steps (ieskf.cpp:101-123) through
+    vmp_ieskf_predict.  The step's SO3 exp calls sin / cos, whose CUDA and
+    glibc results may differ in the last bit, so state and covariance are
+    compared within 1e-13 (absolute for the state, relative for P), not bit
+    for bit."""
     rng = np.random.default_rng(9)
     cfg = abi.default_config()
     g = lio_mod.LIOBuilder(cfg)
@@ -293,7 +298,6 @@ def test_ieskf_predict_bit_exact(lio_mod, oracle_lib):
         xo = abi.vmp_state()
         Po = np.zeros(529)
         oracle_lib.orc_get_state(o, C.byref(xo), _dp(Po))
-        dx = max(abs(a - b) for a, b in zip(bytes(xg), bytes(xo))) if False else None
         for f in ("pos", "rot", "vel", "bg", "ba", "g"):
             a = np.array(getattr(xg, f)[:])
             b = np.array(getattr(xo, f)[:])

@@ -60,10 +60,60 @@ def test_noalloc_downsample_matches_existing_entry_point():
     g.close()
 
 
+def _noalloc(lib, d_in, n, leaf, d_out):
+    m = C.c_int(-1)
+    code = lib.vmp_downsample_noalloc(C.c_void_p(d_in), n, leaf, C.c_void_p(d_out), C.byref(m), None)
+    return code, m.value
+
+
+def test_noalloc_downsample_overflow_and_single_point():
+    """The two other ways out of the filter: a leaf so small that the leaf
+    grid would overflow 32-bit indices (the input comes back unchanged, as
+    pcl::VoxelGrid returns it) and a one-point cloud -- each bit for bit as
+    the existing entry point gives them."""
+    import torch
+    from voxelmapplus_fastlio2_gb300 import lio
+    lib = _lib()
+    g = lio.LIOBuilder(abi.default_config(max_scan_points=MAX_POINTS))
+    rng = np.random.default_rng(77)
+    for n, leaf in ((5000, 1e-4), (1, 0.1)):
+        pts = _cloud(rng, n)
+        ref = g.downsample(pts, leaf)
+        if leaf < 1e-3:
+            assert ref.shape[0] == n  # the overflow path: output = input
+        d_in = torch.from_numpy(pts).cuda()
+        d_out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        code, m = _noalloc(lib, d_in.data_ptr(), n, leaf, d_out.data_ptr())
+        assert code == abi.VMP_OK, abi.STATUS_NAMES.get(code)
+        assert m == ref.shape[0]
+        got = d_out[:m].cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    g.close()
+
+
 def test_noalloc_downsample_rejects_oversize_and_bad_args():
+    """Sizes beyond the limit and pointers the float4 kernels cannot take are
+    rejected before anything is launched: a device pointer off by 4 bytes, a
+    host (numpy) array, and an output that overlaps the input."""
+    import torch
     lib = _lib()
     m = C.c_int(0)
     dummy = C.c_void_p(1)
-    assert lib.vmp_downsample_noalloc(dummy, MAX_POINTS + 1, 0.1, dummy, C.byref(m), None) == 9  # VMP_ERR_CAPACITY
-    assert lib.vmp_downsample_noalloc(dummy, 10, 0.0, dummy, C.byref(m), None) == 1  # VMP_ERR_INVALID_ARG
+    assert lib.vmp_downsample_noalloc(dummy, MAX_POINTS + 1, 0.1, dummy, C.byref(m), None) == abi.VMP_ERR_CAPACITY
+    assert lib.vmp_downsample_noalloc(dummy, 10, 0.0, dummy, C.byref(m), None) == abi.VMP_ERR_INVALID_ARG
     assert lib.vmp_downsample_noalloc(None, 0, 0.1, None, C.byref(m), None) == 0 and m.value == 0
+    n = 1000
+    d_in = torch.zeros((2 * n + 4, 4), dtype=torch.float32, device="cuda")
+    d_out = torch.zeros((n + 4, 4), dtype=torch.float32, device="cuda")
+    host = np.zeros((n, 4), dtype=np.float32)
+    torch.cuda.synchronize()
+    base_in, base_out = d_in.data_ptr(), d_out.data_ptr()
+    assert _noalloc(lib, base_in + 4, n, 0.1, base_out)[0] == abi.VMP_ERR_INVALID_ARG  # misaligned input
+    assert _noalloc(lib, base_in, n, 0.1, base_out + 4)[0] == abi.VMP_ERR_INVALID_ARG  # misaligned output
+    assert _noalloc(lib, host.ctypes.data, n, 0.1, base_out)[0] == abi.VMP_ERR_INVALID_ARG  # host input
+    assert _noalloc(lib, base_in, n, 0.1, host.ctypes.data)[0] == abi.VMP_ERR_INVALID_ARG  # host output
+    assert _noalloc(lib, base_in, n, 0.1, base_in)[0] == abi.VMP_ERR_INVALID_ARG  # in place
+    assert _noalloc(lib, base_in, n, 0.1, base_in + 16 * (n - 1))[0] == abi.VMP_ERR_INVALID_ARG  # overlap
+    code, _ = _noalloc(lib, base_in, n, 0.1, base_in + 16 * n)  # adjacent, not overlapping
+    assert code == abi.VMP_OK, abi.STATUS_NAMES.get(code)

@@ -38,6 +38,7 @@ def _declare(lib):
         "vmp_map_update": ([vp, P(d), P(d), C.c_int], st),
         "vmp_map_info_get": ([vp, P(abi.vmp_map_info)], st),
         "vmp_map_export": ([vp, P(abi.vmp_voxel), C.c_longlong, P(C.c_longlong)], st),
+        "vmp_map_keys": ([vp, P(C.c_int64), C.c_longlong, P(C.c_longlong)], st),
         "vmp_map_import": ([vp, P(abi.vmp_voxel), C.c_longlong, P(d), P(d), C.c_longlong], st),
         "vmp_map_export_points": ([vp, P(d), P(d), C.c_longlong, P(C.c_longlong)], st),
         "vmp_residual_reduce": ([vp, P(abi.vmp_state), P(d), P(d), P(d), C.c_int, P(d), P(d), P(C.c_int)], st),

@@ -57,7 +57,6 @@ void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------- downsample
-constexpr int kMinMaxBlocks = 152;
 
 __global__ void k_minmax_partial(const float4* __restrict__ c, const int* d_n, float* blk) {
     __shared__ float red[6][kPtThreads];

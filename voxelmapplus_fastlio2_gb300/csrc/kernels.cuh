@@ -6,6 +6,10 @@
 
 namespace vmp {
 
+// CTAs of the downsample's bounding-box pass (k_minmax_partial); the scratch
+// behind DScan::blk_minmax holds kMinMaxBlocks * 6 + 8 floats.
+constexpr int kMinMaxBlocks = 152;
+
 // Per-scan device buffers of one stream.
 // Per-scan scalars on the device (one host->device copy per scan), so that a
 // captured graph of the scan needs no per-scan kernel parameters.
@@ -33,7 +37,7 @@ struct DScan {
     float4* down;          // [max_pts]
     int* d_n_down;
     float* minmax;         // [6] + per-block partials
-    float* blk_minmax;     // [blocks * 6]
+    float* blk_minmax;     // [kMinMaxBlocks * 6 + 8]
     int* ds_params;        // [16] leaf grid parameters / overflow flag
     uint32_t* run_start;   // [max_pts + 1]
     // per downsampled point

@@ -102,6 +102,16 @@ __global__ void k_export(DMap m, vmp_voxel* out, int* d_count, int max) {
         for (int k = 0; k < 36; ++k) v.cov[k] = c.cov[k];
     }
 }
+// Keys and LRU stamps of the live records (for vmp_map_keys).
+__global__ void k_export_keys(DMap m, unsigned long long* out /* [max][2] */, int* d_count, int max) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m.rec_pool; r += gridDim.x * blockDim.x) {
+        if (!(m.hot[r].flags & F_ALIVE)) continue;
+        const int pos = atomicAdd(d_count, 1);
+        if (pos >= max) continue;
+        out[2 * (size_t)pos] = m.cold[r].stamp;
+        out[2 * (size_t)pos + 1] = m.cold[r].key;
+    }
+}
 // Test hook: the shared-divisor division against the FP64 division, per pair.
 __global__ void k_div_check(const double* a, const double* b, int n, double* by_recip, double* by_div) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -609,7 +619,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     CREATE_TRY(dalloc(s, &sc.down, max_pts));
     CREATE_TRY(dalloc(s, &sc.d_n_down, 4));
     CREATE_TRY(dalloc(s, &sc.minmax, 8));
-    CREATE_TRY(dalloc(s, &sc.blk_minmax, 152 * 6 + 8));
+    CREATE_TRY(dalloc(s, &sc.blk_minmax, kMinMaxBlocks * 6 + 8));
     CREATE_TRY(dalloc(s, &sc.ds_params, 32));
     CREATE_TRY(dalloc(s, &sc.run_start, max_pts + 16));
     CREATE_TRY(dalloc(s, &sc.pl, (size_t)max_pts * 3));
@@ -1324,6 +1334,43 @@ vmp_status vmp_map_export(vmp_stream_t s, vmp_voxel* out, long long max, long lo
     long long n = std::min<long long>(max, (long long)all.size());
     if (n > 0) std::memcpy(out, all.data(), sizeof(vmp_voxel) * (size_t)n);
     if (n_out) *n_out = (long long)all.size();
+    return VMP_OK;
+}
+
+vmp_status vmp_map_keys(vmp_stream_t s, int64_t* keys, long long max, long long* n_out) {
+    if (!s || max < 0 || (!keys && max > 0)) return VMP_ERR_INVALID_ARG;
+    if (s->broken) return fail(s, VMP_ERR_CUDA, "stream unusable after a CUDA error: " + s->err);
+    vmp_status v = read_counters(s);
+    if (v != VMP_OK) return v;
+    const long long n = s->h_cnt->size;
+    if (n_out) *n_out = n;
+    if (n == 0 || max == 0) return VMP_OK;
+    unsigned long long* d = nullptr;
+    VMP_TRY(cudaMallocAsync(&d, sizeof(unsigned long long) * (2 * (size_t)n + 1), s->st), "key export");
+    int* d_count = reinterpret_cast<int*>(d + 2 * (size_t)n);
+    std::vector<unsigned long long> h(2 * (size_t)n);
+    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(int), s->st);
+    if (e == cudaSuccess) {
+        VMP_NOTE_LAUNCH(); k_export_keys<<<1216, 256, 0, s->st>>>(s->m, d, d_count, (int)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h.data(), d, sizeof(unsigned long long) * 2 * (size_t)n, cudaMemcpyDeviceToHost, s->st);
+    cudaFreeAsync(d, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cuda_fail(s, e, "key export");
+    std::vector<size_t> ord((size_t)n);
+    for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return h[2 * a] > h[2 * b]; });
+    const long long m = std::min(max, n);
+    for (long long i = 0; i < m; ++i) {
+        int64_t x, y, z;
+        unpack_key(h[2 * ord[(size_t)i] + 1], x, y, z);
+        keys[3 * i] = x;
+        keys[3 * i + 1] = y;
+        keys[3 * i + 2] = z;
+    }
+    s->io_d2h += (long long)sizeof(unsigned long long) * 2 * n;
     return VMP_OK;
 }
 

@@ -15,11 +15,18 @@
 // In host code the array's name is only a host-side handle, not a device
 // address: the first call on each device (with that device current) resolves
 // the device address with cudaGetSymbolAddress and caches it, so that first
-// call should come before any stream capture.  All calls share the one array:
-// two calls whose work overlaps on the GPU race on it and must be serialised
-// by the caller (same stream, or events).  Each call writes every scratch word
-// it reads before reading it, so nothing has to start at zero and no state
-// survives from one call to the next.
+// call should come before any stream capture.  The cached address belongs to
+// the device's context of that moment: cudaDeviceReset while libvmp is loaded
+// is not supported.  All calls share the one array: two calls whose work
+// overlaps on the GPU race on it and must be serialised by the caller (same
+// stream, or events).  Each call writes every scratch word it reads before
+// reading it, so nothing has to start at zero and no state survives from one
+// call to the next.
+//
+// The input and output are read as float4, so both must be 16-byte aligned
+// device (or managed) memory, and they must not overlap: the centroid pass
+// reads input points across the whole cloud while other threads write output
+// points.  All three are checked before anything is launched.
 #include <mutex>
 
 #include "kernels.cuh"
@@ -44,7 +51,7 @@ constexpr size_t kOffNRaw = 0;
 constexpr size_t kOffNDown = align256(kOffNRaw + sizeof(int));
 constexpr size_t kOffParams = align256(kOffNDown + sizeof(int));
 constexpr size_t kOffMinMax = align256(kOffParams + 32 * sizeof(int));
-constexpr size_t kOffSortK = align256(kOffMinMax + (152 * 6 + 8) * sizeof(float));
+constexpr size_t kOffSortK = align256(kOffMinMax + (kMinMaxBlocks * 6 + 8) * sizeof(float));
 constexpr size_t kOffSortV = align256(kOffSortK + kU32N);
 constexpr size_t kOffFlags = align256(kOffSortV + kU32N);
 constexpr size_t kOffScan = align256(kOffFlags + kU32N);
@@ -59,6 +66,16 @@ static_assert(kOffEnd <= kNoAllocBytes, "no-alloc scratch layout exceeds the sta
 
 std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_dev_ptr[kNoAllocMaxDevices] = {};
+
+// Device or managed memory (cudaPointerGetAttributes allocates nothing).
+bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
 
 __global__ void k_noalloc_set_n(int* p, int v) {
     if (threadIdx.x == 0) *p = v;
@@ -94,6 +111,11 @@ extern "C" vmp_status vmp_downsample_noalloc(const vmp_point* d_in, int n, doubl
         *n_out = 0;
         return VMP_OK;
     }
+    const uintptr_t in_a = reinterpret_cast<uintptr_t>(d_in), out_a = reinterpret_cast<uintptr_t>(d_out);
+    const uintptr_t bytes = uintptr_t(n) * sizeof(vmp_point);
+    if ((in_a | out_a) & 15) return VMP_ERR_INVALID_ARG;              // float4 loads and stores
+    if (in_a < out_a + bytes && out_a < in_a + bytes) return VMP_ERR_INVALID_ARG;  // overlapping buffers
+    if (!is_device_pointer(d_in) || !is_device_pointer(d_out)) return VMP_ERR_INVALID_ARG;
     unsigned char* base = nullptr;
     if (noalloc_scratch(&base) != cudaSuccess) {
         cudaGetLastError();

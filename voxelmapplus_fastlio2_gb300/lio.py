@@ -92,6 +92,15 @@ class VoxelMapView:
         check(self._o.h, self._o.lib.vmp_map_export(self._o.h, arr, n.value, C.byref(n)))
         return arr, n.value
 
+    def keys(self):
+        """Keys of all voxels, most recently used first ((n, 3) int64)."""
+        n = C.c_longlong()
+        check(self._o.h, self._o.lib.vmp_map_keys(self._o.h, None, 0, C.byref(n)))
+        out = np.zeros((max(1, n.value), 3), dtype=np.int64)
+        check(self._o.h, self._o.lib.vmp_map_keys(self._o.h, out.ctypes.data_as(C.POINTER(C.c_int64)), n.value,
+                                                  C.byref(n)))
+        return out[: n.value]
+
     def planes(self, max_markers=100000):
         """voxel2MarkerArray's data: the frozen planes in LRU order
         (records of abi.plane_marker_dtype())."""
