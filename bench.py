@@ -16,7 +16,8 @@ HBM budget, served by libvmp's server (vmp_submit / vmp_poll).
   value     scans/s of all streams: `--steps` mapping scans per stream, the
             packages already in HBM (vmp_submit_device), all submitted at
             once, wall time until the last result is on the host;
-  e2e       the same from host memory (vmp_submit copies each package; the
+  e2e       the same scans from the same map states on a second server,
+            packages from host memory (vmp_submit copies each package; the
             host->device copies and the result reads are inside the timing);
   latency   open loop: each stream a Poisson process at 10 Hz, p50 / p99 of
             (result on host - submission);
@@ -28,6 +29,8 @@ HBM budget, served by libvmp's server (vmp_submit / vmp_poll).
             FP64-bound phases against the FP64 pipe's issue rate;
   cpu_baseline  the CPU oracle (restated reference, one thread as the
             reference's MP_PROC_NUM=1) on a bounded sample of the streams.
+The line ends with latency_ms and served_over_plain_same_mix (the metric's
+two halves); per-phase detail goes to stderr ("bench detail: {...}").
 `--impl reference` runs the CPU restatement on all streams of the served
 workload, one single-threaded oracle per stream, all host cores.
 
@@ -652,7 +655,9 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
         name = SERVE_NAME.replace("64 independent", f"{args.streams} independent")
     else:
         name = SERVE_NAME
-    cfg_line = {"workload": name, "streams_per_gpu": args.streams, "rays_per_scan": [s[1] for s in streams],
+    rays = [s[1] for s in streams]
+    cfg_line = {"workload": name, "streams_per_gpu": args.streams,
+                "rays_per_scan": {"min": min(rays), "max": max(rays), "mean": round(float(np.mean(rays)))},
                 "ieskf_max_iter": {"room": 5, "urban": 4}, "scan_resolution": {"room": 0.2, "urban": 0.1},
                 "voxel_size": 0.5, "map_capacity": {"room": 100000, "urban": 400000},
                 "parallelism": f"stream-sharded x{ws}, {args.streams} streams per GPU"}
@@ -676,12 +681,14 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
         print(json.dumps(line))
         return
     vbuild.build_all()
-    pkgs = make_serve_packages(streams, 2 + W + 2 * K + L)
+    pkgs = make_serve_packages(streams, 2 + W + K + L)
     workers = args.workers or min(32, len(streams))
-    served = run_served(args, streams, pkgs, workers, ["device", "host", "open"], barrier, keep_results=True)
+    # value (packages in HBM) and e2e (host buffers) on two servers fed the
+    # same packages: the same scans from the same map states
+    served = run_served(args, streams, pkgs, workers, ["device", "open"], barrier, keep_results=True)
     gpu_res = {(r[0], r[1]): (r[2], r[3], r[6]) for r in served["device"].pop("results")}
-    for ph in ("host", "open"):
-        served[ph].pop("results", None)
+    served["open"].pop("results", None)
+    served_host = run_served(args, streams, pkgs, workers, ["host"], barrier)
     plain_mix = run_served(args, streams, pkgs, 1, ["device"], barrier)
     # plain one-stream urban block (per-phase profile: the kernel roofline)
     kind, pts, ucfg, seed, uname = workload(args, rank, "urban")
@@ -692,33 +699,33 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
     uval_s = sum(uval["step_ms"]) / 1e3
     dv = served["device"]
     value = aggregate_value(ws, dv["scans"], dv["wall_s"], allmax)
-    hv = served["host"]
+    hv = served_host["host"]
     h2d = float(np.mean([p.n * C.sizeof(abi.vmp_point) + p.n_imu * C.sizeof(abi.vmp_imu)
-                         for pk in pkgs for p in pk[2 + W + K:2 + W + 2 * K]]))
+                         for pk in pkgs for p in pk[2 + W:2 + W + K]]))
+    roof = roofline_of(uval["prof"])
+    detail = {"served": {"streams": args.streams, "workers": workers, "hbm_budget_gb": args.hbm_budget_gb,
+                         "budget_used_gb": served["budget_used_gb"], "autotuner": served["tuning"],
+                         "device_resident": dv, "host_buffers": hv, "open_loop_10hz": served["open"]},
+              "rays_per_scan": rays, "roofline_phases": roof.pop("phases"),
+              "fp64_phases": roof["fp64"].pop("phases"),
+              "profile_ms_per_step_urban200k": {k: v["ms"] / uval["prof_steps"] for k, v in uval["prof"].items()}}
+    roof["measured_on"] = "plain one-stream urban block run"
     line = {"metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": 1e3 * allmax(dv["wall_s"]) / dv["scans"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-            "config": dict(cfg_line, steps_meaning=f"{K} mapping scans per stream, all submitted at once; "
-                                                   "value = scans of all streams / wall time"),
-            "latency_ms": served["open"]["latency_ms"],
+            "config": cfg_line,
+            "steps_meaning": f"{K} mapping scans per stream, all submitted at once; value = scans of all streams "
+                             "/ wall time; e2e = the same scans from the same map states on a second server, "
+                             "packages from host memory",
             "e2e": {"value": ws * hv["scans"] / allmax(hv["wall_s"]), "unit": "scans/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(C.sizeof(abi.vmp_result)),
                     "latency_ms": hv["latency_ms"]},
-            "served": {"streams": args.streams, "workers": workers, "hbm_budget_gb": args.hbm_budget_gb,
-                       "budget_used_gb": served["budget_used_gb"], "autotuner": served["tuning"],
-                       "device_resident": dv, "host_buffers": hv,
-                       "open_loop_10hz": served["open"]},
             "plain_1stream": {
                 "same_mix_scans_per_s": plain_mix["device"]["scans_per_s"],
-                "same_mix_note": "the same streams and packages with one package on the GPU at a time",
                 "urban200k": {"scans_per_s": len(uval["step_ms"]) / uval_s,
                               "latency_ms": {"p50": float(np.percentile(uval["step_ms"], 50)),
-                                             "p99": float(np.percentile(uval["step_ms"], 99))},
-                              "workload": uname}},
-            "served_over_plain_same_mix": dv["scans_per_s"] / plain_mix["device"]["scans_per_s"],
-            "roofline": dict(roofline_of(uval["prof"]), measured_on="plain one-stream urban block run"),
-            "profile_ms_per_step_urban200k": {k: v["ms"] / uval["prof_steps"] for k, v in uval["prof"].items()},
-            "clocks": dv["clocks"], "gpu_launches": dv["launches"]}
+                                             "p99": float(np.percentile(uval["step_ms"], 99))}}},
+            "roofline": roof, "clocks": dv["clocks"], "gpu_launches": dv["launches"]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         ids = list(range(min(4, len(streams))))
         cpk = [pkgs[i][:2 + W + K] if i in ids else [] for i in range(len(streams))]
@@ -730,7 +737,13 @@ def main_serve(args, rank, ws, barrier, allmax, dist):
                                           f"{[streams[i][1] for i in ids]}) after {W} warm-up scans; CPU "
                                           "restatement of the reference on 1 thread",
                                 "host_cores": os.cpu_count()}
+    # the metric's two halves last, so that a record keeping only the end of
+    # the line still holds them
+    line["latency_ms"] = dict(served["open"]["latency_ms"], arrivals="Poisson 10 Hz per stream",
+                              streams=args.streams)
+    line["served_over_plain_same_mix"] = dv["scans_per_s"] / plain_mix["device"]["scans_per_s"]
     if rank == 0:
+        print("bench detail: " + json.dumps(detail), file=sys.stderr)
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -333,6 +333,11 @@ vmp_status vmp_test_division(const double* a, const double* b, int n, double* by
 vmp_status vmp_test_body_cov(const double* pts, int n, double range_inc, double degree_inc, double* pts_out,
                              double* cov);
 
+/* Test hook: point_crossmat * P_rr * point_crossmat^T (lio_builder.cpp:199-202,
+ * 240-243) on the device for n points (pts n x 3) and matrices (M n x 9),
+ * host arrays; out n x 9. */
+vmp_status vmp_test_hat_sandwich(const double* pts, const double* M, int n, double* out);
+
 /* The same leaf-centroid downsample for callers that cannot allocate device
  * memory (no counterpart in the reference): a real-time sensor thread that
  * must not call cudaMalloc/cudaFree, or a host framework whose own allocator

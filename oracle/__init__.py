@@ -77,6 +77,8 @@ def load():
     lib.orc_calc_body_cov.argtypes = [P(d), C.c_int, d, d, P(d), P(d)]
     lib.orc_last_cloud.argtypes = [vp, C.c_int, P(abi.vmp_point), C.c_int]
     lib.orc_last_cloud.restype = C.c_int
+    lib.orc_hat_sandwich.argtypes = [P(d), P(d), C.c_int, P(d)]
+    lib.orc_restatement_check.argtypes = [C.c_int, C.c_longlong, C.c_ulonglong, P(C.c_longlong), P(d)]
     lib.orc_so3_exp.argtypes = [P(d), P(d)]
     lib.orc_so3_log.argtypes = [P(d), P(d)]
     lib.orc_eig_sym3.argtypes = [P(d), P(d), P(d)]

@@ -167,23 +167,12 @@ inline M3 hat(const V3& w) {
     return m;
 }
 
-// [w]x M [w]x^T as ([w]x M) [w]x^T without the products with [w]x's zero
-// diagonal: the dense left-to-right sums less their +-0 terms (the same
-// values up to the sign of an exact zero; the device evaluates it alike).
+// point_crossmat * P_rr * point_crossmat.transpose() (lio_builder.cpp:199-202,
+// 240-243) as written: t = [w]x M, then t [w]x^T, every entry a dense k = 0..2
+// left-to-right sum (the products with [w]x's zero diagonal included).
 inline M3 hatSandwich(const V3& w, const M3& M) {
     const M3 h = hat(w);
-    M3 t, o;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            const int k0 = i == 0 ? 1 : 0, k1 = i == 2 ? 1 : 2;
-            t(i, j) = h(i, k0) * M(k0, j) + h(i, k1) * M(k1, j);
-        }
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            const int k0 = j == 0 ? 1 : 0, k1 = j == 2 ? 1 : 2;
-            o(i, j) = t(i, k0) * h(j, k0) + t(i, k1) * h(j, k1);
-        }
-    return o;
+    return (h * M) * T(h);
 }
 
 struct Quat { double w, x, y, z; };

@@ -239,19 +239,12 @@ inline void calcBodyCov(V3& pb, double range_inc, double degree_inc, M3& cov) {
     N(0, 0) = b1[0]; N(0, 1) = b2[0];
     N(1, 0) = b1[1]; N(1, 1) = b2[1];
     N(2, 0) = b1[2]; N(2, 1) = b2[2];
-    // A = (range [d]x) N and A dvar, without the products with the zero
-    // diagonal of [d]x and the zero off-diagonal of dvar: the dense sums less
-    // their +-0 terms (the same values up to the sign of an exact zero; the
-    // device evaluates it alike)
-    M32 A, AD;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 2; ++j) {
-            const int k0 = i == 0 ? 1 : 0, k1 = i == 2 ? 1 : 2;
-            A(i, j) = (range * dh(i, k0)) * N(k0, j) + (range * dh(i, k1)) * N(k1, j);
-        }
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 2; ++j) AD(i, j) = A(i, j) * dvar(j, j);
-    cov = (d * range_var) * T(d) + AD * T(A);
+    // A = range * direction_hat * N, cov = d range_var d^T + A dvar A^T
+    // (commons.cpp:40-43) as written: (range [d]x) N and (A dvar) A^T, dense
+    // left-to-right sums (the products with the zeros of [d]x and dvar
+    // included)
+    const M32 A = (range * dh) * N;
+    cov = (d * range_var) * T(d) + (A * dvar) * T(A);
 }
 
 // ---------------------------------------------------------------- VoxelMap
@@ -424,40 +417,25 @@ void VoxelGrid::updatePlane() {  // voxel_map.cpp:97-136
     eigSym3(cov, evals, evecs);
     if (evals[0] > plane_thresh) { is_plane = false; return; }
     is_plane = true;
-    // J = [evecs * F; I / n] (voxel_map.cpp:115-130).  The per-refit factors
-    // are formed once, the products with J's known zeros (row 0 of F, the
-    // off-diagonal of I / n) are left out (the same sums without their +-0
-    // terms), and J cov J^T is accumulated as the symmetric matrix it is:
-    // its upper triangle per point, mirrored after the refit's points.
-    const double inv_n = 1.0 / static_cast<double>(plane.n);
+    // J = [evecs * F; J_Q], J_Q = I / n, and plane.cov += J * pv.cov * J^T
+    // (voxel_map.cpp:115-130) as written: F's row 0 stays zero, J_Q has its
+    // zero off-diagonal, every product is the dense left-to-right sum
+    // (J * pv.cov first, then (J * pv.cov) * J^T), and all 36 entries are
+    // accumulated, the lower triangle with its own rounding.
+    M3 J_Q = M3::Identity() / static_cast<double>(plane.n);
     V3 pn = v3(evecs(0, 0), evecs(1, 0), evecs(2, 0));
-    M3 Mm[3];
-    double den[3] = {0.0, 0.0, 0.0};
-    for (int m = 1; m < 3; m++) {
-        V3 vm = v3(evecs(0, m), evecs(1, m), evecs(2, m));
-        Mm[m] = vm * T(pn) + pn * T(vm);
-        den[m] = (plane.n) * (evals[0] - evals[m]);
-    }
     for (PointWithCov& pv : temp_points) {
-        const V3 d = pv.point - plane.mean;
         M3 F = M3::Zero();
         for (int m = 1; m < 3; m++) {
-            Mat<1, 3> Fm = (T(d) / den[m]) * Mm[m];
+            V3 vm = v3(evecs(0, m), evecs(1, m), evecs(2, m));
+            Mat<1, 3> Fm = (T(pv.point - plane.mean) / ((plane.n) * (evals[0] - evals[m]))) * (vm * T(pn) + pn * T(vm));
             F(m, 0) = Fm(0, 0); F(m, 1) = Fm(0, 1); F(m, 2) = Fm(0, 2);
         }
-        M3 top;
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) top(i, j) = evecs(i, 1) * F(1, j) + evecs(i, 2) * F(2, j);
-        const M3 A = top * pv.cov;  // rows 0-2 of J * cov
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                if (j >= i) plane.cov(i, j) += (A(i, 0) * top(j, 0) + A(i, 1) * top(j, 1)) + A(i, 2) * top(j, 2);
-                plane.cov(i, 3 + j) += A(i, j) * inv_n;
-                if (j >= i) plane.cov(3 + i, 3 + j) += (inv_n * pv.cov(i, j)) * inv_n;
-            }
+        Mat<6, 3> J;
+        J.setBlock(0, 0, evecs * F);
+        J.setBlock(3, 0, J_Q);
+        plane.cov += (J * pv.cov) * T(J);
     }
-    for (int i = 0; i < 6; ++i)
-        for (int j = i + 1; j < 6; ++j) plane.cov(j, i) = plane.cov(i, j);
     double axis_distance = -dot(plane.mean, pn);
     if (axis_distance < 0.0) pn = -pn;
     plane.norm = pn;
@@ -1060,6 +1038,15 @@ int orc_downsample(const vmp_point* pts, int n, double leaf, vmp_point* out) {
     return (int)o.size();
 }
 
+// point_crossmat * P_rr * point_crossmat^T as written (lio_builder.cpp:199-202).
+void orc_hat_sandwich(const double* pts, const double* M, int n, double* out) {
+    for (int i = 0; i < n; ++i) {
+        M3 m;
+        for (int k = 0; k < 9; ++k) m[k] = M[i * 9 + k];
+        const M3 o = hatSandwich(v3(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]), m);
+        for (int k = 0; k < 9; ++k) out[i * 9 + k] = o[k];
+    }
+}
 void orc_calc_body_cov(const double* pts, int n, double range_inc, double degree_inc, double* pts_out, double* cov) {
     for (int i = 0; i < n; ++i) {
         V3 p = v3(pts[i * 3], pts[i * 3 + 1], pts[i * 3 + 2]);

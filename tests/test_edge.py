@@ -158,14 +158,20 @@ def test_shared_divisor_division_is_exact():
 @pytest.mark.gpu
 def test_body_cov_bit_exact(oracle_lib):
     """calcBodyCov on the device (normalisations through one reciprocal per
-    vector with Markstein's correction) against the oracle, bit for bit,
-    including points with z == 0 (fixed to 0.001 in place, as the reference)."""
+    vector with Markstein's correction, the products with the zeros of
+    direction_hat and dvar left out) against the oracle's dense form
+    (commons.cpp:18-45 as written), bit for bit over 1 M points, including
+    points with z == 0 (fixed to 0.001 in place, as the reference) and
+    exact zeros of both signs in x and y."""
     from voxelmapplus_fastlio2_gb300._lib import load
     rng = np.random.default_rng(23)
-    n = 50000
+    n = 1_000_000
     pts = rng.normal(0, 8, (n, 3))
     pts[::97, 2] = 0.0
     pts[::89] = pts[::89].astype(np.float32).astype(np.float64)
+    pts[::53, 0] = 0.0
+    pts[::59, 1] = -0.0
+    pts[::61, 2] = -0.0
     gp, gc = np.zeros((n, 3)), np.zeros((n, 9))
     op, oc = np.zeros((n, 3)), np.zeros((n, 9))
     dp = lambda x: C.c_void_p(x.ctypes.data)
@@ -173,6 +179,30 @@ def test_body_cov_bit_exact(oracle_lib):
     oracle_lib.orc_calc_body_cov(_dp(pts), n, 0.04, 0.1, _dp(op), _dp(oc))
     assert np.array_equal(gp, op)
     assert np.array_equal(gc.view(np.uint64), oc.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_hat_sandwich_matches_dense_form(oracle_lib):
+    """[p]x P_rr [p]x^T on the device (the products with [p]x's zero diagonal
+    left out) against the oracle's dense form (lio_builder.cpp:199-202 as
+    written) over 1 M inputs with exact zeros of both signs: equal values
+    everywhere, bits different only where the value is zero."""
+    from voxelmapplus_fastlio2_gb300._lib import load
+    rng = np.random.default_rng(29)
+    n = 1_000_000
+    pts = rng.normal(0, 10, (n, 3))
+    for k, step in enumerate((7, 11, 13)):
+        pts[::step, k] = 0.0 if k % 2 else -0.0
+    A = rng.normal(0, 0.02, (n, 3, 3))
+    M = (A @ A.transpose(0, 2, 1) + np.eye(3) * 1e-4).reshape(n, 9)
+    M[::17, 1] = M[::17, 3] = 0.0
+    gout, oout = np.zeros((n, 9)), np.zeros((n, 9))
+    dp = lambda x: C.c_void_p(x.ctypes.data)
+    assert load().vmp_test_hat_sandwich(dp(pts), dp(M), n, dp(gout)) == 0
+    oracle_lib.orc_hat_sandwich(_dp(pts), _dp(M), n, _dp(oout))
+    assert np.array_equal(gout, oout)
+    bits = gout.view(np.uint64) != oout.view(np.uint64)
+    assert np.all(oout[bits] == 0.0)
 
 
 @pytest.mark.gpu

@@ -80,6 +80,7 @@ def _declare(lib):
         "vmp_map_planes": ([vp, vp, C.c_int, P(C.c_int)], st),
         "vmp_test_division": ([vp, vp, C.c_int, vp, vp], st),
         "vmp_test_body_cov": ([vp, C.c_int, d, d, vp, vp], st),
+        "vmp_test_hat_sandwich": ([vp, vp, C.c_int, vp], st),
         "vmp_test_barrier_timeout": ([C.c_int, C.c_longlong, P(C.c_int), P(d)], st),
         "vmp_std_plane_voxels": ([vp, C.c_int, C.c_int, d, C.c_int, d, vp, C.c_int, P(C.c_int)], st),
         "vmp_livox_decode": ([vp, vp, C.c_int, C.c_int, d, d, vp, vp, P(C.c_int), P(C.c_float)], st),

@@ -258,6 +258,15 @@ __global__ void k_body_cov_check(const double* pts, int n, double range_inc, dou
     }
 }
 
+// Test hook: [p]x M [p]x^T (hat_sandwich) for explicit points and matrices.
+__global__ void k_hat_sandwich_check(const double* pts, const double* M, int n, double* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double o[9];
+        hat_sandwich(pts + 3 * (size_t)i, M + 9 * (size_t)i, o);
+        for (int k = 0; k < 9; ++k) out[i * 9 + k] = o[k];
+    }
+}
+
 // ---------------------------------------------------------------- map batch
 __global__ void k_map_batch(const DFilter* __restrict__ f, const float4* __restrict__ pts, const int* d_n,
                             const double* __restrict__ pl, const double* __restrict__ covl, int full,
@@ -452,6 +461,28 @@ extern "C" vmp_status vmp_test_body_cov(const double* pts, int n, double range_i
     }
     if (e == cudaSuccess) e = cudaMemcpy(pts_out, d + 3 * (size_t)n, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(cov, d + 6 * (size_t)n, sizeof(double) * 9 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return VMP_ERR_CUDA;
+    }
+    return VMP_OK;
+}
+
+extern "C" vmp_status vmp_test_hat_sandwich(const double* pts, const double* M, int n, double* out) {
+    if (n < 0 || (n > 0 && (!pts || !M || !out))) return VMP_ERR_INVALID_ARG;
+    if (n == 0) return VMP_OK;
+    double* d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * 21 * (size_t)n) != cudaSuccess) return VMP_ERR_OUT_OF_MEMORY;
+    cudaError_t e = cudaMemcpy(d, pts, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + 3 * (size_t)n, M, sizeof(double) * 9 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        VMP_NOTE_LAUNCH();
+        vmp::k_hat_sandwich_check<<<(n + 255) / 256 < 1216 ? (n + 255) / 256 : 1216, 256>>>(
+            d, d + 3 * (size_t)n, n, d + 12 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 12 * (size_t)n, sizeof(double) * 9 * (size_t)n, cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) {
         cudaGetLastError();
