@@ -11,10 +11,15 @@
 //     u = R^T n, v = n x p,      r_cov = u^T S u,
 // and the H / b accumulation uses FMA; these differ from the reference's
 // dense evaluation only by rounding (relative 1e-16), which cannot move a gate
-// decision except for a residual within that distance of its threshold.  The
-// upper triangle of H (and b, and the valid count) is reduced by warp shuffles
-// and a per-block fold; the last CTA to finish folds the block partials in a
-// fixed order (deterministic) and runs the filter step.
+// decision except for a residual within that distance of its threshold.
+// Accumulation: the valid points of a warp's 32 are compacted (ballot, lane
+// order) into a shared-memory row per point -- J, J w, r, 1 -- and lane k of
+// the warp then adds entry k of the upper triangle of H (then b, then the
+// valid count) over those rows: one FMA per row and value, every lane busy,
+// one accumulator per lane instead of 28 per thread.  Warps, then blocks are
+// folded in a fixed order; the last CTA to finish folds the block partials
+// (a fixed stripe-then-sum tree) and runs the filter step, so the result
+// depends only on the grid, which depends only on the scan size bound.
 //
 // The filter step solves the reference's information-form normal equations
 //     H = J^T P^-1 J + E Hm E^T,  b = J^T P^-1 d + E bm,  step = -H^-1 b
@@ -27,6 +32,8 @@
 // Gauss-Jordan solve and products with block-diagonal matrices, all spread
 // over the lanes, with the transcendental functions of the boxminus / boxplus
 // on separate lanes.
+#include <cstdlib>
+
 #include "kernels.cuh"
 
 namespace vmp {
@@ -38,15 +45,28 @@ template <int NJ>
 struct Red {
     static constexpr int NH = NJ * (NJ + 1) / 2;
     static constexpr int NV = NH + NJ + 1;  // H upper triangle, b, count
-    static constexpr int NP = (NV + 31) / 32 * 32;  // padded to whole warps
+    static constexpr int VPL = (NV + 31) / 32;  // values per lane
+    static constexpr int RW = 2 * NJ + 2;  // row: J, J w, r, 1
+    static constexpr int STRIPES = kIekfThreads / NV;  // last-CTA fold
 };
 
 // ---------------------------------------------------------------- point part
+// Gate of one point (buildResidual) and, for a valid one, its Jacobian row J,
+// weight w and residual r (sharedUpdateFunc loop 2).  from_down: the LiDAR
+// point is the downsampled float point (after calcBodyCov's z == 0 fix, as
+// k_body_cov stores it), else the FP64 point of s.pl.
 template <int NJ>
-__device__ inline void residual_point(int i, const DScan& s, const DMap& m, const double* rwl, const double* pwl,
-                                      const double* rot, const double* rext, const double* pext, const double* Prr,
-                                      const double* Ppp, double* acc) {
-    const double pl[3] = {s.pl[i * 3], s.pl[i * 3 + 1], s.pl[i * 3 + 2]};
+__device__ inline bool residual_row(int i, const DScan& s, const DMap& m, int from_down, const double* rwl,
+                                    const double* pwl, const double* rot, const double* rext, const double* pext,
+                                    const double* Prr, const double* Ppp, double* J, double& w, double& r) {
+    double pl[3];
+    if (from_down) {
+        const float4 q = s.down[i];
+        pl[0] = (double)q.x; pl[1] = (double)q.y; pl[2] = (double)q.z;
+        if (pl[2] == 0) pl[2] = 0.001;
+    } else {
+        pl[0] = s.pl[i * 3]; pl[1] = s.pl[i * 3 + 1]; pl[2] = s.pl[i * 3 + 2];
+    }
     double pw[3];
     m3v(rwl, pl, pw);
     for (int a = 0; a < 3; ++a) pw[a] = pw[a] + pwl[a];
@@ -57,7 +77,8 @@ __device__ inline void residual_point(int i, const DScan& s, const DMap& m, cons
     // u = R^T n and r_cov = u^T S u of a plane found in this call: the
     // accumulation below uses the same values (same operations), so they are
     // formed once; a miss recomputes them from the stored normal
-    double u[3], r_cov = 0.0, n[3], r = 0.0;
+    double u[3], r_cov = 0.0, n[3];
+    r = 0.0;
     bool fresh = false;
     int valid = 0;
     if (rec != kNoRec) {
@@ -98,16 +119,16 @@ __device__ inline void residual_point(int i, const DScan& s, const DMap& m, cons
             r = s.rres[i];
         }
     }
-    if (!valid) return;
+    if (!valid) return false;
     if (!fresh) {
         double su[3];
         for (int c = 0; c < 3; ++c) u[c] = fma(rwl[6 + c], n[2], fma(rwl[3 + c], n[1], rwl[c] * n[0]));
         for (int c = 0; c < 3; ++c) su[c] = fma(cl[c * 3 + 2], u[2], fma(cl[c * 3 + 1], u[1], cl[c * 3] * u[0]));
         r_cov = fma(u[2], su[2], fma(u[1], su[1], u[0] * su[0]));
     }
-    const double w = r_cov < 0.0002 ? 5000 : 1.0 / r_cov;
+    w = r_cov < 0.0002 ? 5000 : 1.0 / r_cov;
     // J = [n, (-rot^T n) x q, ...]  with q = rot_ext p_l + pos_ext
-    double J[NJ], q[3], v1[3];
+    double q[3], v1[3];
     for (int c = 0; c < 3; ++c) {
         q[c] = fma(rext[c * 3 + 2], pl[2], fma(rext[c * 3 + 1], pl[1], rext[c * 3] * pl[0])) + pext[c];
         v1[c] = -fma(rot[6 + c], n[2], fma(rot[3 + c], n[1], rot[c] * n[0]));
@@ -123,35 +144,7 @@ __device__ inline void residual_point(int i, const DScan& s, const DMap& m, cons
         J[8 % NJ] = -fma(u[0], pl[1], -u[1] * pl[0]);
         J[9 % NJ] = -v1[0]; J[10 % NJ] = -v1[1]; J[11 % NJ] = -v1[2];
     }
-    int k = 0;
-#pragma unroll
-    for (int a = 0; a < NJ; ++a) {
-        const double ua = J[a] * w;
-#pragma unroll
-        for (int b = a; b < NJ; ++b) { acc[k] = fma(ua, J[b], acc[k]); ++k; }
-    }
-#pragma unroll
-    for (int a = 0; a < NJ; ++a) acc[Red<NJ>::NH + a] = fma(J[a] * w, r, acc[Red<NJ>::NH + a]);
-    acc[Red<NJ>::NH + NJ] += 1.0;
-}
-
-// ---------------------------------------------------------------- reductions
-// Butterfly reduce-scatter of 32 values per lane: after it, lane l holds the
-// warp's sum of value l (31 additions per lane instead of 5 x 32).  The tree
-// order is fixed, so the result is deterministic.
-__device__ inline double warp_reduce_scatter32(double* v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 16, L = 32; o > 0; o >>= 1, L >>= 1) {
-        const bool up = (lane & o) != 0;
-#pragma unroll
-        for (int i = 0; i < L / 2; ++i) {
-            const double send = up ? v[i] : v[i + L / 2];
-            const double keep = up ? v[i + L / 2] : v[i];
-            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-        }
-    }
-    return v[0];
+    return true;
 }
 
 // ---------------------------------------------------------------- filter step
@@ -374,17 +367,31 @@ __global__ void k_update_begin(DFilter* f) {
     }
 }
 
-// func_ (sharedUpdateFunc) over all downsampled points, then -- in the last
-// CTA to finish -- the filter step of this iteration.
+// Dynamic shared memory of k_residual<NJ>: the warps' row tiles, later reused
+// for the block fold and the filter step's scratch.
 template <int NJ>
-__global__ void __launch_bounds__(kIekfThreads) k_residual(DFilter* f, DScan s, DMap m, double eps, int do_step) {
+constexpr size_t residual_smem_bytes() {
+    using R = Red<NJ>;
+    constexpr size_t rows = sizeof(double) * (kIekfThreads / 32) * 32 * R::RW;
+    constexpr size_t fold = sizeof(double) * (kIekfThreads / 32) * 32 * R::VPL;
+    return rows > fold ? rows : fold;
+}
+// ... and of k_residual_fold<NJ>: the stripes, then the filter step's scratch.
+template <int NJ>
+constexpr size_t fold_smem_bytes() {
+    using R = Red<NJ>;
+    constexpr size_t fold = sizeof(double) * (R::STRIPES + 1) * R::NV;
+    return fold > sizeof(IekfSm) ? fold : sizeof(IekfSm);
+}
+
+// func_ (sharedUpdateFunc) over all downsampled points: per block the sums of
+// the upper triangle of H, of b and of the valid count (block partials).
+template <int NJ, int MINB>
+__global__ void __launch_bounds__(kIekfThreads, MINB) k_residual(DFilter* f, DScan s, DMap m, int from_down) {
     using R = Red<NJ>;
     constexpr int kWarps = kIekfThreads / 32;
-    static_assert(sizeof(double) * kWarps * R::NP <= sizeof(IekfSm), "partials fit in the step scratch");
-    __shared__ __align__(16) unsigned char smem_raw[sizeof(IekfSm)];
+    extern __shared__ __align__(16) unsigned char smem_dyn[];
     __shared__ double s_rwl[9], s_pwl[3], s_rot[9], s_rext[9], s_pext[3], s_prr[9], s_ppp[9];
-    __shared__ double sH[144], sb[12];
-    __shared__ int s_last;
     if (f->converged) return;  // written by the previous launch; uniform
     const int n = *s.d_n_down;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -402,38 +409,95 @@ __global__ void __launch_bounds__(kIekfThreads) k_residual(DFilter* f, DScan s, 
         s_ppp[a] = f->P[(a / 3) * 23 + a % 3];
         if (a < 3) s_pext[a] = f->x.pos_ext[a];
     }
-    __syncthreads();
-    double acc[R::NP];
+    // the values this lane accumulates: entry k = lane + 32 v is the product
+    // of row slots oa[v] and ob[v] (H(a, b): J w [a] J[b]; b(a): J w [a] r;
+    // the count: 1 * 1)
+    int oa[R::VPL], ob[R::VPL];
 #pragma unroll
-    for (int k = 0; k < R::NP; ++k) acc[k] = 0.0;
-    for (int i = blockIdx.x * blockDim.x + t; i < n; i += gridDim.x * blockDim.x)
-        residual_point<NJ>(i, s, m, s_rwl, s_pwl, s_rot, s_rext, s_pext, s_prr, s_ppp, acc);
-    // warp -> block -> grid, each in a fixed order
-    double* s_red = reinterpret_cast<double*>(smem_raw);
-#pragma unroll
-    for (int c = 0; c < R::NP / 32; ++c) {
-        const double v = warp_reduce_scatter32(acc + 32 * c);
-        s_red[warp * R::NP + 32 * c + lane] = v;
+    for (int v = 0; v < R::VPL; ++v) {
+        const int k = lane + 32 * v;
+        oa[v] = -1;
+        ob[v] = 0;
+        if (k < R::NH) {
+            int a = 0, rem = k;
+            while (rem >= NJ - a) { rem -= NJ - a; ++a; }
+            oa[v] = NJ + a;
+            ob[v] = a + rem;
+        } else if (k < R::NH + NJ) {
+            oa[v] = NJ + (k - R::NH);
+            ob[v] = 2 * NJ;
+        } else if (k == R::NH + NJ) {
+            oa[v] = ob[v] = 2 * NJ + 1;
+        }
     }
+    double acc[R::VPL];
+#pragma unroll
+    for (int v = 0; v < R::VPL; ++v) acc[v] = 0.0;
+    double* wrows = reinterpret_cast<double*>(smem_dyn) + (size_t)warp * 32 * R::RW;
+    __syncthreads();
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + t;
+        double J[NJ], w = 0.0, r = 0.0;
+        const bool valid = i < n && residual_row<NJ>(i, s, m, from_down, s_rwl, s_pwl, s_rot, s_rext, s_pext, s_prr,
+                                                     s_ppp, J, w, r);
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            double* row = wrows + __popc(vm & ((1u << lane) - 1u)) * R::RW;
+#pragma unroll
+            for (int a = 0; a < NJ; ++a) {
+                row[a] = J[a];
+                row[NJ + a] = J[a] * w;
+            }
+            row[2 * NJ] = r;
+            row[2 * NJ + 1] = 1.0;
+        }
+        __syncwarp();
+        const int cnt = __popc(vm);
+        for (int j = 0; j < cnt; ++j) {
+            const double* row = wrows + j * R::RW;
+#pragma unroll
+            for (int v = 0; v < R::VPL; ++v)
+                if (oa[v] >= 0) acc[v] = fma(row[oa[v]], row[ob[v]], acc[v]);
+        }
+        __syncwarp();
+    }
+    // warps -> block, in warp order
+    __syncthreads();
+    double* s_red = reinterpret_cast<double*>(smem_dyn);
+#pragma unroll
+    for (int v = 0; v < R::VPL; ++v) s_red[(warp * R::VPL + v) * 32 + lane] = acc[v];
     __syncthreads();
     for (int k = t; k < R::NV; k += blockDim.x) {
-        double v = s_red[k];
-        for (int w = 1; w < kWarps; ++w) v = v + s_red[w * R::NP + k];
-        s.partials[blockIdx.x * kPartStride2 + k] = v;
+        const int v = k >> 5, l = k & 31;
+        double x = s_red[v * 32 + l];
+        for (int w2 = 1; w2 < kWarps; ++w2) x = x + s_red[(w2 * R::VPL + v) * 32 + l];
+        s.partials[blockIdx.x * kPartStride2 + k] = x;
     }
-    __threadfence();
-    __syncthreads();
-    if (t == 0) {
-        const unsigned int ticket = atomicAdd(s.done_ctr, 1u);
-        s_last = (ticket == gridDim.x - 1) ? 1 : 0;
+}
+
+// The grid's block partials folded in a fixed order -- thread (stripe q,
+// value k) adds blocks q, q + STRIPES, ... in order, then the stripes are
+// added in order -- and the filter step of this iteration.  One CTA.
+template <int NJ>
+__global__ void __launch_bounds__(kIekfThreads) k_residual_fold(DFilter* f, DScan s, int G, double eps, int do_step) {
+    using R = Red<NJ>;
+    extern __shared__ __align__(16) unsigned char smem_dyn[];
+    __shared__ double sH[144], sb[12];
+    if (f->converged) return;  // uniform
+    const int t = threadIdx.x;
+    double* s_red = reinterpret_cast<double*>(smem_dyn);
+    if (t < R::STRIPES * R::NV) {
+        const int q = t / R::NV, k = t - q * R::NV;
+        double x = 0.0;
+        for (int b = q; b < G; b += R::STRIPES) x = x + s.partials[b * kPartStride2 + k];
+        s_red[q * R::NV + k] = x;
     }
     __syncthreads();
-    if (!s_last) return;
-    __threadfence();
+    double* s_sum = s_red + R::STRIPES * R::NV;
     for (int k = t; k < R::NV; k += blockDim.x) {
-        double v = __ldcg(s.partials + k);
-        for (int b = 1; b < (int)gridDim.x; ++b) v = v + __ldcg(s.partials + b * kPartStride2 + k);
-        s_red[k] = v;
+        double x = s_red[k];
+        for (int q = 1; q < R::STRIPES; ++q) x = x + s_red[q * R::NV + k];
+        s_sum[k] = x;
     }
     __syncthreads();
     for (int e = t; e < 144; e += blockDim.x) {
@@ -441,23 +505,22 @@ __global__ void __launch_bounds__(kIekfThreads) k_residual(DFilter* f, DScan s, 
         double v = 0.0;
         if (r < NJ && c < NJ) {
             const int a = r < c ? r : c, b = r < c ? c : r;
-            v = s_red[a * NJ - a * (a - 1) / 2 + (b - a)];
+            v = s_sum[a * NJ - a * (a - 1) / 2 + (b - a)];
         }
         sH[e] = v;
         f->Hm[e] = v;
     }
     if (t < 12) {
-        sb[t] = t < NJ ? s_red[R::NH + t] : 0.0;
+        sb[t] = t < NJ ? s_sum[R::NH + t] : 0.0;
         f->bm[t] = sb[t];
     }
     if (t == 0) {
-        const int eff = (int)s_red[R::NH + NJ];
+        const int eff = (int)s_sum[R::NH + NJ];
         f->effect_num = eff;
         if (eff < 1) f->no_effect = 1;
-        *s.done_ctr = 0;
     }
     __syncthreads();
-    if (do_step) iekf_step(f, *reinterpret_cast<IekfSm*>(smem_raw), sH, sb, NJ, eps);
+    if (do_step) iekf_step(f, *reinterpret_cast<IekfSm*>(smem_dyn), sH, sb, NJ, eps);
 }
 
 // P = L H^-1 L^T (ieskf.cpp:149-155) with H^-1 = M - K Hm (E^T M) of the last
@@ -504,19 +567,53 @@ void launch_update_begin(DFilter* f, cudaStream_t st) {
     VMP_NOTE_LAUNCH();
     k_update_begin<<<1, 64, 0, st>>>(f);
 }
+// Resident CTAs per SM that k_residual is compiled for (register budget):
+// 3 (no spills) or 4 (64 registers); VMP_RESIDUAL_CTAS_PER_SM selects, the
+// arithmetic is the same either way.
+static int g_residual_minb = 3;
+
+template <int NJ, int MINB>
+static cudaError_t set_residual_smem() {
+    return cudaFuncSetAttribute(k_residual<NJ, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)residual_smem_bytes<NJ>());
+}
+cudaError_t residual_setup() {
+    if (const char* v = std::getenv("VMP_RESIDUAL_CTAS_PER_SM")) g_residual_minb = std::atoi(v) == 4 ? 4 : 3;
+    cudaError_t e = set_residual_smem<6, 3>();
+    if (e == cudaSuccess) e = set_residual_smem<6, 4>();
+    if (e == cudaSuccess) e = set_residual_smem<12, 3>();
+    if (e == cudaSuccess) e = set_residual_smem<12, 4>();
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_residual_fold<6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fold_smem_bytes<6>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_residual_fold<12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fold_smem_bytes<12>());
+    return e;
+}
+template <int NJ>
+static void launch_residual_nj(DFilter* f, DScan& s, const DMap& m, int grid, double eps, cudaStream_t st,
+                               int do_step, int from_down) {
+    VMP_NOTE_LAUNCH();
+    if (g_residual_minb == 4)
+        k_residual<NJ, 4><<<grid, kIekfThreads, residual_smem_bytes<NJ>(), st>>>(f, s, m, from_down);
+    else
+        k_residual<NJ, 3><<<grid, kIekfThreads, residual_smem_bytes<NJ>(), st>>>(f, s, m, from_down);
+    VMP_NOTE_LAUNCH();
+    k_residual_fold<NJ><<<1, kIekfThreads, fold_smem_bytes<NJ>(), st>>>(f, s, grid, eps, do_step);
+}
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
-                          cudaStream_t st, int do_step) {
-    // about two points per thread for the largest scans, fewer CTAs for small
-    // ones (n_max bounds the downsampled count); the fold and the reduction
-    // order follow the grid, which depends only on n_max
-    int grid = (n_max + 2 * kIekfThreads - 1) / (2 * kIekfThreads);
+                          cudaStream_t st, int do_step, int from_down) {
+    // one point per thread and tile; the fold and the reduction order follow
+    // the grid, which depends only on n_max (the bound of the downsampled
+    // count)
+    int grid = (n_max + kIekfThreads - 1) / kIekfThreads;
     if (grid > s.res_blocks) grid = s.res_blocks;
     if (grid < 1) grid = 1;
-    VMP_NOTE_LAUNCH();
     if (estimate_ext)
-        k_residual<12><<<grid, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
+        launch_residual_nj<12>(f, s, m, grid, eps, st, do_step, from_down);
     else
-        k_residual<6><<<grid, kIekfThreads, 0, st>>>(f, s, m, eps, do_step);
+        launch_residual_nj<6>(f, s, m, grid, eps, st, do_step, from_down);
 }
 void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st) {
     VMP_NOTE_LAUNCH();

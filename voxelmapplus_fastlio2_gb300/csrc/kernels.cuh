@@ -71,8 +71,11 @@ void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st);
 void launch_predict_chain2(DFilter* f, DScan& s, cudaStream_t st);
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st);
 void launch_update_begin(DFilter* f, cudaStream_t st);
+// k_residual's shared-memory limit (once per process and device, before any capture).
+cudaError_t residual_setup();
+// from_down: LiDAR points from the downsampled cloud (s.down), else from s.pl.
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
-                          cudaStream_t st, int do_step = 1);
+                          cudaStream_t st, int do_step, int from_down);
 void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st);
 
 // ---- k_points.cu

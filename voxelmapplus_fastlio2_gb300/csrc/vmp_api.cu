@@ -572,6 +572,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
             return e == cudaErrorMemoryAllocation ? VMP_ERR_OUT_OF_MEMORY : VMP_ERR_CUDA; \
         }                                        \
     } while (0)
+    CREATE_TRY(residual_setup());
     CREATE_TRY(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
     CREATE_TRY(cudaEventCreateWithFlags(&s->done_ev, cudaEventBlockingSync | cudaEventDisableTiming));
     CREATE_TRY(cudaStreamCreateWithFlags(&s->st_side, cudaStreamNonBlocking));
@@ -604,7 +605,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     DScan& sc = s->s;
     sc.max_pts = max_pts;
     sc.max_imu = max_imu;
-    sc.res_blocks = 2 * 152;
+    sc.res_blocks = 4 * 152;
     CREATE_TRY(dalloc(s, &sc.raw, max_pts));
     CREATE_TRY(dalloc(s, &sc.cloud, max_pts));
     CREATE_TRY(dalloc(s, &sc.raw_int, max_pts));
@@ -959,7 +960,7 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     s->pend(VMP_PROF_UPDATE_OTHER, -1);
     for (int it = 0; it < cfg.ieskf_max_iter; ++it) {
         s->pbeg();
-        launch_residual_iter(s->f, s->s, s->m, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+        launch_residual_iter(s->f, s->s, s->m, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1, 1);
         s->pend(VMP_PROF_RESIDUAL, 1);
     }
     s->pbeg();
@@ -1553,7 +1554,7 @@ vmp_status vmp_ieskf_update(vmp_stream_t s, const float* pts_l, int n, int* iter
     launch_body_cov(s->s, n, s->cfg.ranging_cov, s->sin_deg, s->st);
     launch_update_begin(s->f, s->st);
     for (int it = 0; it < s->cfg.ieskf_max_iter; ++it)
-        launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 1);
+        launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 1, 1);
     launch_update_end(s->f, s->cfg.estimate_ext, s->st);
     vmp_status v = finish_result(s, n, nullptr);
     if (v != VMP_OK) return v;
@@ -1574,7 +1575,7 @@ vmp_status vmp_residual_reduce(vmp_stream_t s, const vmp_state* x, const double*
     if (v != VMP_OK) return v;
     VMP_NOTE_LAUNCH(); k_set_int<<<1, 32, 0, s->st>>>(s->s.d_n_down, n);
     VMP_NOTE_LAUNCH(); k_reset_filter_iter<<<1, 32, 0, s->st>>>(s->f);
-    launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 0);
+    launch_residual_iter(s->f, s->s, s->m, n, s->cfg.estimate_ext, s->cfg.ieskf_eps, s->st, 0, 0);
     double* d_h = s->s.bcov;  // scratch
     int* d_e = reinterpret_cast<int*>(s->s.bcov + 160);
     VMP_NOTE_LAUNCH(); k_read_hm<<<1, 256, 0, s->st>>>(s->f, d_h, d_h + 144, d_e);
