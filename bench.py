@@ -73,7 +73,7 @@ ALGO_BYTES = {
     "downsample": (32.0, "raw point"),                            # K-DS (+16 B per output point, not counted)
 }
 PROF_NAMES = ["upload", "time_sort", "predict", "undistort", "downsample", "body_cov", "residual", "residual_idle",
-              "update_other", "map_batch", "map_group", "map_state", "map_finish", "result"]
+              "update_other", "map_batch", "map_group", "map_state", "map_finish", "result", "residual_step"]
 
 
 def parse():
@@ -302,11 +302,20 @@ def run_value(args, pkgs, cfg, n_init, barrier):
     launches = g.lib.vmp_launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     g.lib.vmp_profile_enable(g.h, 1)
+    m_calls, m_rounds, m_phase = [], [], []
     for i in range(W + K, W + K + P):
         d_pts, d_imu, p = dev[i]
         with torch.cuda.stream(stream):
             flush.fill_(i & 255)
         g.process_device(d_pts.data_ptr(), p.n, p.t_start, p.t_end, d_imu.data_ptr(), p.n_imu)
+        # merge statistics of the scan (these reads wait for the stream; the
+        # profiled scans are not timed)
+        m_calls.append(g.lib.vmp_last_merge_calls(g.h))
+        m_rounds.append(g.lib.vmp_last_merge_rounds(g.h))
+        mp = (C.c_double * 64)()
+        nmp = g.lib.vmp_last_merge_profile(g.h, mp, 64)
+        if nmp > 2:
+            m_phase.append([float(mp[k]) for k in range(nmp)])
     torch.cuda.synchronize()
     ms = (C.c_double * 16)()
     nl = (C.c_longlong * 16)()
@@ -316,9 +325,28 @@ def run_value(args, pkgs, cfg, n_init, barrier):
     g.lib.vmp_profile_enable(g.h, 0)
     out = {"step_ms": step_ms, "wall_s": t_wall, "launches": launches, "clocks": clk, "prof": prof,
            "prof_steps": max(P, 1), "n_raw": float(np.mean(n_raw)), "n_down": float(np.mean(n_down)),
-           "map_size": int(res.map_size), "iters_last": int(res.iters)}
+           "map_size": int(res.map_size), "iters_last": int(res.iters),
+           "merge": {"calls_per_scan": float(np.mean(m_calls)) if m_calls else 0.0,
+                     "rounds_per_scan": float(np.mean(m_rounds)) if m_rounds else 0.0,
+                     "rounds_max": int(max(m_rounds)) if m_rounds else 0,
+                     "fixpoint_us": _merge_phases(m_phase)}}
     g.close()
     return out
+
+
+def _merge_phases(runs):
+    """Mean phase times (us) of the merge fixed point over the profiled
+    scans: setup, the call tests and the merging calls of each round (over
+    the scans that ran that round), and CTA 0's write-back."""
+    if not runs:
+        return None
+    rounds = []
+    for k in range(max((len(r) - 2) // 2 for r in runs)):
+        rs = [r for r in runs if len(r) - 2 >= 2 * (k + 1)]
+        rounds.append({"tests": round(float(np.mean([r[1 + 2 * k] for r in rs])), 2),
+                       "merges": round(float(np.mean([r[2 + 2 * k] for r in rs])), 2), "scans": len(rs)})
+    return {"setup": float(np.mean([r[0] for r in runs])), "rounds": rounds,
+            "write_back": float(np.mean([r[-1] for r in runs])), "total": float(np.mean([sum(r) for r in runs]))}
 
 
 def run_e2e(args, pkgs, cfg, n_init, barrier):
@@ -1240,6 +1268,8 @@ def main():
     prof = val["prof"]
     line["roofline"] = roofline_of(prof)
     line["profile_ms_per_step"] = {k: v["ms"] / val["prof_steps"] for k, v in prof.items()}
+    line["merge"] = dict(val["merge"], map_finish_ms_per_scan=prof["map_finish"]["ms"] / val["prof_steps"],
+                         note="map_finish = the merge fixed point (one cooperative launch) + LRU queue + finalize")
     line["clocks"] = val["clocks"]
     line["gpu_launches"] = val["launches"]
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

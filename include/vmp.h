@@ -426,14 +426,15 @@ enum {
     VMP_PROF_UNDISTORT = 3,     /* per-point motion compensation */
     VMP_PROF_DOWNSAMPLE = 4,    /* leaf-centroid downsample */
     VMP_PROF_BODY_COV = 5,      /* calcBodyCov per downsampled point */
-    VMP_PROF_RESIDUAL = 6,      /* residual + reduction + IEKF step launches that ran an iteration */
-    VMP_PROF_RESIDUAL_IDLE = 7, /* residual launches after convergence (return at once) */
+    VMP_PROF_RESIDUAL = 6,      /* residual + H/b block reduction launches that ran an iteration */
+    VMP_PROF_RESIDUAL_IDLE = 7, /* residual and step launches after convergence (return at once) */
     VMP_PROF_UPDATE_OTHER = 8,  /* P^-1 before, covariance update after the iterations */
     VMP_PROF_MAP_BATCH = 9,     /* float world transform + point covariances */
     VMP_PROF_MAP_GROUP = 10,    /* keys, hash insert, creation order, sort into voxel segments */
     VMP_PROF_MAP_STATE = 11,    /* per-voxel pushPoint state machine + plane refits */
     VMP_PROF_MAP_FINISH = 12,   /* merges, LRU queue, evictions */
     VMP_PROF_RESULT = 13,       /* result gather + device->host copy */
+    VMP_PROF_RESIDUAL_STEP = 14, /* fold of the block partials + IEKF step of an iteration (one CTA) */
     VMP_PROF_SLOTS = 16
 };
 /* Enables (1) or disables (0) the profiler; either resets the totals. */
@@ -453,6 +454,13 @@ long long vmp_launch_count(void);
  * produced the result). */
 vmp_status vmp_set_merge_mode(vmp_stream_t s, int mode);
 int vmp_last_merge_rounds(vmp_stream_t s);
+/* merge() calls of the last map batch (the points that reached a frozen
+ * plane voxel, voxel_map.cpp:70-73); waits for the stream. */
+int vmp_last_merge_calls(vmp_stream_t s);
+/* Phase times (us) of the last batch's merge fixed point: setup, then per
+ * round the call tests and the merging calls, then the write-back; returns
+ * how many were written (0: no fixed point ran).  Waits for the stream. */
+int vmp_last_merge_profile(vmp_stream_t s, double* us, int max);
 /* Test hooks: valid flags of the persistent residual records; the clouds of
  * the last scan (kind 0 undistorted time-sorted cloud, 1 downsampled). */
 vmp_status vmp_residual_valid(vmp_stream_t s, unsigned char* valid, int n);
@@ -487,7 +495,8 @@ vmp_status vmp_set_wait_mode(vmp_stream_t s, int blocking);
  * A server owns its streams (each a vmp_stream_t with its own map, filter
  * and CUDA stream).  vmp_server_open_stream admits a stream while the sum of
  * the admitted streams' device memory stays within the HBM budget and a slot
- * is free, else returns VMP_ERR_ADMISSION_DENIED.  vmp_submit copies a
+ * is free, else returns VMP_ERR_ADMISSION_DENIED; vmp_server_open_stream_wait
+ * waits instead, admitting the stream as slots and memory free up.  vmp_submit copies a
  * package and returns at once.  Worker threads run each stream's packages in
  * submission order and many streams at once, each on its own CUDA stream,
  * so their kernels overlap on the GPU; a package submitted while others run
@@ -520,15 +529,41 @@ typedef struct vmp_server_result {
 } vmp_server_result;
 
 void vmp_server_config_default(vmp_server_config* c);
-/* The autotuner's state: the merge grid divisor in use, the windows of 128
- * completed packages measured so far and the best rate seen (packages/s).
- * The divisor changes only the launch shape of a deterministic fixed point:
- * results are the same under every setting. */
+/* The autotuner (config.autotune, servers with more than one worker): a
+ * coordinate hill climb over launch shapes on windows of 128 completed
+ * packages -- merge_grid_divisor (served merge launches use SMs / d CTAs,
+ * d in 4..64) and residual_ctas_per_sm (the residual kernel's register
+ * budget, 3 or 4 resident CTAs per SM; scan graphs are captured again after
+ * a change).  Both are process-wide and change launch shapes only: results
+ * are the same under every setting.  vmp_server_tuning: the merge divisor in
+ * use, the windows measured so far and the best rate seen (packages/s);
+ * vmp_server_knob: a knob's value by name. */
 vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long* windows, double* best_rate);
+vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value);
+/* Sets residual_ctas_per_sm by hand (3 or 4; process-wide, what the
+ * autotuner does; VMP_RESIDUAL_CTAS_PER_SM gives the value at load). */
+vmp_status vmp_set_residual_ctas_per_sm(int ctas);
+/* Test hook: the autotuner's climb on a model instead of a GPU (no CUDA
+ * call).  rates[i * 2 + j]: packages/s with merge divisor candidate i
+ * (4, 8, 16, 32, 64) and residual CTAs per SM candidate j (3, 4); trace
+ * (2 x windows ints): both knobs after each window. */
+vmp_status vmp_test_autotune(int merge_divisor, int residual_ctas, const double* rates, int windows, int* trace);
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out);
-/* Waits for the packages that are running; queued ones are dropped. */
+/* Waits for the packages that are running; queued ones are dropped;
+ * admission requests still waiting return VMP_ERR_STATE. */
 vmp_status vmp_server_destroy(vmp_server_t sv);
+/* Admits a stream now or answers VMP_ERR_ADMISSION_DENIED (no free slot, or
+ * its device memory would take the open streams past the HBM budget). */
 vmp_status vmp_server_open_stream(vmp_server_t sv, const vmp_config* cfg, int* stream_id);
+/* The same, waiting: the request queues behind earlier ones (arrival order)
+ * until a slot is free and the stream fits the budget beside the open
+ * streams -- both free up as vmp_server_close_stream retires streams, while
+ * the other streams keep running -- or until timeout_ms passes
+ * (VMP_ERR_TIMEOUT; timeout_ms < 0: no limit, 0: as vmp_server_open_stream).
+ * A stream larger than the whole budget is denied at once.  The footprint of
+ * a configuration is measured by creating the stream once; a creation that
+ * runs out of device memory is retried after the next close. */
+vmp_status vmp_server_open_stream_wait(vmp_server_t sv, const vmp_config* cfg, int timeout_ms, int* stream_id);
 /* Waits until the stream's queued packages are done, then frees it. */
 vmp_status vmp_server_close_stream(vmp_server_t sv, int stream_id);
 vmp_status vmp_submit(vmp_server_t sv, int stream_id, const vmp_scan* scan, const vmp_imu* imus, int n_imu,

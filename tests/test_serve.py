@@ -3,7 +3,8 @@
 The reference has no serving layer; these tests pin the server's contract:
 each stream's results are bit-identical alone and in the mix (their work
 overlaps on the device), per-stream order is kept, admission follows the HBM
-budget, and a closed stream frees its budget.
+budget (at once, or waiting for slots and memory to free up), and a closed
+stream frees its budget.
 """
 import ctypes as C
 
@@ -113,6 +114,107 @@ def test_admission_by_budget_and_release():
         srv.close()
 
 
+def _alone(kind, pkgs):
+    """A stream's per-package results on a stream of its own."""
+    from voxelmapplus_fastlio2_gb300 import lio
+    g = lio.LIOBuilder(_cfg(kind))
+    out = [_key(g.process(p)) for p in pkgs]
+    g.close()
+    return out
+
+
+def test_admission_waits_for_budget_while_streams_run():
+    """vmp_server_open_stream_wait: with the budget full and packages of the
+    open streams in flight, a request waits (the other streams keep
+    running), is admitted as soon as a stream closes, and its stream then
+    runs; every stream's results equal its results alone.  A request that
+    never fits is denied at once; one that outlasts its time limit times out."""
+    import threading
+    import time
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    from voxelmapplus_fastlio2_gb300._lib import VmpError
+    kinds = [synth.KIND_ROOM, synth.KIND_ROOM, synth.KIND_ROOM]
+    pk = [_packages(k, 0x5EED0000 + 400 + i, [6000, 9000, 7000][i], 10) for i, k in enumerate(kinds)]
+    ref = [_alone(k, p) for k, p in zip(kinds, pk)]
+    srv = Server(hbm_budget_bytes=150e9, max_streams=4, workers=2)
+    try:
+        srv.open_stream(_cfg(synth.KIND_ROOM))
+        one = srv.info()["budget_used"]
+    finally:
+        srv.close()
+    srv = Server(hbm_budget_bytes=int(2.5 * one), max_streams=4, workers=2)
+    try:
+        a = srv.open_stream(_cfg(kinds[0]))
+        b = srv.open_stream(_cfg(kinds[1]))
+        for k in range(10):
+            srv.submit(a, pk[0][k], cookie=k)
+            srv.submit(b, pk[1][k], cookie=k)
+        got = {}
+        waiter = {}
+
+        def wait_open():
+            try:
+                waiter["sid"] = srv.open_stream_wait(_cfg(kinds[2]), timeout_ms=120000)
+            except VmpError as e:
+                waiter["err"] = e.code
+
+        th = threading.Thread(target=wait_open)
+        th.start()
+        time.sleep(0.3)
+        assert th.is_alive() and srv.info()["streams_open"] == 2  # waiting while a and b run
+        srv.close_stream(a)  # waits for a's packages, frees its budget
+        th.join(timeout=60)
+        assert not th.is_alive() and "sid" in waiter, waiter
+        c = waiter["sid"]
+        for k in range(10):
+            srv.submit(c, pk[2][k], cookie=k)
+        while sum(len(v) for v in got.values()) < 30:
+            for r in srv.poll(timeout_ms=1000):
+                assert r.status == abi.VMP_OK, r.status
+                got.setdefault(r.stream_id, []).append((r.cookie, _key(r.result)))
+        for sid, i in ((a, 0), (b, 1), (c, 2)):
+            seq = sorted(got[sid])
+            assert [x for x, _ in seq] == list(range(10))
+            assert [k for _, k in seq] == ref[i], f"stream {i} differs from its results alone"
+        # budget full again (b and c open): a request with a short limit times out
+        with pytest.raises(VmpError) as e:
+            srv.open_stream_wait(_cfg(synth.KIND_ROOM), timeout_ms=200)
+        assert e.value.code == abi.VMP_ERR_TIMEOUT
+        assert srv.info()["streams_open"] == 2
+    finally:
+        srv.close()
+    srv = Server(hbm_budget_bytes=int(0.5 * one), max_streams=4, workers=2)
+    try:
+        with pytest.raises(VmpError) as e:
+            srv.open_stream_wait(_cfg(synth.KIND_ROOM), timeout_ms=-1)  # larger than the whole budget
+        assert e.value.code == abi.VMP_ERR_ADMISSION_DENIED
+    finally:
+        srv.close()
+
+
+def test_residual_register_budget_does_not_change_results():
+    """The autotuner's second knob: the residual kernel compiled for 3 or 4
+    resident CTAs per SM, switched between scans (the scan graphs are
+    captured again): the same results as with either setting throughout."""
+    from voxelmapplus_fastlio2_gb300 import lio
+    kind = synth.KIND_URBAN
+    pk = _packages(kind, 0x5EED0000 + 500, 30000, 10)
+    lib = lio.load()
+    runs = []
+    try:
+        for sched in ([3] * 10, [4] * 10, [3, 3, 3, 4, 4, 3, 4, 3, 4, 4]):
+            g = lio.LIOBuilder(_cfg(kind))
+            res = []
+            for c, p in zip(sched, pk):
+                assert lib.vmp_set_residual_ctas_per_sm(c) == 0
+                res.append(_key(g.process(p)))
+            runs.append(res)
+            g.close()
+    finally:
+        lib.vmp_set_residual_ctas_per_sm(3)
+    assert runs[1] == runs[0] and runs[2] == runs[0]
+
+
 def test_merge_launch_shape_does_not_change_results():
     """The served merge resolution runs on grids of SMs / divisor CTAs (the
     autotuner's knob): every divisor gives the same results and maps."""
@@ -133,6 +235,7 @@ def test_autotuner_reports_state():
     try:
         t = srv.tuning()
         assert t["merge_grid_divisor"] in (4, 8, 16, 32, 64) and t["windows"] == 0
+        assert t["residual_ctas_per_sm"] in (3, 4)
     finally:
         srv.close()
 

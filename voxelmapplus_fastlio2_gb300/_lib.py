@@ -57,6 +57,8 @@ def _declare(lib):
         "vmp_launch_count": ([], C.c_longlong),
         "vmp_io_bytes": ([vp, P(C.c_longlong), P(C.c_longlong)], st),
         "vmp_last_merge_rounds": ([vp], C.c_int),
+        "vmp_last_merge_calls": ([vp], C.c_int),
+        "vmp_last_merge_profile": ([vp, P(d), C.c_int], C.c_int),
         "vmp_device_bytes": ([vp], C.c_longlong),
         "vmp_eviction_splits": ([vp], C.c_longlong),
         "vmp_set_wait_mode": ([vp, C.c_int], st),
@@ -65,6 +67,7 @@ def _declare(lib):
         "vmp_server_create": ([P(abi.vmp_server_config), P(vp)], st),
         "vmp_server_destroy": ([vp], st),
         "vmp_server_open_stream": ([vp, P(abi.vmp_config), P(C.c_int)], st),
+        "vmp_server_open_stream_wait": ([vp, P(abi.vmp_config), C.c_int, P(C.c_int)], st),
         "vmp_server_close_stream": ([vp, C.c_int], st),
         "vmp_submit": ([vp, C.c_int, P(abi.vmp_scan), P(abi.vmp_imu), C.c_int, C.c_longlong], st),
         "vmp_submit_device": ([vp, C.c_int, vp, C.c_int, d, d, vp, C.c_int, C.c_longlong], st),
@@ -74,6 +77,9 @@ def _declare(lib):
         "vmp_server_info": ([vp, P(C.c_longlong), P(C.c_int), P(C.c_int), P(C.c_int)], st),
         "vmp_server_last_error": ([vp], C.c_char_p),
         "vmp_server_tuning": ([vp, P(C.c_int), P(C.c_longlong), P(d)], st),
+        "vmp_server_knob": ([vp, C.c_char_p, P(C.c_int)], st),
+        "vmp_set_residual_ctas_per_sm": ([C.c_int], st),
+        "vmp_test_autotune": ([C.c_int, C.c_int, vp, C.c_int, vp], st),
         "vmp_fit_planes": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp], st),
         "vmp_fit_planes_device": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp, vp], st),
         "vmp_fit_profile": ([C.c_int], st),

@@ -32,6 +32,7 @@
 // Gauss-Jordan solve and products with block-diagonal matrices, all spread
 // over the lanes, with the transcendental functions of the boxminus / boxplus
 // on separate lanes.
+#include <atomic>
 #include <cstdlib>
 
 #include "kernels.cuh"
@@ -568,9 +569,19 @@ void launch_update_begin(DFilter* f, cudaStream_t st) {
     k_update_begin<<<1, 64, 0, st>>>(f);
 }
 // Resident CTAs per SM that k_residual is compiled for (register budget):
-// 3 (no spills) or 4 (64 registers); VMP_RESIDUAL_CTAS_PER_SM selects, the
-// arithmetic is the same either way.
-static int g_residual_minb = 3;
+// 3 (no spills) or 4 (64 registers); the arithmetic is the same either way.
+// The serving autotuner sets it (VMP_RESIDUAL_CTAS_PER_SM gives the start);
+// a change bumps the launch-shape epoch, so that captured scan graphs are
+// captured again with the new kernel.
+static std::atomic<int> g_residual_minb{3};
+static std::atomic<long long> g_shape_epoch{0};
+
+void residual_set_ctas_per_sm(int c) {
+    const int v = c == 4 ? 4 : 3;
+    if (g_residual_minb.exchange(v) != v) g_shape_epoch.fetch_add(1);
+}
+int residual_ctas_per_sm() { return g_residual_minb.load(); }
+long long launch_shape_epoch() { return g_shape_epoch.load(); }
 
 template <int NJ, int MINB>
 static cudaError_t set_residual_smem() {
@@ -578,7 +589,11 @@ static cudaError_t set_residual_smem() {
                                 (int)residual_smem_bytes<NJ>());
 }
 cudaError_t residual_setup() {
-    if (const char* v = std::getenv("VMP_RESIDUAL_CTAS_PER_SM")) g_residual_minb = std::atoi(v) == 4 ? 4 : 3;
+    static const bool from_env = [] {
+        if (const char* v = std::getenv("VMP_RESIDUAL_CTAS_PER_SM")) g_residual_minb = std::atoi(v) == 4 ? 4 : 3;
+        return true;
+    }();
+    (void)from_env;
     cudaError_t e = set_residual_smem<6, 3>();
     if (e == cudaSuccess) e = set_residual_smem<6, 4>();
     if (e == cudaSuccess) e = set_residual_smem<12, 3>();
@@ -591,29 +606,42 @@ cudaError_t residual_setup() {
                                  (int)fold_smem_bytes<12>());
     return e;
 }
-template <int NJ>
-static void launch_residual_nj(DFilter* f, DScan& s, const DMap& m, int grid, double eps, cudaStream_t st,
-                               int do_step, int from_down) {
+// one point per thread and tile; the fold and the reduction order follow the
+// grid, which depends only on n_max (the bound of the downsampled count)
+static int residual_grid(const DScan& s, int n_max) {
+    int grid = (n_max + kIekfThreads - 1) / kIekfThreads;
+    if (grid > s.res_blocks) grid = s.res_blocks;
+    return grid < 1 ? 1 : grid;
+}
+void launch_residual_points(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, cudaStream_t st,
+                            int from_down) {
+    const int grid = residual_grid(s, n_max);
     VMP_NOTE_LAUNCH();
-    if (g_residual_minb == 4)
-        k_residual<NJ, 4><<<grid, kIekfThreads, residual_smem_bytes<NJ>(), st>>>(f, s, m, from_down);
+    if (estimate_ext) {
+        if (g_residual_minb == 4)
+            k_residual<12, 4><<<grid, kIekfThreads, residual_smem_bytes<12>(), st>>>(f, s, m, from_down);
+        else
+            k_residual<12, 3><<<grid, kIekfThreads, residual_smem_bytes<12>(), st>>>(f, s, m, from_down);
+    } else {
+        if (g_residual_minb == 4)
+            k_residual<6, 4><<<grid, kIekfThreads, residual_smem_bytes<6>(), st>>>(f, s, m, from_down);
+        else
+            k_residual<6, 3><<<grid, kIekfThreads, residual_smem_bytes<6>(), st>>>(f, s, m, from_down);
+    }
+}
+void launch_residual_step(DFilter* f, DScan& s, int n_max, int estimate_ext, double eps, cudaStream_t st,
+                          int do_step) {
+    const int grid = residual_grid(s, n_max);
+    VMP_NOTE_LAUNCH();
+    if (estimate_ext)
+        k_residual_fold<12><<<1, kIekfThreads, fold_smem_bytes<12>(), st>>>(f, s, grid, eps, do_step);
     else
-        k_residual<NJ, 3><<<grid, kIekfThreads, residual_smem_bytes<NJ>(), st>>>(f, s, m, from_down);
-    VMP_NOTE_LAUNCH();
-    k_residual_fold<NJ><<<1, kIekfThreads, fold_smem_bytes<NJ>(), st>>>(f, s, grid, eps, do_step);
+        k_residual_fold<6><<<1, kIekfThreads, fold_smem_bytes<6>(), st>>>(f, s, grid, eps, do_step);
 }
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step, int from_down) {
-    // one point per thread and tile; the fold and the reduction order follow
-    // the grid, which depends only on n_max (the bound of the downsampled
-    // count)
-    int grid = (n_max + kIekfThreads - 1) / kIekfThreads;
-    if (grid > s.res_blocks) grid = s.res_blocks;
-    if (grid < 1) grid = 1;
-    if (estimate_ext)
-        launch_residual_nj<12>(f, s, m, grid, eps, st, do_step, from_down);
-    else
-        launch_residual_nj<6>(f, s, m, grid, eps, st, do_step, from_down);
+    launch_residual_points(f, s, m, n_max, estimate_ext, st, from_down);
+    launch_residual_step(f, s, n_max, estimate_ext, eps, st, do_step);
 }
 void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st) {
     VMP_NOTE_LAUNCH();

@@ -41,6 +41,7 @@ constexpr int kLogs = 3;  // round r writes log r % 3, reads log (r - 1) % 3, cl
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint64_t kSigNone = 0x1234567ull;
 constexpr long long kBarrierSpinLimit = 20000000;  // x >= 64 ns sleeps: about a second or more
+constexpr int kMaxMarks = 4 + 2 * kMaxRounds;
 
 struct MState {
     double mean[3];
@@ -71,6 +72,10 @@ struct MergeCtl {
     unsigned int bar_count;
     unsigned int bar_gen;
     unsigned int epoch;  // batches resolved so far (tags rec_round)
+    int n_marks;
+    // %globaltimer (ns) at the kernel's start and after each of its grid
+    // barriers (for the per-round profile of the last batch)
+    unsigned long long t_mark[kMaxMarks];
 };
 
 struct MergeScratch {
@@ -424,6 +429,20 @@ __device__ uint64_t warp_merge_call(const DMap& m, MergeScratch& g, uint32_t a_r
     return mix64(sig, (uint64_t)nout);
 }
 
+__device__ inline unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Thread 0 of CTA 0 notes the time (after a grid barrier: all CTAs passed it).
+__device__ inline void mark(MergeCtl* c, int& k) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && k < kMaxMarks) {
+        c->t_mark[k] = global_ns();
+        c->n_marks = k + 1;
+    }
+    ++k;
+}
+
 // All rounds of the fixed point and the final write-back, one cooperative
 // launch.
 __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeScratch g,
@@ -435,6 +454,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31, gw = tid >> 5, nw = nth >> 5;
     const uint64_t noop_sig = mix64(kSigNone, 0);
+    int nm = 0;
+    mark(c, nm);
     // the three logs still hold the previous batch's entries: unlink them
     int old_n[kLogs];
     for (int b = 0; b < kLogs; ++b) old_n[b] = min(c->n_ent[b], g.pool);
@@ -450,6 +471,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
     for (int b = 0; b < kLogs; ++b)
         for (int e = tid; e < old_n[b]; e += nth) g.head[b][g.ent[b][e].rec] = kNone;
     grid_barrier(c);
+    mark(c, nm);
 
     int final_log = -1;
     for (int r = 0; r < kMaxRounds; ++r) {
@@ -497,6 +519,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
             }
         }
         grid_barrier(c);
+        mark(c, nm);
         if (tid == 0) c->n_ent[nxt] = 0;  // its unlinking above is done
         // one warp per call that merges: the whole call, lane-parallel
         const int nq = c->n_queue[r];
@@ -515,6 +538,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
         }
         if (ovf && lane == 0) c->overflow = 1;
         grid_barrier(c);
+        mark(c, nm);
         if (tid == 0) c->rounds = r + 1;
         if (c->wait_error || c->overflow) break;
         if (first && nq == 0) { final_log = cur; break; }  // no call merges anything
@@ -534,6 +558,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
         if (tid == 0) c->converged = 1;
     }
     if (tid == 0 && c->wait_error) set_error(m.cnt, E_MERGE_WAIT);
+    mark(c, nm);  // CTA 0's end of the write-back
 }
 
 cudaError_t merge_scratch_alloc(void** out, int max_batch, int rec_pool) {
@@ -659,6 +684,21 @@ cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, 
     }
     VMP_NOTE_LAUNCH(); k_merge_sequential<<<1, 32, 0, st>>>(m, ms.ev_list, ms.ev_rec, ms.d_n_ev, g.ctl);
     return cudaGetLastError();
+}
+
+// Phase times of the last batch's fixed point (us): setup, then per round
+// the call tests and the merging calls, then CTA 0's write-back; returns how
+// many (0 when no fixed point ran).  Waits for the stream.
+int merge_profile_read(void* scratch, cudaStream_t st, double* us, int max) {
+    MergeScratch& g = *(MergeScratch*)scratch;
+    MergeCtl h;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    if (cudaMemcpy(&h, g.ctl, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    if (!h.converged) return 0;
+    int n = 0;
+    for (int k = 1; k < h.n_marks && k < kMaxMarks && n < max; ++k)
+        us[n++] = (double)(h.t_mark[k] - h.t_mark[k - 1]) * 1e-3;
+    return n;
 }
 
 // Rounds the last batch's fixed point ran (0 when the replay ran alone);

@@ -73,7 +73,19 @@ void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro
 void launch_update_begin(DFilter* f, cudaStream_t st);
 // k_residual's shared-memory limit (once per process and device, before any capture).
 cudaError_t residual_setup();
-// from_down: LiDAR points from the downsampled cloud (s.down), else from s.pl.
+// k_residual's register budget (resident CTAs per SM: 3 or 4; same results).
+void residual_set_ctas_per_sm(int c);
+int residual_ctas_per_sm();
+// Bumped whenever a launch shape that captured graphs hold changes.
+long long launch_shape_epoch();
+// One IEKF iteration: launch_residual_points (sharedUpdateFunc over the points,
+// block partials of H / b) then launch_residual_step (their fold and, with
+// do_step, the filter step).  from_down: LiDAR points from the downsampled
+// cloud (s.down), else from s.pl.
+void launch_residual_points(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, cudaStream_t st,
+                            int from_down);
+void launch_residual_step(DFilter* f, DScan& s, int n_max, int estimate_ext, double eps, cudaStream_t st,
+                          int do_step);
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step, int from_down);
 void launch_update_end(DFilter* f, int estimate_ext, cudaStream_t st);
@@ -165,6 +177,7 @@ void merge_scratch_free(void* p);
 cudaError_t run_merge_events(DMap& m, MapScratch& ms, void* scratch, int n_max, int mode, int* rounds_out,
                              cudaStream_t st);
 int merge_rounds_read(void* scratch, cudaStream_t st);
+int merge_profile_read(void* scratch, cudaStream_t st, double* us, int max);
 // While at least one multi-worker server exists (on: one more, off: one
 // fewer), cooperative merge launches use 1/16 of the SMs and run several at
 // once instead of one at a time on all SMs.

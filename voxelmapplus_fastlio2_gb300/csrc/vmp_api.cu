@@ -354,7 +354,7 @@ struct vmp_stream_s {
     // g1 / g2: the steady scan around the merge resolution; g0: the scan
     // front alone (time sort to map batch), for scans whose map update may
     // evict and therefore runs its map part with host decisions
-    struct ScanGraphs { int nb; cudaGraphExec_t g1, g2, g0; long long k1, k2, k0; };
+    struct ScanGraphs { int nb; cudaGraphExec_t g1, g2, g0; long long k1, k2, k0; long long epoch; };
     std::deque<ScanGraphs> graphs;
     bool use_graphs = true;
     // vmp_map_planes scratch (allocated by its first call)
@@ -414,6 +414,8 @@ struct vmp_stream_s {
             if (slot == VMP_PROF_RESIDUAL) {
                 if (res_seen >= iters) slot = VMP_PROF_RESIDUAL_IDLE;
                 ++res_seen;
+            } else if (slot == VMP_PROF_RESIDUAL_STEP && res_seen > iters) {
+                slot = VMP_PROF_RESIDUAL_IDLE;  // the fold launch after convergence
             }
             prof_ms[slot] += ms;
             prof_launches[slot] += 1;
@@ -960,8 +962,11 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     s->pend(VMP_PROF_UPDATE_OTHER, -1);
     for (int it = 0; it < cfg.ieskf_max_iter; ++it) {
         s->pbeg();
-        launch_residual_iter(s->f, s->s, s->m, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1, 1);
+        launch_residual_points(s->f, s->s, s->m, nb, cfg.estimate_ext, st, 1);
         s->pend(VMP_PROF_RESIDUAL, 1);
+        s->pbeg();
+        launch_residual_step(s->f, s->s, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+        s->pend(VMP_PROF_RESIDUAL_STEP, -1);
     }
     s->pbeg();
     launch_update_end(s->f, cfg.estimate_ext, st);
@@ -972,10 +977,21 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
 }
 
 // The graphs of size class nb (an empty entry on first use).
+// Graphs captured before a launch shape changed (launch_shape_epoch) are
+// dropped and captured again (an exec still running is freed when it ends).
 static vmp_stream_s::ScanGraphs* graphs_for(vmp_stream_t s, int nb) {
+    const long long ep = launch_shape_epoch();
     for (auto& g : s->graphs)
-        if (g.nb == nb) return &g;
-    s->graphs.push_back(vmp_stream_s::ScanGraphs{nb, nullptr, nullptr, nullptr, 0, 0, 0});
+        if (g.nb == nb) {
+            if (g.epoch != ep) {
+                if (g.g1) cudaGraphExecDestroy(g.g1);
+                if (g.g2) cudaGraphExecDestroy(g.g2);
+                if (g.g0) cudaGraphExecDestroy(g.g0);
+                g = vmp_stream_s::ScanGraphs{nb, nullptr, nullptr, nullptr, 0, 0, 0, ep};
+            }
+            return &g;
+        }
+    s->graphs.push_back(vmp_stream_s::ScanGraphs{nb, nullptr, nullptr, nullptr, 0, 0, 0, ep});
     return &s->graphs.back();
 }
 
@@ -1702,5 +1718,24 @@ vmp_status vmp_set_wait_mode(vmp_stream_t s, int blocking) {
     return VMP_OK;
 }
 int vmp_last_merge_rounds(vmp_stream_t s) { return s ? merge_rounds_read(s->ms.merge, s->st) : -1; }
+int vmp_last_merge_profile(vmp_stream_t s, double* us, int max) {
+    if (!s || !us || max <= 0) return -1;
+    return merge_profile_read(s->ms.merge, s->st, us, max);
+}
+vmp_status vmp_set_residual_ctas_per_sm(int ctas) {
+    if (ctas != 3 && ctas != 4) return VMP_ERR_INVALID_ARG;
+    residual_set_ctas_per_sm(ctas);
+    return VMP_OK;
+}
+int vmp_last_merge_calls(vmp_stream_t s) {
+    if (!s) return -1;
+    int n = -1;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess ||
+        cudaMemcpy(&n, s->ms.d_n_ev, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return n;
+}
 
 }  // extern "C"

@@ -10,12 +10,15 @@
 // streams keep the GPU busy, so the kernels of different streams overlap.
 // Admission: a stream is opened while the device memory of the open streams
 // (each stream's footprint is what vmp_create allocated) stays within the
-// HBM budget and a slot is free.
+// HBM budget and a slot is free.  vmp_server_open_stream answers at once;
+// vmp_server_open_stream_wait queues the request (arrival order) until a slot
+// and the budget free up as streams close, or until its time limit.
 #include <chrono>
 #include <condition_variable>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -26,6 +29,8 @@
 namespace vmp {
 void merge_set_throughput_mode(bool on);
 void merge_set_grid_divisor(int d);
+void residual_set_ctas_per_sm(int c);
+int residual_ctas_per_sm();
 }
 
 namespace {
@@ -58,75 +63,136 @@ struct Slot {
 
 }  // namespace
 
-// Online autotuner of the served merge launch shape, a hill climb over the
-// grid divisors kCand: a window of completed packages at the current divisor
-// (the first packages after a switch are not counted), then one at each
-// neighbour; the fastest of the three becomes current.  When the current one
-// wins, it is kept for kExploit windows before its neighbours are measured
-// again (the stream mix may have changed).  It starts at 16 (measured best
-// on 64 mixed streams) and climbs first after kFirst windows, so short runs
-// pay nothing for the exploration.
-struct MergeTuner {
-    static constexpr int kWindow = 128, kSettle = 16, kExploit = 32, kN = 5;
-    static constexpr int kCand[kN] = {4, 8, 16, 32, 64};
-    static constexpr int kFirst = 8;  // windows at the starting divisor before the first climb
-    int idx = 2;             // current candidate
-    int probe = 3;           // 0: current, 1: idx + 1, 2: idx - 1, 3: exploiting
-    int exploit_left = kFirst;
-    int seen = 0;            // packages completed in the window (settling first)
-    double t_begin = 0.0;
-    double rate[3] = {};     // current, upper, lower
-    long long windows = 0;
-    double best = 0.0;
+// One knob of the online autotuner: a hill climb over its candidate values.
+// From the current value (its rate measured), it measures one window at each
+// neighbour; the fastest of the three becomes current, and the climb goes
+// on from a new current until the current one wins ("settled").
+struct KnobClimb {
+    const char* name;
+    std::vector<int> cand;
+    void (*apply)(int);
+    int idx = 0;          // current candidate
+    int probe = 3;        // 1: measuring idx + 1, 2: idx - 1, 3: not climbing
+    double rate[3] = {};  // current, upper, lower
 
     int cur() const {
         const int i = probe == 1 ? idx + 1 : (probe == 2 ? idx - 1 : idx);
-        return kCand[i];
+        return cand[i];
     }
-    // the next probe that has a candidate, from `p` on
     int next_probe(int p) const {
-        if (p == 1 && idx + 1 >= kN) p = 2;
+        if (p == 1 && idx + 1 >= (int)cand.size()) p = 2;
         if (p == 2 && idx - 1 < 0) p = 3;
         return p;
     }
-    // called under the server lock at every completion; returns the divisor
-    // to switch to, or 0
-    int on_done(double now_ms) {
+    // starts a climb from the current value, whose rate is r; false: nothing
+    // to probe
+    bool start(double r) {
+        rate[0] = r;
+        probe = next_probe(1);
+        return probe != 3;
+    }
+    // the rate of the window just measured at cur(); returns true once settled
+    bool feed(double r) {
+        rate[probe] = r;
+        probe = next_probe(probe + 1);
+        if (probe < 3) return false;
+        int pick = 0;
+        if (idx + 1 < (int)cand.size() && rate[1] > rate[pick]) pick = 1;
+        if (idx - 1 >= 0 && rate[2] > rate[pick]) pick = 2;
+        if (pick == 0) return true;
+        idx += pick == 1 ? 1 : -1;
+        rate[0] = rate[pick];
+        probe = next_probe(1);
+        return probe == 3;
+    }
+    void set_nearest(int v) {
+        int bi = 0;
+        for (int i = 1; i < (int)cand.size(); ++i)
+            if (std::abs(cand[i] - v) < std::abs(cand[bi] - v)) bi = i;
+        idx = bi;
+    }
+};
+
+// Online autotuner of the served launch shapes: windows of kWindow completed
+// packages (the first kSettle after a switch are not counted) measure the
+// throughput of the current shapes; the knobs are climbed one after the
+// other (coordinate-wise), then the shapes are kept for kExploit windows
+// before the next round of climbs (the stream mix may have changed).  The
+// first climb starts after kFirst windows, so short runs pay nothing for the
+// exploration.  Every knob changes launch shapes only, never results:
+//   merge_grid_divisor    served merge launches use SMs / d CTAs;
+//   residual_ctas_per_sm  the residual kernel's register budget (3 or 4
+//                         resident CTAs per SM; scan graphs are recaptured).
+struct Autotuner {
+    static constexpr int kWindow = 128, kSettle = 16, kExploit = 32, kFirst = 8;
+    std::vector<KnobClimb> knobs;
+    int active = -1;  // the knob being climbed (-1: exploiting)
+    int exploit_left = kFirst;
+    int seen = 0;
+    double t_begin = 0.0;
+    long long windows = 0;
+    double best = 0.0;
+
+    void apply_all() {
+        for (auto& k : knobs) k.apply(k.cur());
+    }
+    // from knob `from` on, the first one with something to probe (rate r at
+    // the current shapes); none: exploit
+    void climb_from(int from, double r) {
+        for (int k = from; k < (int)knobs.size(); ++k)
+            if (knobs[k].start(r)) {
+                active = k;
+                knobs[k].apply(knobs[k].cur());
+                return;
+            }
+        active = -1;
+        exploit_left = kExploit;
+    }
+    // called at every completion (time in ms); applies the next shapes
+    void on_done(double now_ms) {
         ++seen;
         if (seen == kSettle) t_begin = now_ms;
-        if (seen < kSettle + kWindow) return 0;
+        if (seen < kSettle + kWindow) return;
         const double r = kWindow / ((now_ms - t_begin) * 1e-3);
         seen = 0;
         ++windows;
         if (r > best) best = r;
-        if (probe == 3) {
-            if (--exploit_left > 0) return 0;
-            rate[0] = r;  // the current one, freshly measured
-            probe = next_probe(1);
-            return probe == 3 ? 0 : cur();
+        if (active < 0) {
+            if (--exploit_left > 0) return;
+            climb_from(0, r);
+            return;
         }
-        rate[probe] = r;
-        probe = next_probe(probe + 1);
-        if (probe < 3) return cur();
-        int pick = 0;  // decide among current / upper / lower
-        if (idx + 1 < kN && rate[1] > rate[pick]) pick = 1;
-        if (idx - 1 >= 0 && rate[2] > rate[pick]) pick = 2;
-        if (pick == 0) {
-            exploit_left = kExploit;
-        } else {
-            idx += pick == 1 ? 1 : -1;
-            rate[0] = rate[pick];
-            probe = next_probe(1);
-            if (probe == 3) exploit_left = kExploit;
-        }
-        return cur();
+        KnobClimb& k = knobs[active];
+        const bool settled = k.feed(r);
+        k.apply(k.cur());
+        if (settled) climb_from(active + 1, k.rate[0]);
+    }
+    int value(const char* name) const {
+        for (const auto& k : knobs)
+            if (std::strcmp(k.name, name) == 0) return k.cur();
+        return -1;
     }
 };
-constexpr int MergeTuner::kCand[MergeTuner::kN];
+
+static void apply_merge_divisor(int d) { vmp::merge_set_grid_divisor(d); }
+static void apply_residual_ctas(int c) { vmp::residual_set_ctas_per_sm(c); }
+// the launch shapes of vmp_test_autotune's model (one caller at a time)
+static int g_model_d = 0, g_model_c = 0;
+static void model_set_d(int d) { g_model_d = d; }
+static void model_set_c(int c) { g_model_c = c; }
+
+static Autotuner make_tuner(int merge_divisor, int residual_ctas, void (*set_d)(int), void (*set_c)(int)) {
+    Autotuner t;
+    t.knobs.push_back(KnobClimb{"merge_grid_divisor", {4, 8, 16, 32, 64}, set_d});
+    t.knobs.push_back(KnobClimb{"residual_ctas_per_sm", {3, 4}, set_c});
+    t.knobs[0].set_nearest(merge_divisor);
+    t.knobs[1].set_nearest(residual_ctas);
+    return t;
+}
 
 struct vmp_server_s {
     vmp_server_config cfg{};
-    MergeTuner tuner;
+    Autotuner tuner;
     int fixed_divisor = 16;
     std::mutex mu;
     std::condition_variable cv_work;  // workers: a package is ready / stop
@@ -140,6 +206,27 @@ struct vmp_server_s {
     int queued = 0;
     std::string err;
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    // admission requests in arrival order (tickets); the front one is served
+    std::condition_variable cv_admit;
+    std::deque<unsigned long long> admit_q;
+    unsigned long long admit_ticket = 0;
+    unsigned long long closes = 0;  // streams closed so far (a create that ran out of memory retries after one)
+    // measured device footprint of each stream configuration seen
+    std::vector<std::pair<vmp_config, long long>> footprints;
+
+    long long known_bytes(const vmp_config& c) const {
+        for (const auto& f : footprints)
+            if (std::memcmp(&f.first, &c, sizeof(vmp_config)) == 0) return f.second;
+        return -1;
+    }
+    void remember_bytes(const vmp_config& c, long long b) {
+        if (known_bytes(c) < 0) footprints.emplace_back(c, b);
+    }
+    int free_slot() const {
+        for (int i = 0; i < (int)slots.size(); ++i)
+            if (!slots[i].open && !slots[i].closing && !slots[i].h) return i;
+        return -1;
+    }
 
     double now_ms() const {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -201,10 +288,7 @@ struct vmp_server_s {
             lk.lock();
             sl.busy = false;
             --running;
-            if (cfg.autotune && cfg.workers > 1) {
-                const int d = tuner.on_done(r.end_ms);
-                if (d > 0) vmp::merge_set_grid_divisor(d);
-            }
+            if (cfg.autotune && cfg.workers > 1) tuner.on_done(r.end_ms);
             done.push_back(r);
             cv_done.notify_all();
             cv_work.notify_all();
@@ -250,12 +334,9 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
         vmp::merge_set_throughput_mode(true);
         const int d0 = cfg.merge_grid_divisor > 0 ? cfg.merge_grid_divisor : 16;
         vmp::merge_set_grid_divisor(d0);
-        if (cfg.autotune) {  // the climb starts at the candidate nearest the configured divisor
-            int bi = 0;
-            for (int i = 1; i < MergeTuner::kN; ++i)
-                if (std::abs(MergeTuner::kCand[i] - d0) < std::abs(MergeTuner::kCand[bi] - d0)) bi = i;
-            sv->tuner.idx = bi;
-            vmp::merge_set_grid_divisor(sv->tuner.cur());
+        if (cfg.autotune) {  // the climbs start at the candidates nearest the configured shapes
+            sv->tuner = make_tuner(d0, vmp::residual_ctas_per_sm(), apply_merge_divisor, apply_residual_ctas);
+            sv->tuner.apply_all();
         }
         sv->fixed_divisor = d0;
     }
@@ -268,7 +349,8 @@ vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long
     if (!sv) return VMP_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(sv->mu);
     if (merge_grid_divisor)
-        *merge_grid_divisor = sv->cfg.autotune && sv->cfg.workers > 1 ? sv->tuner.cur() : sv->fixed_divisor;
+        *merge_grid_divisor =
+            sv->cfg.autotune && sv->cfg.workers > 1 ? sv->tuner.value("merge_grid_divisor") : sv->fixed_divisor;
     if (windows) *windows = sv->tuner.windows;
     if (best_rate) *best_rate = sv->tuner.best;
     return VMP_OK;
@@ -277,8 +359,11 @@ vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long
 vmp_status vmp_server_destroy(vmp_server_t sv) {
     if (!sv) return VMP_ERR_INVALID_ARG;
     {
-        std::lock_guard<std::mutex> lk(sv->mu);
+        std::unique_lock<std::mutex> lk(sv->mu);
         sv->stop = true;
+        sv->cv_admit.notify_all();
+        // admission requests still waiting return VMP_ERR_STATE; wait until they left
+        sv->cv_admit.wait(lk, [&] { return sv->admit_q.empty(); });
     }
     sv->cv_work.notify_all();
     for (auto& t : sv->workers) t.join();
@@ -289,45 +374,99 @@ vmp_status vmp_server_destroy(vmp_server_t sv) {
     return VMP_OK;
 }
 
-vmp_status vmp_server_open_stream(vmp_server_t sv, const vmp_config* cfg, int* stream_id) {
+// Admission of one stream (timeout_ms: 0 answer at once, < 0 no limit).
+static vmp_status open_stream(vmp_server_t sv, const vmp_config* cfg_in, int timeout_ms, int* stream_id) {
     if (!sv || !stream_id) return VMP_ERR_INVALID_ARG;
     *stream_id = -1;
-    int id = -1;
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        for (int i = 0; i < (int)sv->slots.size(); ++i)
-            if (!sv->slots[i].open && !sv->slots[i].closing && !sv->slots[i].h) { id = i; break; }
-        if (id < 0) {
-            sv->err = "no free stream slot";
-            return VMP_ERR_ADMISSION_DENIED;
-        }
-        sv->slots[id].closing = true;  // reserved while the stream is created
-    }
-    vmp_stream_t h = nullptr;
-    vmp_status st = vmp_create(cfg, &h);
-    std::lock_guard<std::mutex> lk(sv->mu);
-    Slot& s = sv->slots[id];
-    s.closing = false;
-    if (st != VMP_OK) {
-        sv->err = std::string("vmp_create: ") + vmp_last_error(nullptr);
+    vmp_config cfg;
+    if (cfg_in) cfg = *cfg_in; else vmp_config_default(&cfg);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms > 0 ? timeout_ms : 0);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    const unsigned long long ticket = sv->admit_ticket++;
+    sv->admit_q.push_back(ticket);
+    auto leave = [&](vmp_status st, const std::string& why) {
+        for (auto it = sv->admit_q.begin(); it != sv->admit_q.end(); ++it)
+            if (*it == ticket) { sv->admit_q.erase(it); break; }
+        if (!why.empty()) sv->err = why;
+        sv->cv_admit.notify_all();
         return st;
+    };
+    // waits for `pred`; false when the time limit passed first
+    auto wait_for = [&](const std::function<bool()>& pred) {
+        if (pred()) return true;
+        if (timeout_ms == 0) return false;
+        if (timeout_ms < 0) { sv->cv_admit.wait(lk, pred); return true; }
+        return sv->cv_admit.wait_until(lk, deadline, pred);
+    };
+    const long long budget = sv->cfg.hbm_budget_bytes;
+    for (;;) {
+        const long long kb = sv->known_bytes(cfg);
+        if (kb > budget)
+            return leave(VMP_ERR_ADMISSION_DENIED, "stream footprint " + std::to_string(kb) + " bytes > HBM budget");
+        const bool ready = wait_for([&] {
+            if (sv->stop) return true;
+            const long long k = sv->known_bytes(cfg);
+            return sv->admit_q.front() == ticket && sv->free_slot() >= 0 && (k < 0 || sv->used + k <= budget);
+        });
+        if (sv->stop) return leave(VMP_ERR_STATE, "server is shutting down");
+        if (!ready) {
+            if (timeout_ms != 0) return leave(VMP_ERR_TIMEOUT, "admission wait ran out");
+            const long long k = sv->known_bytes(cfg);
+            if (sv->free_slot() < 0) return leave(VMP_ERR_ADMISSION_DENIED, "no free stream slot");
+            return leave(VMP_ERR_ADMISSION_DENIED, "HBM budget: " + std::to_string(sv->used) + " + " +
+                                                       std::to_string(k) + " bytes > " + std::to_string(budget));
+        }
+        const int id = sv->free_slot();
+        sv->slots[id].closing = true;  // reserved while the stream is created
+        const unsigned long long closes0 = sv->closes;
+        lk.unlock();
+        vmp_stream_t h = nullptr;
+        const vmp_status st = vmp_create(&cfg, &h);
+        const long long b = st == VMP_OK ? vmp_device_bytes(h) : 0;
+        lk.lock();
+        sv->slots[id].closing = false;
+        if (st == VMP_ERR_OUT_OF_MEMORY && timeout_ms != 0) {
+            // the device is full: try again once a stream has closed
+            if (!wait_for([&] { return sv->stop || sv->closes != closes0; }))
+                return leave(VMP_ERR_TIMEOUT, "admission wait ran out (device memory)");
+            continue;
+        }
+        if (st != VMP_OK) return leave(st, std::string("vmp_create: ") + vmp_last_error(nullptr));
+        if (sv->stop) {
+            lk.unlock();
+            vmp_destroy(h);
+            lk.lock();
+            return leave(VMP_ERR_STATE, "server is shutting down");
+        }
+        sv->remember_bytes(cfg, b);
+        if (b > budget || sv->used + b > budget) {
+            lk.unlock();
+            vmp_destroy(h);
+            lk.lock();
+            if (b > budget || timeout_ms == 0)
+                return leave(VMP_ERR_ADMISSION_DENIED, "HBM budget: " + std::to_string(sv->used) + " + " +
+                                                           std::to_string(b) + " bytes > " + std::to_string(budget));
+            continue;  // footprint now known: wait for the budget
+        }
+        vmp_set_wait_mode(h, 1);
+        sv->used += b;
+        Slot& sl = sv->slots[id];
+        sl.open = true;
+        sl.busy = false;
+        sl.h = h;
+        sl.bytes = b;
+        sl.q.clear();
+        *stream_id = id;
+        return leave(VMP_OK, "");
     }
-    vmp_set_wait_mode(h, 1);
-    const long long b = vmp_device_bytes(h);
-    if (sv->used + b > sv->cfg.hbm_budget_bytes) {
-        vmp_destroy(h);
-        sv->err = "HBM budget: " + std::to_string(sv->used) + " + " + std::to_string(b) + " bytes > " +
-                  std::to_string(sv->cfg.hbm_budget_bytes);
-        return VMP_ERR_ADMISSION_DENIED;
-    }
-    sv->used += b;
-    s.open = true;
-    s.busy = false;
-    s.h = h;
-    s.bytes = b;
-    s.q.clear();
-    *stream_id = id;
-    return VMP_OK;
+}
+
+vmp_status vmp_server_open_stream(vmp_server_t sv, const vmp_config* cfg, int* stream_id) {
+    return open_stream(sv, cfg, 0, stream_id);
+}
+
+vmp_status vmp_server_open_stream_wait(vmp_server_t sv, const vmp_config* cfg, int timeout_ms, int* stream_id) {
+    return open_stream(sv, cfg, timeout_ms, stream_id);
 }
 
 vmp_status vmp_server_close_stream(vmp_server_t sv, int id) {
@@ -340,12 +479,14 @@ vmp_status vmp_server_close_stream(vmp_server_t sv, int id) {
     s.open = false;
     vmp_stream_t h = s.h;
     s.h = nullptr;
-    sv->used -= s.bytes;
-    s.bytes = 0;
     lk.unlock();
     vmp_destroy(h);
     lk.lock();
+    sv->used -= s.bytes;  // released once its memory is freed
+    s.bytes = 0;
     s.closing = false;
+    ++sv->closes;
+    sv->cv_admit.notify_all();
     return VMP_OK;
 }
 
@@ -444,6 +585,48 @@ vmp_status vmp_server_info(vmp_server_t sv, long long* budget_used, int* streams
     }
     if (queued) *queued = sv->queued;
     if (running) *running = sv->running;
+    return VMP_OK;
+}
+
+vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value) {
+    if (!sv || !name || !value) return VMP_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (std::strcmp(name, "merge_grid_divisor") == 0) {
+        *value = sv->cfg.autotune && sv->cfg.workers > 1 ? sv->tuner.value(name) : sv->fixed_divisor;
+        return VMP_OK;
+    }
+    if (std::strcmp(name, "residual_ctas_per_sm") == 0) {
+        *value = vmp::residual_ctas_per_sm();
+        return VMP_OK;
+    }
+    return VMP_ERR_INVALID_ARG;
+}
+
+// Test hook: the autotuner's climb on a model throughput instead of a GPU.
+// rates[i * 2 + j]: packages/s with merge divisor candidate i (4, 8, 16, 32,
+// 64) and residual CTAs per SM candidate j (3, 4); completions are spaced
+// by 1 / rate.  trace[2 * w], trace[2 * w + 1]: the two knobs after window w.
+vmp_status vmp_test_autotune(int merge_divisor, int residual_ctas, const double* rates, int windows, int* trace) {
+    if (!rates || !trace || windows < 0) return VMP_ERR_INVALID_ARG;
+    Autotuner t = make_tuner(merge_divisor, residual_ctas, model_set_d, model_set_c);
+    t.apply_all();
+    double now = 0.0;
+    for (int w = 0; w < windows;) {
+        int di = 0;
+        for (int i = 0; i < (int)t.knobs[0].cand.size(); ++i)
+            if (t.knobs[0].cand[i] == g_model_d) di = i;
+        const int ci = g_model_c == 4 ? 1 : 0;
+        const double r = rates[di * 2 + ci];
+        if (!(r > 0.0)) return VMP_ERR_INVALID_ARG;
+        now += 1000.0 / r;
+        const long long before = t.windows;
+        t.on_done(now);
+        if (t.windows != before) {
+            trace[2 * w] = g_model_d;
+            trace[2 * w + 1] = g_model_c;
+            ++w;
+        }
+    }
     return VMP_OK;
 }
 

@@ -44,6 +44,14 @@ class Server:
         self._cfgs[sid.value] = config
         return sid.value
 
+    def open_stream_wait(self, config, timeout_ms=-1):
+        """open_stream that waits for a slot and budget (vmp_server_open_stream_wait)."""
+        sid = C.c_int(-1)
+        self._check(self.lib.vmp_server_open_stream_wait(self.h, C.byref(config), int(timeout_ms), C.byref(sid)),
+                    "open_stream_wait")
+        self._cfgs[sid.value] = config
+        return sid.value
+
     def close_stream(self, sid):
         self._check(self.lib.vmp_server_close_stream(self.h, int(sid)), "close_stream")
         self._cfgs.pop(sid, None)
@@ -97,7 +105,10 @@ class Server:
         """The online autotuner's state (vmp_server_tuning)."""
         d, w, r = C.c_int(), C.c_longlong(), C.c_double()
         self._check(self.lib.vmp_server_tuning(self.h, C.byref(d), C.byref(w), C.byref(r)), "vmp_server_tuning")
-        return {"merge_grid_divisor": d.value, "windows": w.value, "best_rate": r.value}
+        k = C.c_int()
+        self._check(self.lib.vmp_server_knob(self.h, b"residual_ctas_per_sm", C.byref(k)), "vmp_server_knob")
+        return {"merge_grid_divisor": d.value, "residual_ctas_per_sm": k.value, "windows": w.value,
+                "best_rate": r.value}
 
     def close(self):
         if getattr(self, "h", None):
