@@ -165,15 +165,16 @@ def test_admission_waits_for_budget_while_streams_run():
         srv.close_stream(a)  # waits for a's packages, frees its budget
         th.join(timeout=60)
         assert not th.is_alive() and "sid" in waiter, waiter
-        c = waiter["sid"]
+        c = waiter["sid"]  # may reuse a's slot: its packages carry cookies 100..109
         for k in range(10):
-            srv.submit(c, pk[2][k], cookie=k)
+            srv.submit(c, pk[2][k], cookie=100 + k)
         while sum(len(v) for v in got.values()) < 30:
             for r in srv.poll(timeout_ms=1000):
                 assert r.status == abi.VMP_OK, r.status
-                got.setdefault(r.stream_id, []).append((r.cookie, _key(r.result)))
-        for sid, i in ((a, 0), (b, 1), (c, 2)):
-            seq = sorted(got[sid])
+                i = 2 if r.cookie >= 100 else (0 if r.stream_id == a else 1)
+                got.setdefault(i, []).append((r.cookie % 100, _key(r.result)))
+        for i in range(3):
+            seq = sorted(got[i])
             assert [x for x, _ in seq] == list(range(10))
             assert [k for _, k in seq] == ref[i], f"stream {i} differs from its results alone"
         # budget full again (b and c open): a request with a short limit times out
