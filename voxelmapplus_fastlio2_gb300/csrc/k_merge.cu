@@ -147,6 +147,55 @@ __device__ inline uint32_t merge_candidate(const DMap& m, int64_t x, int64_t y, 
     return b_rec;
 }
 
+// merge_candidate for all six neighbours at once, with the loads of the six
+// lookups issued together (the first probe of each; a collision falls back to
+// the probe loop) and then those of the six records: one memory round trip
+// per step instead of six.
+__device__ inline void merge_candidates6(const DMap& m, int64_t x, int64_t y, int64_t z, unsigned long long T,
+                                         uint32_t out[6]) {
+    const int64_t nb[6][3] = {{x - 1, y, z}, {x, y - 1, z}, {x, y, z - 1}, {x + 1, y, z}, {x, y + 1, z}, {x, y, z + 1}};
+    uint64_t key[6], h[6], kk[6];
+    bool ok[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        ok[k] = key_in_range(nb[k][0]) && key_in_range(nb[k][1]) && key_in_range(nb[k][2]);
+        key[k] = ok[k] ? pack_key(nb[k][0], nb[k][1], nb[k][2]) : 0;
+        h[k] = hash_key(key[k]) & m.table_mask;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) kk[k] = ok[k] ? __ldg(&m.keys[h[k]]) : kEmptyKey;
+    uint32_t rec[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) rec[k] = (ok[k] && kk[k] == key[k]) ? __ldg(&m.vals[h[k]]) : kNoRec;
+    for (int k = 0; k < 6; ++k)  // first slot taken by another key: probe on (rare)
+        if (ok[k] && kk[k] != key[k] && kk[k] != kEmptyKey) rec[k] = map_find(m, key[k]);
+    unsigned long long cg[6], eg[6], fg[6];
+    uint32_t fl[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const bool v = rec[k] != kNoRec && rec[k] < (uint32_t)m.rec_pool;
+        if (!v) rec[k] = kNoRec;
+        const uint32_t r = v ? rec[k] : 0;
+        fl[k] = v ? m.hot[r].flags : 0u;
+        cg[k] = v ? m.cold[r].create_g : 0ull;
+        eg[k] = v ? m.cold[r].evict_g : 0ull;
+        fg[k] = v ? m.cold[r].freeze_g : 0ull;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        uint32_t r = rec[k];
+        if (r != kNoRec) {
+            if (!(fl[k] & F_ALIVE) && eg[k] == kNever) r = kNone;
+            else if (!(cg[k] < T && eg[k] > T)) r = kNone;  // not in the map at this point
+            else if (!(fg[k] < T)) r = kNone;
+            else if (!(fl[k] & F_PLANE)) r = kNone;
+        } else {
+            r = kNone;
+        }
+        out[k] = r;
+    }
+}
+
 // One merge() call by record a_rec at batch point t, one thread (the replay).
 // Outputs the written states (neighbours first, in probe order, then the
 // caller) into out/out_rec; returns how many.
@@ -279,16 +328,31 @@ __device__ inline void plane_at(const DMap& m, uint32_t r, uint32_t t, const MEn
 
 // Does the call merge anything?  merge()'s tests up to its first merge, with
 // the caller's state as of the call (one thread).
+// The group ids of the six neighbours are read first (independent loads and
+// log walks, which overlap); a neighbour of the caller's group is skipped
+// without reading its plane.
 __device__ bool call_merges(const DMap& m, uint32_t a_rec, uint32_t t, const uint32_t* cand, const MEntry* ent,
                             const uint32_t* head) {
     PlaneRef a;
     plane_at(m, a_rec, t, ent, head, a);
+    uint32_t eb[6];
+    uint64_t gb[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        eb[k] = cand[k] != kNone ? find_entry(cand[k], t, ent, head) : kNone;
+        gb[k] = cand[k] == kNone ? a.group : (eb[k] == kNone ? m.hot[cand[k]].group : ent[eb[k]].s.group);
+    }
     for (int k = 0; k < 6; ++k) {
         const uint32_t b_rec = cand[k];
-        if (b_rec == kNone) continue;
+        if (b_rec == kNone || gb[k] == a.group) continue;
         PlaneRef b;
-        plane_at(m, b_rec, t, ent, head, b);
-        if (b.group == a.group) continue;
+        if (eb[k] == kNone) {
+            const RecHot& hb = m.hot[b_rec];
+            for (int q = 0; q < 3; ++q) { b.mean[q] = hb.mean[q]; b.norm[q] = hb.norm[q]; }
+        } else {
+            const MState& sb = ent[eb[k]].s;
+            for (int q = 0; q < 3; ++q) { b.mean[q] = sb.mean[q]; b.norm[q] = sb.norm[q]; }
+        }
         double norm_distance = 1.0 - dot3(b.norm, a.norm);
         double axis_distance = fabs(dot3(b.norm, b.mean) - dot3(a.norm, a.mean));
         if (norm_distance > m.merge_angle || axis_distance > m.merge_dist) continue;
@@ -373,22 +437,29 @@ __device__ uint64_t warp_merge_call(const DMap& m, MergeScratch& g, uint32_t a_r
                                     const MEntry* pent, const uint32_t* phead, int cur, bool& overflow,
                                     uint32_t round_tag) {
     const int lane = threadIdx.x & 31;
-    uint32_t ea = 0;
-    if (lane == 0) ea = find_entry(a_rec, t, pent, phead);
-    ea = __shfl_sync(0xffffffffu, ea, 0);
+    // the log entries of the caller (lane 6) and of the six neighbours (lanes
+    // 0-5) as of the call, and the neighbours' group ids: walked in parallel
+    // (nothing the call writes changes a neighbour's state before it is read)
+    uint32_t e_l = kNone;
+    uint64_t g_l = 0;
+    if (lane < 6 && cand[lane] != kNone) {
+        e_l = find_entry(cand[lane], t, pent, phead);
+        g_l = e_l == kNone ? m.hot[cand[lane]].group : pent[e_l].s.group;
+    } else if (lane == 6) {
+        e_l = find_entry(a_rec, t, pent, phead);
+    }
+    const uint32_t ea = __shfl_sync(0xffffffffu, e_l, 6);
     WState a;
     wstate_load(m, a_rec, ea, pent, lane, a);
     uint64_t sig = kSigNone;
     int nout = 0;
     for (int k = 0; k < 6; ++k) {
         const uint32_t b_rec = cand[k];
-        if (b_rec == kNone) continue;
-        uint32_t eb = 0;
-        if (lane == 0) eb = find_entry(b_rec, t, pent, phead);
-        eb = __shfl_sync(0xffffffffu, eb, 0);
+        const uint32_t eb = __shfl_sync(0xffffffffu, e_l, k);
+        const uint64_t gbk = __shfl_sync(0xffffffffu, g_l, k);
+        if (b_rec == kNone || gbk == a.group) continue;
         WState b;
         wstate_load(m, b_rec, eb, pent, lane, b);
-        if (b.group == a.group) continue;
         double norm_distance = 1.0 - dot3(b.norm, a.norm);
         double axis_distance = fabs(dot3(b.norm, b.mean) - dot3(a.norm, a.mean));
         if (norm_distance > m.merge_angle || axis_distance > m.merge_dist) continue;
@@ -445,7 +516,7 @@ __device__ inline void mark(MergeCtl* c, int& k) {
 
 // All rounds of the fixed point and the final write-back, one cooperative
 // launch.
-__global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeScratch g,
+__global__ void __launch_bounds__(kMergeThreads, 3) k_merge_fixpoint(DMap m, MergeScratch g,
                                                                   const uint32_t* __restrict__ ev_list,
                                                                   const uint32_t* __restrict__ ev_rec,
                                                                   const int* d_n_ev) {
@@ -503,10 +574,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_fixpoint(DMap m, MergeS
                 const unsigned long long T = m.cnt->batch_base + t;
                 int64_t x, y, z;
                 unpack_key(m.cold[a_rec].key, x, y, z);
-                for (int k = 0; k < 6; ++k) {
-                    cl[k] = merge_candidate(m, x, y, z, k, T);
-                    g.cand[(size_t)e * 6 + k] = cl[k];
-                }
+                merge_candidates6(m, x, y, z, T, cl);
+                for (int k = 0; k < 6; ++k) g.cand[(size_t)e * 6 + k] = cl[k];
             } else {
                 for (int k = 0; k < 6; ++k) cl[k] = g.cand[(size_t)e * 6 + k];
             }
