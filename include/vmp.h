@@ -530,24 +530,29 @@ typedef struct vmp_server_result {
 
 void vmp_server_config_default(vmp_server_config* c);
 /* The autotuner (config.autotune, servers with more than one worker): a
- * coordinate hill climb over launch shapes on windows of 128 completed
- * packages -- merge_grid_divisor (served merge launches use SMs / d CTAs,
- * d in 4..64) and residual_ctas_per_sm (the residual kernel's register
- * budget, 3 or 4 resident CTAs per SM; scan graphs are captured again after
- * a change).  Both are process-wide and change launch shapes only: results
- * are the same under every setting.  vmp_server_tuning: the merge divisor in
- * use, the windows measured so far and the best rate seen (packages/s);
- * vmp_server_knob: a knob's value by name. */
+ * coordinate hill climb over two scheduling knobs on windows of 128
+ * completed packages, starting after 24 windows (short runs keep the
+ * starting shapes, the best measured ones) -- merge_grid_divisor (served
+ * merge launches use SMs / d CTAs, d in 4..64; process-wide) and
+ * max_inflight (packages on the GPU at once: 8, 16, 24 or 32 of the
+ * workers).  Neither changes results, and neither needs the streams' scan
+ * graphs captured again.  vmp_server_tuning: the merge divisor in use, the
+ * windows measured so far and the best rate seen (packages/s);
+ * vmp_server_knob: "merge_grid_divisor", "max_inflight" or
+ * "residual_ctas_per_sm" by name. */
 vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long* windows, double* best_rate);
 vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value);
-/* Sets residual_ctas_per_sm by hand (3 or 4; process-wide, what the
- * autotuner does; VMP_RESIDUAL_CTAS_PER_SM gives the value at load). */
+/* The residual kernel's register budget, by hand: 3 or 4 resident CTAs per
+ * SM (process-wide; VMP_RESIDUAL_CTAS_PER_SM gives the value at load).  The
+ * results are the same; the streams' scan graphs are captured again at their
+ * next scan, which costs milliseconds per stream, so the online tuner leaves
+ * this one alone. */
 vmp_status vmp_set_residual_ctas_per_sm(int ctas);
 /* Test hook: the autotuner's climb on a model instead of a GPU (no CUDA
- * call).  rates[i * 2 + j]: packages/s with merge divisor candidate i
- * (4, 8, 16, 32, 64) and residual CTAs per SM candidate j (3, 4); trace
+ * call).  rates[i * 4 + j]: packages/s with merge divisor candidate i
+ * (4, 8, 16, 32, 64) and max_inflight candidate j (8, 16, 24, 32); trace
  * (2 x windows ints): both knobs after each window. */
-vmp_status vmp_test_autotune(int merge_divisor, int residual_ctas, const double* rates, int windows, int* trace);
+vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, const double* rates, int windows, int* trace);
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out);
 /* Waits for the packages that are running; queued ones are dropped;
  * admission requests still waiting return VMP_ERR_STATE. */

@@ -3,12 +3,13 @@ model throughput instead of a GPU through the vmp_test_autotune hook: the
 same code the server runs at every completed package, fed completion times
 spaced by 1 / rate of the launch shapes it currently applies.
 
-Knobs: merge grid divisor (4, 8, 16, 32, 64) and residual CTAs per SM
-(3, 4).  The climbs start after 8 windows of 128 packages at the starting
-shapes, take the knobs one after the other, and then keep the shapes for 32
-windows.  That both knobs leave results unchanged is tested on the GPU
-(test_serve.py: test_merge_launch_shape_does_not_change_results,
-test_residual_register_budget_does_not_change_results)."""
+Knobs: merge grid divisor (4, 8, 16, 32, 64) and max_inflight, the packages
+on the GPU at once (8, 16, 24, 32).  The climbs start after 24 windows of
+128 packages at the starting shapes, take the knobs one after the other, and
+then keep the shapes for 32 windows.  Neither knob changes results: the
+merge divisor is tested on the GPU (test_serve.py:
+test_merge_launch_shape_does_not_change_results); max_inflight only decides
+when a worker starts the next package."""
 import ctypes as C
 import os
 
@@ -16,7 +17,8 @@ import numpy as np
 import pytest
 
 DIV = [4, 8, 16, 32, 64]
-CTAS = [3, 4]
+INFL = [8, 16, 24, 32]
+FIRST = 24  # windows at the starting shapes
 
 
 def _lib():
@@ -27,7 +29,7 @@ def _lib():
 
 
 def _climb(start_d, start_c, rate_fn, windows):
-    rates = np.array([[rate_fn(d, c) for c in CTAS] for d in DIV], dtype=np.float64).reshape(-1)
+    rates = np.array([[rate_fn(d, c) for c in INFL] for d in DIV], dtype=np.float64).reshape(-1)
     trace = np.zeros(2 * windows, dtype=np.int32)
     code = _lib().vmp_test_autotune(start_d, start_c, C.c_void_p(rates.ctypes.data), windows,
                                     C.c_void_p(trace.ctypes.data))
@@ -37,7 +39,8 @@ def _climb(start_d, start_c, rate_fn, windows):
 
 def _peaked(best_d, best_c):
     # throughput falling off with the distance (in candidates) from the best shape
-    return lambda d, c: 5000.0 - 400.0 * abs(DIV.index(d) - DIV.index(best_d)) - 150.0 * abs(c - best_c)
+    return lambda d, c: (5000.0 - 400.0 * abs(DIV.index(d) - DIV.index(best_d))
+                         - 150.0 * abs(INFL.index(c) - INFL.index(best_c)))
 
 
 def _settled(tr, last=40):
@@ -48,21 +51,22 @@ def _settled(tr, last=40):
 
 
 def test_climb_moves_off_a_bad_start():
-    tr = _climb(64, 3, _peaked(16, 4), 80)
-    assert all(tuple(t) == (64, 3) for t in tr[:7])  # the first windows keep the starting shapes
-    assert _settled(tr) == (16, 4)
+    tr = _climb(64, 8, _peaked(16, 24), 110)
+    assert all(tuple(t) == (64, 8) for t in tr[:FIRST - 1])  # the first windows keep the starting shapes
+    assert _settled(tr) == (16, 24)
     # settled within the first round of climbs, then kept for the exploit windows
-    assert all(tuple(t) == (16, 4) for t in tr[20:45])
+    assert all(tuple(t) == (16, 24) for t in tr[FIRST + 16:FIRST + 40])
 
 
-@pytest.mark.parametrize("best", [(4, 3), (32, 4), (64, 4)])
+@pytest.mark.parametrize("best", [(4, 8), (32, 32), (64, 16)])
 def test_climb_reaches_the_best_shape(best):
-    tr = _climb(16, 3, _peaked(*best), 80)
+    tr = _climb(16, 32, _peaked(*best), 110)
     assert _settled(tr) == best
 
 
 def test_climb_keeps_a_good_start():
-    tr = _climb(16, 3, _peaked(16, 3), 80)
+    tr = _climb(16, 32, _peaked(16, 32), 110)
     # probes visit the neighbours only; the kept shape is the start
     assert set(int(d) for d in tr[:, 0]) <= {8, 16, 32}
-    assert _settled(tr) == (16, 3)
+    assert set(int(c) for c in tr[:, 1]) <= {24, 32}
+    assert _settled(tr) == (16, 32)

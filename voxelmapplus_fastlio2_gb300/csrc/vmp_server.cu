@@ -70,7 +70,7 @@ struct Slot {
 struct KnobClimb {
     const char* name;
     std::vector<int> cand;
-    void (*apply)(int);
+    std::function<void(int)> apply;
     int idx = 0;          // current candidate
     int probe = 3;        // 1: measuring idx + 1, 2: idx - 1, 3: not climbing
     double rate[3] = {};  // current, upper, lower
@@ -118,13 +118,16 @@ struct KnobClimb {
 // throughput of the current shapes; the knobs are climbed one after the
 // other (coordinate-wise), then the shapes are kept for kExploit windows
 // before the next round of climbs (the stream mix may have changed).  The
-// first climb starts after kFirst windows, so short runs pay nothing for the
-// exploration.  Every knob changes launch shapes only, never results:
-//   merge_grid_divisor    served merge launches use SMs / d CTAs;
-//   residual_ctas_per_sm  the residual kernel's register budget (3 or 4
-//                         resident CTAs per SM; scan graphs are recaptured).
+// first climb starts after kFirst windows (about 3 000 packages), so that
+// short runs stay on the starting shapes, the best measured ones.  Both
+// knobs change scheduling only, never results, and neither needs the
+// streams' captured scan graphs to be captured again:
+//   merge_grid_divisor  served merge launches use SMs / d CTAs;
+//   max_inflight        packages on the GPU at once (of the workers' slots):
+//                       fewer contend less for the hardware work queues,
+//                       more overlap more.
 struct Autotuner {
-    static constexpr int kWindow = 128, kSettle = 16, kExploit = 32, kFirst = 8;
+    static constexpr int kWindow = 128, kSettle = 16, kExploit = 32, kFirst = 24;
     std::vector<KnobClimb> knobs;
     int active = -1;  // the knob being climbed (-1: exploiting)
     int exploit_left = kFirst;
@@ -175,18 +178,18 @@ struct Autotuner {
 };
 
 static void apply_merge_divisor(int d) { vmp::merge_set_grid_divisor(d); }
-static void apply_residual_ctas(int c) { vmp::residual_set_ctas_per_sm(c); }
 // the launch shapes of vmp_test_autotune's model (one caller at a time)
 static int g_model_d = 0, g_model_c = 0;
 static void model_set_d(int d) { g_model_d = d; }
 static void model_set_c(int c) { g_model_c = c; }
 
-static Autotuner make_tuner(int merge_divisor, int residual_ctas, void (*set_d)(int), void (*set_c)(int)) {
+static Autotuner make_tuner(int merge_divisor, int inflight, std::function<void(int)> set_d,
+                            std::function<void(int)> set_c) {
     Autotuner t;
     t.knobs.push_back(KnobClimb{"merge_grid_divisor", {4, 8, 16, 32, 64}, set_d});
-    t.knobs.push_back(KnobClimb{"residual_ctas_per_sm", {3, 4}, set_c});
+    t.knobs.push_back(KnobClimb{"max_inflight", {8, 16, 24, 32}, set_c});
     t.knobs[0].set_nearest(merge_divisor);
-    t.knobs[1].set_nearest(residual_ctas);
+    t.knobs[1].set_nearest(inflight);
     return t;
 }
 
@@ -204,6 +207,7 @@ struct vmp_server_s {
     long long used = 0;
     int running = 0;
     int queued = 0;
+    int max_inflight = 1 << 30;  // packages on the GPU at once (the autotuner's second knob)
     std::string err;
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     // admission requests in arrival order (tickets); the front one is served
@@ -232,8 +236,10 @@ struct vmp_server_s {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
 
-    // the ready stream whose oldest package was submitted first (-1: none)
+    // the ready stream whose oldest package was submitted first (-1: none, or
+    // max_inflight packages running)
     int pick() const {
+        if (running >= max_inflight) return -1;
         int best = -1;
         double bt = 0.0;
         for (int i = 0; i < (int)slots.size(); ++i) {
@@ -335,7 +341,11 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
         const int d0 = cfg.merge_grid_divisor > 0 ? cfg.merge_grid_divisor : 16;
         vmp::merge_set_grid_divisor(d0);
         if (cfg.autotune) {  // the climbs start at the candidates nearest the configured shapes
-            sv->tuner = make_tuner(d0, vmp::residual_ctas_per_sm(), apply_merge_divisor, apply_residual_ctas);
+            // (applied under the server lock: the tuner runs in on_done, called with it held)
+            sv->tuner = make_tuner(d0, cfg.workers, apply_merge_divisor, [sv](int c) {
+                sv->max_inflight = c;
+                sv->cv_work.notify_all();
+            });
             sv->tuner.apply_all();
         }
         sv->fixed_divisor = d0;
@@ -595,6 +605,10 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value) {
         *value = sv->cfg.autotune && sv->cfg.workers > 1 ? sv->tuner.value(name) : sv->fixed_divisor;
         return VMP_OK;
     }
+    if (std::strcmp(name, "max_inflight") == 0) {
+        *value = sv->max_inflight < sv->cfg.workers ? sv->max_inflight : sv->cfg.workers;
+        return VMP_OK;
+    }
     if (std::strcmp(name, "residual_ctas_per_sm") == 0) {
         *value = vmp::residual_ctas_per_sm();
         return VMP_OK;
@@ -604,19 +618,21 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value) {
 
 // Test hook: the autotuner's climb on a model throughput instead of a GPU.
 // rates[i * 2 + j]: packages/s with merge divisor candidate i (4, 8, 16, 32,
-// 64) and residual CTAs per SM candidate j (3, 4); completions are spaced
+// 64) and max_inflight candidate j (8, 16, 24, 32); completions are spaced
 // by 1 / rate.  trace[2 * w], trace[2 * w + 1]: the two knobs after window w.
-vmp_status vmp_test_autotune(int merge_divisor, int residual_ctas, const double* rates, int windows, int* trace) {
+vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, const double* rates, int windows, int* trace) {
     if (!rates || !trace || windows < 0) return VMP_ERR_INVALID_ARG;
-    Autotuner t = make_tuner(merge_divisor, residual_ctas, model_set_d, model_set_c);
+    Autotuner t = make_tuner(merge_divisor, max_inflight, model_set_d, model_set_c);
     t.apply_all();
     double now = 0.0;
     for (int w = 0; w < windows;) {
         int di = 0;
         for (int i = 0; i < (int)t.knobs[0].cand.size(); ++i)
             if (t.knobs[0].cand[i] == g_model_d) di = i;
-        const int ci = g_model_c == 4 ? 1 : 0;
-        const double r = rates[di * 2 + ci];
+        int ci = 0;
+        for (int i = 0; i < (int)t.knobs[1].cand.size(); ++i)
+            if (t.knobs[1].cand[i] == g_model_c) ci = i;
+        const double r = rates[di * 4 + ci];
         if (!(r > 0.0)) return VMP_ERR_INVALID_ARG;
         now += 1000.0 / r;
         const long long before = t.windows;

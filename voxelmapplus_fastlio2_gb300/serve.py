@@ -106,8 +106,8 @@ class Server:
         d, w, r = C.c_int(), C.c_longlong(), C.c_double()
         self._check(self.lib.vmp_server_tuning(self.h, C.byref(d), C.byref(w), C.byref(r)), "vmp_server_tuning")
         k = C.c_int()
-        self._check(self.lib.vmp_server_knob(self.h, b"residual_ctas_per_sm", C.byref(k)), "vmp_server_knob")
-        return {"merge_grid_divisor": d.value, "residual_ctas_per_sm": k.value, "windows": w.value,
+        self._check(self.lib.vmp_server_knob(self.h, b"max_inflight", C.byref(k)), "vmp_server_knob")
+        return {"merge_grid_divisor": d.value, "max_inflight": k.value, "windows": w.value,
                 "best_rate": r.value}
 
     def close(self):
