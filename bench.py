@@ -215,7 +215,7 @@ TRAFFIC_PER_UNIT = {
 # cycles whatever its active lanes (a dependent-DFMA micro-probe on this
 # GB300), so the pipe's peak is 4 x SMs x clock / 64 warp instructions/s.
 FP64_PER_UNIT = {
-    "residual": 5.81,   # per downsampled point x IEKF iteration
+    "residual": 4.71,   # per downsampled point x IEKF iteration (k_residual<6, 3>: 196.9 k on 41.8 k points)
     "undistort": 7.11,  # per raw point
     "body_cov": 6.22,   # per downsampled point
     "map_batch": 5.57,  # per batch point

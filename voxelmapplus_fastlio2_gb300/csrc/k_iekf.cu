@@ -213,42 +213,40 @@ __device__ void bd_sandwich(const BlkDiag& B, const double* X, double* tmp, doub
 }
 
 // Gauss-Jordan with partial pivoting on s.aug = [S | I] (nj x 2nj); S^-1 ends
-// in the right half.  All threads of the block take part.
-__device__ void gauss_jordan(IekfSm& s, int nj) {
-    const int t = threadIdx.x, lane = t & 31;
+// in the right half.  One warp (the caller's); the other warps wait at the
+// caller's next __syncthreads.
+__device__ void gauss_jordan_warp(IekfSm& s, int nj) {
+    const int lane = threadIdx.x & 31;
     const int w = 2 * nj;
     for (int k = 0; k < nj; ++k) {
-        if (t < 32) {
-            // pivot: largest |a_ik|, i >= k; magnitudes of doubles order like
-            // the integers of their high words (ties go to the lower row)
-            const int i = k + lane;
-            int key = -1;
-            if (i < nj) key = __double2hiint(s.aug[i * w + k]) & 0x7fffffff;
-            int best = i;
+        // pivot: largest |a_ik|, i >= k; magnitudes of doubles order like the
+        // integers of their high words (ties go to the lower row); the
+        // butterfly leaves the winner on every lane
+        const int i = k + lane;
+        int key = -1;
+        if (i < nj) key = __double2hiint(s.aug[i * w + k]) & 0x7fffffff;
+        int best = i;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const int ok = __shfl_xor_sync(0xffffffffu, key, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, best, o);
-                if (ok > key || (ok == key && oi < best)) { key = ok; best = oi; }
-            }
-            if (lane == 0) s.piv = best;
+        for (int o = 16; o > 0; o >>= 1) {
+            const int ok = __shfl_xor_sync(0xffffffffu, key, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, best, o);
+            if (ok > key || (ok == key && oi < best)) { key = ok; best = oi; }
         }
-        __syncthreads();
-        const int p = s.piv;
-        if (p != k && t < w) {
-            const double a = s.aug[k * w + t];
-            s.aug[k * w + t] = s.aug[p * w + t];
-            s.aug[p * w + t] = a;
+        const int p = best;
+        if (p != k && lane < w) {
+            const double a = s.aug[k * w + lane];
+            s.aug[k * w + lane] = s.aug[p * w + lane];
+            s.aug[p * w + lane] = a;
         }
-        __syncthreads();
-        if (t < w) s.prow[t] = s.aug[k * w + t] * (1.0 / s.aug[k * w + k]);
-        else if (t >= 32 && t < 32 + nj) s.col[t - 32] = s.aug[(t - 32) * w + k];
-        __syncthreads();
-        for (int e = t; e < nj * w; e += blockDim.x) {
-            const int i = e / w, j = e - i * w;
-            s.aug[e] = (i == k) ? s.prow[j] : fma(-s.col[i], s.prow[j], s.aug[e]);
+        __syncwarp();
+        if (lane < w) s.prow[lane] = s.aug[k * w + lane] * (1.0 / s.aug[k * w + k]);
+        if (lane < nj) s.col[lane] = s.aug[lane * w + k];
+        __syncwarp();
+        for (int e = lane; e < nj * w; e += 32) {
+            const int r = e / w, j = e - r * w;
+            s.aug[e] = (r == k) ? s.prow[j] : fma(-s.col[r], s.prow[j], s.aug[e]);
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -258,24 +256,29 @@ __device__ inline int lin_state_off(int u) { return u < 3 ? u : u + 18; }
 __device__ inline int lin_delta_idx(int u) { return u < 3 ? u : u + 6; }
 
 // One pass of the IESKF::update loop body after func_ (ieskf.cpp:135-148) in
-// the information-form rewrite described at the top of this file.  H / b of
-// the measurement (nj x nj, nj) are in shared memory.  One CTA.
-__device__ void iekf_step(DFilter* f, IekfSm& s, const double* Hm, const double* bm, int nj, double eps) {
+// the information-form rewrite described at the top of this file, in two
+// parts.  iekf_boxminus: delta = x boxminus x_pred and D = J^-1, the
+// transcendental pieces on separate warps (thread `base`: rot, base + 32:
+// rot_ext, base + 64: the S2 block, base + 96 .. 110: the linear
+// coordinates); it needs nothing of the measurement, so it runs beside the
+// fold of the block partials.  iekf_step_rest: the rest, after a
+// __syncthreads.  H / b of the measurement (nj x nj, nj) are in shared
+// memory.  One CTA.
+__device__ void iekf_boxminus(const DFilter* f, IekfSm& s, int base) {
     const int t = threadIdx.x;
     const DState& x = f->x;
     const DState& xp = f->x_pred;
-    // boxminus delta and D = J^-1, the transcendental pieces in separate warps
-    if (t == 0) {
+    if (t == base) {
         double J[9];
         rot_minus(x.rot, xp.rot, s.d + 3);
         so3_right_jac(s.d + 3, J);
         inv3(J, s.D.r);
-    } else if (t == 32) {
+    } else if (t == base + 32) {
         double J[9];
         rot_minus(x.rot_ext, xp.rot_ext, s.d + 6);
         so3_right_jac(s.d + 6, J);
         inv3(J, s.D.e);
-    } else if (t == 64) {
+    } else if (t == base + 64) {
         double Nx[6], Mx[6], A[4];
         s2_minus(x.g, xp.g, s.d + 21);
         s2_Nx(x.g, Nx);
@@ -284,13 +287,15 @@ __device__ void iekf_step(DFilter* f, IekfSm& s, const double* Hm, const double*
         const double id = 1.0 / (A[0] * A[3] - A[1] * A[2]);
         s.D.g[0] = A[3] * id; s.D.g[1] = -A[1] * id;
         s.D.g[2] = -A[2] * id; s.D.g[3] = A[0] * id;
-    } else if (t >= 96 && t < 111) {
-        const int u = t - 96;
+    } else if (t >= base + 96 && t < base + 111) {
+        const int u = t - base - 96;
         const double* xs = reinterpret_cast<const double*>(&x);
         const double* ps = reinterpret_cast<const double*>(&xp);
         s.d[lin_delta_idx(u)] = xs[lin_state_off(u)] - ps[lin_state_off(u)];
     }
-    __syncthreads();
+}
+__device__ void iekf_step_rest(DFilter* f, IekfSm& s, const double* Hm, const double* bm, int nj, double eps) {
+    const int t = threadIdx.x;
     if (t < 23) s.dp[t] = bd_row(s.D, s.d, 1, t, 0);
     bd_sandwich(s.D, f->P, s.T, s.M);  // M = D P D^T
     // S = I + Hm M_EE as [S | I];  y = Hm d'_E - bm
@@ -314,7 +319,8 @@ __device__ void iekf_step(DFilter* f, IekfSm& s, const double* Hm, const double*
         s.y[i] = a - bm[i];
     }
     __syncthreads();
-    gauss_jordan(s, nj);
+    if (t < 32) gauss_jordan_warp(s, nj);
+    __syncthreads();
     // K = M_E S^-1
     for (int e = t; e < 23 * nj; e += blockDim.x) {
         const int i = e / nj, j = e - i * nj;
@@ -377,12 +383,12 @@ constexpr size_t residual_smem_bytes() {
     constexpr size_t fold = sizeof(double) * (kIekfThreads / 32) * 32 * R::VPL;
     return rows > fold ? rows : fold;
 }
-// ... and of k_residual_fold<NJ>: the stripes, then the filter step's scratch.
+// ... and of k_residual_fold<NJ>: the filter step's scratch, then the stripes.
+constexpr int kFoldThreads = 384;  // warps 0-7 fold, warps 8-11 boxminus
 template <int NJ>
 constexpr size_t fold_smem_bytes() {
     using R = Red<NJ>;
-    constexpr size_t fold = sizeof(double) * (R::STRIPES + 1) * R::NV;
-    return fold > sizeof(IekfSm) ? fold : sizeof(IekfSm);
+    return (sizeof(IekfSm) + 15) / 16 * 16 + sizeof(double) * (R::STRIPES + 1) * R::NV;
 }
 
 // func_ (sharedUpdateFunc) over all downsampled points: per block the sums of
@@ -480,18 +486,21 @@ __global__ void __launch_bounds__(kIekfThreads, MINB) k_residual(DFilter* f, DSc
 // value k) adds blocks q, q + STRIPES, ... in order, then the stripes are
 // added in order -- and the filter step of this iteration.  One CTA.
 template <int NJ>
-__global__ void __launch_bounds__(kIekfThreads) k_residual_fold(DFilter* f, DScan s, int G, double eps, int do_step) {
+__global__ void __launch_bounds__(kFoldThreads) k_residual_fold(DFilter* f, DScan s, int G, double eps, int do_step) {
     using R = Red<NJ>;
     extern __shared__ __align__(16) unsigned char smem_dyn[];
     __shared__ double sH[144], sb[12];
     if (f->converged) return;  // uniform
     const int t = threadIdx.x;
-    double* s_red = reinterpret_cast<double*>(smem_dyn);
+    IekfSm& sm = *reinterpret_cast<IekfSm*>(smem_dyn);
+    double* s_red = reinterpret_cast<double*>(smem_dyn + (sizeof(IekfSm) + 15) / 16 * 16);
     if (t < R::STRIPES * R::NV) {
         const int q = t / R::NV, k = t - q * R::NV;
         double x = 0.0;
         for (int b = q; b < G; b += R::STRIPES) x = x + s.partials[b * kPartStride2 + k];
         s_red[q * R::NV + k] = x;
+    } else if (do_step && t >= kIekfThreads) {
+        iekf_boxminus(f, sm, kIekfThreads);
     }
     __syncthreads();
     double* s_sum = s_red + R::STRIPES * R::NV;
@@ -521,7 +530,7 @@ __global__ void __launch_bounds__(kIekfThreads) k_residual_fold(DFilter* f, DSca
         if (eff < 1) f->no_effect = 1;
     }
     __syncthreads();
-    if (do_step) iekf_step(f, *reinterpret_cast<IekfSm*>(smem_dyn), sH, sb, NJ, eps);
+    if (do_step) iekf_step_rest(f, sm, sH, sb, NJ, eps);
 }
 
 // P = L H^-1 L^T (ieskf.cpp:149-155) with H^-1 = M - K Hm (E^T M) of the last
@@ -634,9 +643,9 @@ void launch_residual_step(DFilter* f, DScan& s, int n_max, int estimate_ext, dou
     const int grid = residual_grid(s, n_max);
     VMP_NOTE_LAUNCH();
     if (estimate_ext)
-        k_residual_fold<12><<<1, kIekfThreads, fold_smem_bytes<12>(), st>>>(f, s, grid, eps, do_step);
+        k_residual_fold<12><<<1, kFoldThreads, fold_smem_bytes<12>(), st>>>(f, s, grid, eps, do_step);
     else
-        k_residual_fold<6><<<1, kIekfThreads, fold_smem_bytes<6>(), st>>>(f, s, grid, eps, do_step);
+        k_residual_fold<6><<<1, kFoldThreads, fold_smem_bytes<6>(), st>>>(f, s, grid, eps, do_step);
 }
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step, int from_down) {
