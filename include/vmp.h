@@ -515,7 +515,8 @@ typedef struct vmp_server_config {
     int queue_depth;            /* queued packages per stream before vmp_submit answers VMP_ERR_CAPACITY (default 64) */
     int autotune;               /* 1 (default): tune the launch shape of the served merge resolution online */
     int merge_grid_divisor;     /* served merge launches use SMs / divisor CTAs (0: 16); autotune's start */
-    int reserved[5];
+    int seg_grid_blocks;        /* working blocks of the voxel-chain kernels while the server runs (0: 304); autotune's start */
+    int reserved[4];
 } vmp_server_config;
 
 typedef struct vmp_server_result {
@@ -530,16 +531,18 @@ typedef struct vmp_server_result {
 
 void vmp_server_config_default(vmp_server_config* c);
 /* The autotuner (config.autotune, servers with more than one worker): a
- * coordinate hill climb over two scheduling knobs on windows of 128
+ * coordinate hill climb over three scheduling knobs on windows of 128
  * completed packages, starting after 24 windows (short runs keep the
  * starting shapes, the best measured ones) -- merge_grid_divisor (served
- * merge launches use SMs / d CTAs, d in 4..64; process-wide) and
- * max_inflight (packages on the GPU at once: 8, 16, 24 or 32 of the
- * workers).  Neither changes results, and neither needs the streams' scan
- * graphs captured again.  vmp_server_tuning: the merge divisor in use, the
- * windows measured so far and the best rate seen (packages/s);
- * vmp_server_knob: "merge_grid_divisor", "max_inflight" or
- * "residual_ctas_per_sm" by name. */
+ * merge launches use SMs / d CTAs, d in 4..64; process-wide), max_inflight
+ * (packages on the GPU at once: 8, 16, 24 or 32 of the workers) and
+ * seg_grid_blocks (blocks of the voxel-chain kernels that take work: 152,
+ * 304, 608, 1216 or 2432; process-wide, device-side, back to all blocks when
+ * the last server is destroyed).  None changes results, and none needs the
+ * streams' scan graphs captured again.  vmp_server_tuning: the merge divisor
+ * in use, the windows measured so far and the best rate seen (packages/s);
+ * vmp_server_knob: "merge_grid_divisor", "max_inflight", "seg_grid_blocks"
+ * or "residual_ctas_per_sm" by name. */
 vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long* windows, double* best_rate);
 vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value);
 /* The residual kernel's register budget, by hand: 3 or 4 resident CTAs per
@@ -549,10 +552,12 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value);
  * this one alone. */
 vmp_status vmp_set_residual_ctas_per_sm(int ctas);
 /* Test hook: the autotuner's climb on a model instead of a GPU (no CUDA
- * call).  rates[i * 4 + j]: packages/s with merge divisor candidate i
- * (4, 8, 16, 32, 64) and max_inflight candidate j (8, 16, 24, 32); trace
- * (2 x windows ints): both knobs after each window. */
-vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, const double* rates, int windows, int* trace);
+ * call).  rates[(i * 4 + j) * 5 + k]: packages/s with merge divisor
+ * candidate i (4, 8, 16, 32, 64), max_inflight candidate j (8, 16, 24, 32)
+ * and seg_grid_blocks candidate k (152, 304, 608, 1216, 2432); trace
+ * (3 x windows ints): the three knobs after each window. */
+vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, int seg_blocks, const double* rates, int windows,
+                             int* trace);
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out);
 /* Waits for the packages that are running; queued ones are dropped;
  * admission requests still waiting return VMP_ERR_STATE. */

@@ -230,6 +230,31 @@ def test_merge_launch_shape_does_not_change_results():
         assert maps == runs[0][1]
 
 
+def test_seg_grid_blocks_do_not_change_results():
+    """The voxel-chain kernels' working blocks (the autotuner's
+    seg_grid_blocks knob, read on the device by the captured launches): one
+    block, a few and all of them give the same results and maps, and the
+    setting is undone when the server is destroyed."""
+    from voxelmapplus_fastlio2_gb300 import _lib
+    streams = []
+    for i in range(4):
+        kind = synth.KIND_ROOM if i % 2 == 0 else synth.KIND_URBAN
+        streams.append((kind, _packages(kind, 0x5EED0000 + 300 + i, [8000, 30000, 12000, 24000][i], 7)))
+    runs = [_run_server(streams, workers=4, concurrent=True, autotune=False, seg_grid_blocks=b)
+            for b in (1, 152, 2432)]
+    for res, maps in runs[1:]:
+        assert [[k for _, k in r] for r in res] == [[k for _, k in r] for r in runs[0][0]]
+        assert maps == runs[0][1]
+    from voxelmapplus_fastlio2_gb300.serve import Server
+    srv = Server(hbm_budget_bytes=150e9, max_streams=1, workers=1)  # one worker: no throughput mode
+    try:
+        v = C.c_int()
+        assert _lib.load().vmp_server_knob(srv.h, b"seg_grid_blocks", C.byref(v)) == abi.VMP_OK
+        assert v.value == 0  # every block works again
+    finally:
+        srv.close()
+
+
 def test_autotuner_reports_state():
     from voxelmapplus_fastlio2_gb300.serve import Server
     srv = Server(hbm_budget_bytes=150e9, max_streams=2, workers=2)
@@ -237,6 +262,7 @@ def test_autotuner_reports_state():
         t = srv.tuning()
         assert t["merge_grid_divisor"] in (4, 8, 16, 32, 64) and t["windows"] == 0
         assert t["max_inflight"] == 2  # starts at the workers
+        assert t["seg_grid_blocks"] == 304
     finally:
         srv.close()
 

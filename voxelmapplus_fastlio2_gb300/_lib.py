@@ -79,7 +79,7 @@ def _declare(lib):
         "vmp_server_tuning": ([vp, P(C.c_int), P(C.c_longlong), P(d)], st),
         "vmp_server_knob": ([vp, C.c_char_p, P(C.c_int)], st),
         "vmp_set_residual_ctas_per_sm": ([C.c_int], st),
-        "vmp_test_autotune": ([C.c_int, C.c_int, vp, C.c_int, vp], st),
+        "vmp_test_autotune": ([C.c_int, C.c_int, C.c_int, vp, C.c_int, vp], st),
         "vmp_fit_planes": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp], st),
         "vmp_fit_planes_device": ([vp, vp, vp, C.c_int, C.c_longlong, P(abi.vmp_fit_params), vp, vp], st),
         "vmp_fit_profile": ([C.c_int], st),

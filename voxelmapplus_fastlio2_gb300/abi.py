@@ -134,7 +134,7 @@ def default_config(**kw):
 class vmp_server_config(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_longlong), ("max_streams", C.c_int), ("workers", C.c_int),
                 ("queue_depth", C.c_int), ("autotune", C.c_int), ("merge_grid_divisor", C.c_int),
-                ("reserved", C.c_int * 5)]
+                ("seg_grid_blocks", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class vmp_server_result(C.Structure):

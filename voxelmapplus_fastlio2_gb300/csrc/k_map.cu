@@ -36,6 +36,32 @@ static int grid_for_map(int n) {
     return b < 1 ? 1 : b;
 }
 
+// Blocks of k_seg_chain and k_seg_cov that take work.  The launches keep
+// their full grids (the scan graphs hold them); blocks from this index on
+// return at once.  Their warps take segments from a counter, so the number of
+// working blocks changes only how many voxel chains run at once, never the
+// results.  A server lowers it: a latency-bound chain of one stream then
+// holds fewer SM slots that other streams' kernels could issue from.
+__device__ int g_seg_blocks = 1 << 30;
+static std::mutex g_seg_mu;
+static int g_seg_blocks_host = 0;  // 0: every block works
+
+cudaError_t seg_set_grid_blocks(int blocks) {
+    std::lock_guard<std::mutex> lk(g_seg_mu);
+    static cudaStream_t st = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!st && (e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    const int v = blocks > 0 ? blocks : (1 << 30);
+    e = cudaMemcpyToSymbolAsync(g_seg_blocks, &v, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) g_seg_blocks_host = blocks > 0 ? blocks : 0;
+    return e;
+}
+int seg_grid_blocks() {
+    std::lock_guard<std::mutex> lk(g_seg_mu);
+    return g_seg_blocks_host;
+}
+
 // (k, RN(1 / k)) for k = 1 .. kRecipTable - 1 (the running mean's divisors
 // n + 1), written once per device from the host's correctly rounded divisions.
 constexpr int kRecipTable = 4096;
@@ -523,9 +549,10 @@ constexpr unsigned kPptI = 0x211000u, kPptJ = 0x221210u, kPptIdx = 0x854210u, kP
 __device__ __forceinline__ int ppt_field(unsigned packed, int e) { return (int)((packed >> (4 * e)) & 15u); }
 constexpr int kGroups = 3;
 
-// Slab append for the groups with `app` (all lanes call it).
+// Slab append for the groups with `app` (all lanes call it).  c0 / c1: this
+// lane's covariance entries (lanes 3-9: entry q - 3; lanes 0-1: entry 7 + q).
 __device__ inline void group_slab_append(const DMap& m, bool app, int* chunks, int& nslab, const double* p,
-                                         const double* c, int q, int gbase) {
+                                         double c0, double c1, int q, int gbase) {
     const int ci = nslab / kChunkPts;
     const bool fits = app && ci < kMaxChunks;
     const bool need = fits && (nslab % kChunkPts == 0);
@@ -545,8 +572,8 @@ __device__ inline void group_slab_append(const DMap& m, bool app, int* chunks, i
     if (fits && (!need || got)) {
         double* d = slab_pt(m, chunks, nslab);
         if (q < 3) d[q] = p[q];
-        else d[q] = c[q - 3];  // covariance entries 0-6 on lanes 3-9
-        if (q < 2) d[10 + q] = c[7 + q];
+        else d[q] = c0;  // covariance entries 0-6 on lanes 3-9
+        if (q < 2) d[10 + q] = c1;
         nslab++;
     }
 }
@@ -570,6 +597,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
     const int p_idx = ppt_field(kPptIdx, pe), p_mir = ppt_field(kPptMir, pe);
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    if ((int)blockIdx.x >= g_seg_blocks) return;  // uniform per block
     const int nseg = *d_n_seg;
     const unsigned long long base = m.cnt->batch_base;
     int* chunks = s_chunks[wib][gi];
@@ -648,6 +676,24 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             }
             n += 1;
         };
+        // The point of step jj + 1 (index, coordinates, this lane's covariance
+        // entries) is loaded during step jj, and the index of step jj + 2:
+        // the two dependent loads leave the chain's critical path.
+        uint32_t i_nx = 0, i_nx2 = 0;
+        double p_nx[3] = {0.0, 0.0, 0.0}, c0_nx = 0.0, c1_nx = 0.0;
+        auto fetch = [&](int j) {  // loads point j of the segment (j < e), index of j + 1
+            i_nx = i_nx2;
+            p_nx[0] = bpts[(size_t)i_nx * 3]; p_nx[1] = bpts[(size_t)i_nx * 3 + 1];
+            p_nx[2] = bpts[(size_t)i_nx * 3 + 2];
+            const double* c = bcov + (size_t)i_nx * 9;
+            c0_nx = (q >= 3 && q < 10) ? c[q - 3] : 0.0;
+            c1_nx = q < 2 ? c[7 + q] : 0.0;
+            if (j + 1 < e) i_nx2 = sv[j + 1];
+        };
+        if (mine && b < e) {
+            i_nx2 = sv[b];
+            fetch(b);
+        }
         if (build) {
             // VoxelMap::build: addPoint for every point, one updatePlane at the end.
             const int cnt = e - b;
@@ -655,15 +701,14 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
             for (int jj = 0;; ++jj) {
                 const bool act = mine && b + jj < e;
                 if (!__any_sync(0xffffffffu, act)) break;
-                double p[3] = {0.0, 0.0, 0.0};
-                const double* c = bcov;
+                double p[3] = {0.0, 0.0, 0.0}, c0 = 0.0, c1 = 0.0;
                 if (act) {
-                    const uint32_t i = sv[b + jj];
-                    p[0] = bpts[(size_t)i * 3]; p[1] = bpts[(size_t)i * 3 + 1]; p[2] = bpts[(size_t)i * 3 + 2];
-                    c = bcov + (size_t)i * 9;
+                    p[0] = p_nx[0]; p[1] = p_nx[1]; p[2] = p_nx[2];
+                    c0 = c0_nx; c1 = c1_nx;
+                    if (b + jj + 1 < e) fetch(b + jj + 1);
                     add_point(p);
                 }
-                group_slab_append(m, act && store, chunks, nslab, p, c, q, gbase);
+                group_slab_append(m, act && store, chunks, nslab, p, c0, c1, q, gbase);
             }
             if (mine) {
                 if (!store) flags |= F_DROPPED;
@@ -686,16 +731,16 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_chain(DMap m, const uint32_
                     act = false;
                 }
                 if (!__any_sync(0xffffffffu, act)) break;
-                double p[3] = {0.0, 0.0, 0.0};
-                const double* c = bcov;
+                double p[3] = {0.0, 0.0, 0.0}, c0 = 0.0, c1 = 0.0;
                 uint32_t i = 0;
                 if (act) {
-                    i = sv[b + jj];
-                    p[0] = bpts[(size_t)i * 3]; p[1] = bpts[(size_t)i * 3 + 1]; p[2] = bpts[(size_t)i * 3 + 2];
-                    c = bcov + (size_t)i * 9;
+                    i = i_nx;
+                    p[0] = p_nx[0]; p[1] = p_nx[1]; p[2] = p_nx[2];
+                    c0 = c0_nx; c1 = c1_nx;
+                    if (b + jj + 1 < e) fetch(b + jj + 1);
                     add_point(p);
                 }
-                group_slab_append(m, act && !(flags & F_DROPPED), chunks, nslab, p, c, q, gbase);
+                group_slab_append(m, act && !(flags & F_DROPPED), chunks, nslab, p, c0, c1, q, gbase);
                 if (act) {
                     if (!init) {
                         refit(nslab, 0);
@@ -877,6 +922,7 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t*
                                                          const double* __restrict__ bcov, uint32_t* ev_rec,
                                                          SegScratch ss) {
     __shared__ CovShared sh;
+    if ((int)blockIdx.x >= g_seg_blocks) return;  // uniform per block
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -1065,7 +1111,8 @@ void launch_map_segments(DMap& m, MapScratch& ms, int n_max, cudaStream_t st) {
 void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double* bcov, int n_max, bool build,
                       cudaStream_t st) {
     // warps take their work from counters; the grids keep enough warps for
-    // the longest chains to start at once
+    // the longest chains to start at once (of them, the first g_seg_blocks
+    // blocks work)
     int sg = (n_max + (kSegThreads / 32) - 1) / (kSegThreads / 32);
     if (sg > 152 * 16) sg = 152 * 16;
     if (sg < 1) sg = 1;

@@ -685,6 +685,11 @@ void merge_set_grid_divisor(int d) {
     g_coop_divisor = d < 1 ? 1 : (d > 1024 ? 1024 : d);
 }
 
+bool merge_throughput_mode() {
+    std::lock_guard<std::mutex> lk(g_coop_mu);
+    return g_coop_throughput;
+}
+
 void merge_set_throughput_mode(bool on) {
     std::lock_guard<std::mutex> lk(g_coop_mu);
     g_coop_throughput_refs += on ? 1 : -1;

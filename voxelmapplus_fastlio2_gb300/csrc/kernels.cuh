@@ -182,6 +182,10 @@ int merge_profile_read(void* scratch, cudaStream_t st, double* us, int max);
 // fewer), cooperative merge launches use 1/16 of the SMs and run several at
 // once instead of one at a time on all SMs.
 void merge_set_throughput_mode(bool on);
+bool merge_throughput_mode();
+// working blocks of the voxel-chain kernels (0: all); process-wide, device-side
+cudaError_t seg_set_grid_blocks(int blocks);
+int seg_grid_blocks();
 // Served merge launches use SMs / d CTAs (process-wide; 16 by default).
 void merge_set_grid_divisor(int d);
 // Writes the reciprocal table of the voxel state machine on the current

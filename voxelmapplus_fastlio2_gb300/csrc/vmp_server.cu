@@ -28,7 +28,10 @@
 
 namespace vmp {
 void merge_set_throughput_mode(bool on);
+bool merge_throughput_mode();
 void merge_set_grid_divisor(int d);
+cudaError_t seg_set_grid_blocks(int blocks);
+int seg_grid_blocks();
 void residual_set_ctas_per_sm(int c);
 int residual_ctas_per_sm();
 }
@@ -119,13 +122,17 @@ struct KnobClimb {
 // other (coordinate-wise), then the shapes are kept for kExploit windows
 // before the next round of climbs (the stream mix may have changed).  The
 // first climb starts after kFirst windows (about 3 000 packages), so that
-// short runs stay on the starting shapes, the best measured ones.  Both
-// knobs change scheduling only, never results, and neither needs the
-// streams' captured scan graphs to be captured again:
+// short runs stay on the starting shapes, the best measured ones.  The
+// knobs change scheduling only, never results, and none needs the streams'
+// captured scan graphs to be captured again:
 //   merge_grid_divisor  served merge launches use SMs / d CTAs;
 //   max_inflight        packages on the GPU at once (of the workers' slots):
 //                       fewer contend less for the hardware work queues,
-//                       more overlap more.
+//                       more overlap more;
+//   seg_grid_blocks     blocks of the voxel-chain kernels that take work
+//                       (a device-side value the captured launches read):
+//                       fewer leave more SM slots to other streams' kernels,
+//                       more run more of one scan's chains at once.
 struct Autotuner {
     static constexpr int kWindow = 128, kSettle = 16, kExploit = 32, kFirst = 24;
     std::vector<KnobClimb> knobs;
@@ -178,18 +185,24 @@ struct Autotuner {
 };
 
 static void apply_merge_divisor(int d) { vmp::merge_set_grid_divisor(d); }
+static void apply_seg_blocks(int b) { (void)vmp::seg_set_grid_blocks(b); }
 // the launch shapes of vmp_test_autotune's model (one caller at a time)
-static int g_model_d = 0, g_model_c = 0;
+static int g_model_d = 0, g_model_c = 0, g_model_s = 0;
 static void model_set_d(int d) { g_model_d = d; }
 static void model_set_c(int c) { g_model_c = c; }
+static void model_set_s(int b) { g_model_s = b; }
 
-static Autotuner make_tuner(int merge_divisor, int inflight, std::function<void(int)> set_d,
-                            std::function<void(int)> set_c) {
+constexpr int kDefaultSegBlocks = 304;  // 2 per SM: the best of 152 .. 2432 on the 64-stream mix
+
+static Autotuner make_tuner(int merge_divisor, int inflight, int seg_blocks, std::function<void(int)> set_d,
+                            std::function<void(int)> set_c, std::function<void(int)> set_s) {
     Autotuner t;
     t.knobs.push_back(KnobClimb{"merge_grid_divisor", {4, 8, 16, 32, 64}, set_d});
     t.knobs.push_back(KnobClimb{"max_inflight", {8, 16, 24, 32}, set_c});
+    t.knobs.push_back(KnobClimb{"seg_grid_blocks", {152, 304, 608, 1216, 2432}, set_s});
     t.knobs[0].set_nearest(merge_divisor);
     t.knobs[1].set_nearest(inflight);
+    t.knobs[2].set_nearest(seg_blocks);
     return t;
 }
 
@@ -197,6 +210,7 @@ struct vmp_server_s {
     vmp_server_config cfg{};
     Autotuner tuner;
     int fixed_divisor = 16;
+    int fixed_seg_blocks = kDefaultSegBlocks;
     std::mutex mu;
     std::condition_variable cv_work;  // workers: a package is ready / stop
     std::condition_variable cv_done;  // pollers, close / destroy: a package finished
@@ -313,6 +327,7 @@ void vmp_server_config_default(vmp_server_config* c) {
     c->queue_depth = 64;
     c->autotune = 1;
     c->merge_grid_divisor = 16;
+    c->seg_grid_blocks = kDefaultSegBlocks;
 }
 
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
@@ -339,16 +354,19 @@ vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out) {
     if (cfg.workers > 1) {
         vmp::merge_set_throughput_mode(true);
         const int d0 = cfg.merge_grid_divisor > 0 ? cfg.merge_grid_divisor : 16;
+        const int s0 = cfg.seg_grid_blocks > 0 ? cfg.seg_grid_blocks : kDefaultSegBlocks;
         vmp::merge_set_grid_divisor(d0);
+        apply_seg_blocks(s0);
         if (cfg.autotune) {  // the climbs start at the candidates nearest the configured shapes
             // (applied under the server lock: the tuner runs in on_done, called with it held)
-            sv->tuner = make_tuner(d0, cfg.workers, apply_merge_divisor, [sv](int c) {
+            sv->tuner = make_tuner(d0, cfg.workers, s0, apply_merge_divisor, [sv](int c) {
                 sv->max_inflight = c;
                 sv->cv_work.notify_all();
-            });
+            }, apply_seg_blocks);
             sv->tuner.apply_all();
         }
         sv->fixed_divisor = d0;
+        sv->fixed_seg_blocks = s0;
     }
     for (int i = 0; i < cfg.workers; ++i) sv->workers.emplace_back([sv] { sv->worker(); });
     *out = sv;
@@ -379,7 +397,10 @@ vmp_status vmp_server_destroy(vmp_server_t sv) {
     for (auto& t : sv->workers) t.join();
     for (auto& s : sv->slots)
         if (s.h) vmp_destroy(s.h);
-    if (sv->cfg.workers > 1) vmp::merge_set_throughput_mode(false);
+    if (sv->cfg.workers > 1) {
+        vmp::merge_set_throughput_mode(false);
+        if (!vmp::merge_throughput_mode()) apply_seg_blocks(0);  // the last server: every block works again
+    }
     delete sv;
     return VMP_OK;
 }
@@ -605,6 +626,12 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value) {
         *value = sv->cfg.autotune && sv->cfg.workers > 1 ? sv->tuner.value(name) : sv->fixed_divisor;
         return VMP_OK;
     }
+    if (std::strcmp(name, "seg_grid_blocks") == 0) {
+        *value = sv->cfg.workers <= 1 ? vmp::seg_grid_blocks()
+                 : sv->cfg.autotune  ? sv->tuner.value(name)
+                                     : sv->fixed_seg_blocks;
+        return VMP_OK;
+    }
     if (std::strcmp(name, "max_inflight") == 0) {
         *value = sv->max_inflight < sv->cfg.workers ? sv->max_inflight : sv->cfg.workers;
         return VMP_OK;
@@ -617,12 +644,15 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value) {
 }
 
 // Test hook: the autotuner's climb on a model throughput instead of a GPU.
-// rates[i * 2 + j]: packages/s with merge divisor candidate i (4, 8, 16, 32,
-// 64) and max_inflight candidate j (8, 16, 24, 32); completions are spaced
-// by 1 / rate.  trace[2 * w], trace[2 * w + 1]: the two knobs after window w.
-vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, const double* rates, int windows, int* trace) {
+// rates[(i * 4 + j) * 5 + k]: packages/s with merge divisor candidate i (4,
+// 8, 16, 32, 64), max_inflight candidate j (8, 16, 24, 32) and
+// seg_grid_blocks candidate k (152, 304, 608, 1216, 2432); completions are
+// spaced by 1 / rate.  trace[3 * w .. 3 * w + 2]: the three knobs after
+// window w.
+vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, int seg_blocks, const double* rates, int windows,
+                             int* trace) {
     if (!rates || !trace || windows < 0) return VMP_ERR_INVALID_ARG;
-    Autotuner t = make_tuner(merge_divisor, max_inflight, model_set_d, model_set_c);
+    Autotuner t = make_tuner(merge_divisor, max_inflight, seg_blocks, model_set_d, model_set_c, model_set_s);
     t.apply_all();
     double now = 0.0;
     for (int w = 0; w < windows;) {
@@ -632,14 +662,18 @@ vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, const double* 
         int ci = 0;
         for (int i = 0; i < (int)t.knobs[1].cand.size(); ++i)
             if (t.knobs[1].cand[i] == g_model_c) ci = i;
-        const double r = rates[di * 4 + ci];
+        int si = 0;
+        for (int i = 0; i < (int)t.knobs[2].cand.size(); ++i)
+            if (t.knobs[2].cand[i] == g_model_s) si = i;
+        const double r = rates[(di * 4 + ci) * 5 + si];
         if (!(r > 0.0)) return VMP_ERR_INVALID_ARG;
         now += 1000.0 / r;
         const long long before = t.windows;
         t.on_done(now);
         if (t.windows != before) {
-            trace[2 * w] = g_model_d;
-            trace[2 * w + 1] = g_model_c;
+            trace[3 * w] = g_model_d;
+            trace[3 * w + 1] = g_model_c;
+            trace[3 * w + 2] = g_model_s;
             ++w;
         }
     }

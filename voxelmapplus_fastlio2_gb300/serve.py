@@ -16,7 +16,7 @@ from .lio import LIOBuilder
 
 class Server:
     def __init__(self, hbm_budget_bytes=150e9, max_streams=64, workers=32, queue_depth=64, autotune=True,
-                 merge_grid_divisor=16):
+                 merge_grid_divisor=16, seg_grid_blocks=304):
         self.lib = load()
         cfg = abi.vmp_server_config()
         self.lib.vmp_server_config_default(C.byref(cfg))
@@ -26,6 +26,7 @@ class Server:
         cfg.queue_depth = int(queue_depth)
         cfg.autotune = 1 if autotune else 0
         cfg.merge_grid_divisor = int(merge_grid_divisor)
+        cfg.seg_grid_blocks = int(seg_grid_blocks)
         h = C.c_void_p()
         code = self.lib.vmp_server_create(C.byref(cfg), C.byref(h))
         if code != abi.VMP_OK:
@@ -105,10 +106,11 @@ class Server:
         """The online autotuner's state (vmp_server_tuning)."""
         d, w, r = C.c_int(), C.c_longlong(), C.c_double()
         self._check(self.lib.vmp_server_tuning(self.h, C.byref(d), C.byref(w), C.byref(r)), "vmp_server_tuning")
-        k = C.c_int()
+        k, b = C.c_int(), C.c_int()
         self._check(self.lib.vmp_server_knob(self.h, b"max_inflight", C.byref(k)), "vmp_server_knob")
-        return {"merge_grid_divisor": d.value, "max_inflight": k.value, "windows": w.value,
-                "best_rate": r.value}
+        self._check(self.lib.vmp_server_knob(self.h, b"seg_grid_blocks", C.byref(b)), "vmp_server_knob")
+        return {"merge_grid_divisor": d.value, "max_inflight": k.value, "seg_grid_blocks": b.value,
+                "windows": w.value, "best_rate": r.value}
 
     def close(self):
         if getattr(self, "h", None):
