@@ -545,8 +545,9 @@ void vmp_server_config_default(vmp_server_config* c);
  * or "residual_ctas_per_sm" by name. */
 vmp_status vmp_server_tuning(vmp_server_t sv, int* merge_grid_divisor, long long* windows, double* best_rate);
 vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value);
-/* The residual kernel's register budget, by hand: 3 or 4 resident CTAs per
- * SM (process-wide; VMP_RESIDUAL_CTAS_PER_SM gives the value at load).  The
+/* The residual kernel's register budget, by hand: 3 or 4 (default) resident
+ * CTAs per SM (process-wide; VMP_RESIDUAL_CTAS_PER_SM gives the value at
+ * load).  The
  * results are the same; the streams' scan graphs are captured again at their
  * next scan, which costs milliseconds per stream, so the online tuner leaves
  * this one alone. */

@@ -212,7 +212,7 @@ def test_residual_register_budget_does_not_change_results():
             runs.append(res)
             g.close()
     finally:
-        lib.vmp_set_residual_ctas_per_sm(3)
+        lib.vmp_set_residual_ctas_per_sm(4)  # the default
     assert runs[1] == runs[0] and runs[2] == runs[0]
 
 

@@ -578,11 +578,13 @@ void launch_update_begin(DFilter* f, cudaStream_t st) {
     k_update_begin<<<1, 64, 0, st>>>(f);
 }
 // Resident CTAs per SM that k_residual is compiled for (register budget):
-// 3 (no spills) or 4 (64 registers); the arithmetic is the same either way.
-// The serving autotuner sets it (VMP_RESIDUAL_CTAS_PER_SM gives the start);
-// a change bumps the launch-shape epoch, so that captured scan graphs are
-// captured again with the new kernel.
-static std::atomic<int> g_residual_minb{3};
+// 3 (80 registers, no spills) or 4 (64 registers, a few spilled words); the
+// arithmetic is the same either way.  4 by default: one stream runs as fast
+// with either, and beside other streams' kernels the smaller budget leaves
+// them register file.  VMP_RESIDUAL_CTAS_PER_SM (at load) and
+// vmp_set_residual_ctas_per_sm set it; a change bumps the launch-shape epoch,
+// so that captured scan graphs are captured again with the new kernel.
+static std::atomic<int> g_residual_minb{4};
 static std::atomic<long long> g_shape_epoch{0};
 
 void residual_set_ctas_per_sm(int c) {
@@ -599,7 +601,7 @@ static cudaError_t set_residual_smem() {
 }
 cudaError_t residual_setup() {
     static const bool from_env = [] {
-        if (const char* v = std::getenv("VMP_RESIDUAL_CTAS_PER_SM")) g_residual_minb = std::atoi(v) == 4 ? 4 : 3;
+        if (const char* v = std::getenv("VMP_RESIDUAL_CTAS_PER_SM")) g_residual_minb = std::atoi(v) == 3 ? 3 : 4;
         return true;
     }();
     (void)from_env;

@@ -873,8 +873,9 @@ __device__ inline const double* term_point(const DMap& m, const RefitSnap& sn, i
 constexpr int kTermThreads = 128;
 
 // Every covariance term of every plane refit, one per thread (the terms of
-// all refits of the batch packed densely over the lanes).
-__global__ void __launch_bounds__(kTermThreads) k_cov_terms(DMap m, const uint32_t* __restrict__ seg_start,
+// all refits of the batch packed densely over the lanes).  Register budget:
+// 5 CTAs per SM (96 registers instead of 112).
+__global__ void __launch_bounds__(kTermThreads, 5) k_cov_terms(DMap m, const uint32_t* __restrict__ seg_start,
                                                            const uint32_t* __restrict__ sv,
                                                            const double* __restrict__ bpts,
                                                            const double* __restrict__ bcov, SegScratch ss) {
@@ -913,8 +914,9 @@ struct CovShared {
 
 // Per voxel with refits: the plane covariance sums in point order (terms from
 // the term buffer, or formed here when they did not fit), normal and centre
-// of the last plane refit, merge calls.
-__global__ void __launch_bounds__(kSegThreads) k_seg_cov(DMap m, const uint32_t* __restrict__ seg_start,
+// of the last plane refit, merge calls.  Register budget: 6 CTAs per SM (80
+// registers instead of 152; its warps mostly wait on a serial sum).
+__global__ void __launch_bounds__(kSegThreads, 6) k_seg_cov(DMap m, const uint32_t* __restrict__ seg_start,
                                                          const uint32_t* __restrict__ seg_end,
                                                          const uint32_t* __restrict__ seg_rec,
                                                          const uint32_t* __restrict__ sv,
