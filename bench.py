@@ -209,17 +209,18 @@ TRAFFIC_PER_UNIT = {
 
 
 # FP64 warp instructions (ncu sm__inst_executed_pipe_fp64.sum) per unit of
-# work of the FP64-bound phases, from the same urban-block capture (one
-# steady scan, 50k rays).  These phases are bound by the FP64 pipe, not by
+# work of the FP64-bound phases: means over six steady scans of the 200k-ray
+# urban block (a one-pass capture of this bench's own urban workload).
+# These phases are bound by the FP64 pipe, not by
 # HBM: an FP64 warp instruction holds an SM sub-partition's FP64 pipe for 64
 # cycles whatever its active lanes (a dependent-DFMA micro-probe on this
 # GB300), so the pipe's peak is 4 x SMs x clock / 64 warp instructions/s.
 FP64_PER_UNIT = {
-    "residual": 4.71,   # per downsampled point x IEKF iteration (k_residual<6, 3>: 196.9 k on 41.8 k points)
+    "residual": 5.81,   # per downsampled point x IEKF iteration
     "undistort": 7.11,  # per raw point
-    "body_cov": 6.22,   # per downsampled point
-    "map_batch": 5.57,  # per batch point
-    "map_state": 18.3,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov
+    "body_cov": 6.21,   # per downsampled point
+    "map_batch": 5.59,  # per batch point
+    "map_state": 23.2,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov (19.0-25.6)
 }
 FP64_CYCLES_PER_WARP_INSTR = 64
 
