@@ -349,9 +349,8 @@ vmp_status vmp_test_hat_sandwich(const double* pts, const double* M, int n, doub
  * fixed 2 MiB __device__ array inside libvmp, held by every GPU that loads
  * the library until exit; at most 65536 input points (VMP_ERR_CAPACITY above
  * that).  The call allocates nothing.  Its first call on a device resolves
- * the array's device address, so make that first call before any stream
- * capture; the address is kept for the process, so cudaDeviceReset while
- * libvmp is loaded is not supported.  Calls share the array: calls that
+ * the array's device address and keeps it for the process, so
+ * cudaDeviceReset while libvmp is loaded is not supported.  Calls share the array: calls that
  * overlap on the GPU race and must be serialised by the caller.  cuda_stream
  * may be NULL (default stream); the call returns after that stream
  * finished. */

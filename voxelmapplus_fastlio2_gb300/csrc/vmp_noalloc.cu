@@ -14,8 +14,9 @@
 // Every GPU that loads libvmp.so holds that array until the process exits.
 // In host code the array's name is only a host-side handle, not a device
 // address: the first call on each device (with that device current) resolves
-// the device address with cudaGetSymbolAddress and caches it, so that first
-// call should come before any stream capture.  The cached address belongs to
+// the device address with cudaGetSymbolAddress and caches it.  Every call
+// ends by reading the output count back and synchronising its stream.  The
+// cached address belongs to
 // the device's context of that moment: cudaDeviceReset while libvmp is loaded
 // is not supported.  All calls share the one array: two calls whose work
 // overlaps on the GPU race on it and must be serialised by the caller (same
