@@ -201,8 +201,8 @@ def load_peaks():
 # voxels / 13.16 M points for the fit.  The traffic grows in proportion to
 # the units, so a launch's traffic is this times its units.
 TRAFFIC_PER_UNIT = {
-    "residual": 138.0,   # per downsampled point x IEKF iteration (k_residual<6, 3>)
-    "map_state": 996.0,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov
+    "residual": 138.0,   # per downsampled point x IEKF iteration (k_residual<6, 4>)
+    "map_state": 534.0,  # per inserted point: k_seg_chain + k_refit_eig + k_cov_terms + k_seg_cov
     "undistort": 17.3,   # per raw point
     "fit_fp32c": 51.5,   # per point
 }
