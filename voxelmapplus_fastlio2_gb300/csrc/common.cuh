@@ -95,6 +95,10 @@ struct DFilter {
     double delta[23];
     double Hm[144];
     double bm[12];
+    // x boxminus x_pred of the current IEKF iteration and its block-diagonal
+    // inverse Jacobian (rot 3x3, rot_ext 3x3, S2 2x2), from k_iekf_boxminus
+    double bmx_d[23];
+    double bmx_D[22];
     double last_acc[3], last_gyro[3];
     double last_cloud_end_time;
     double gravity_norm;

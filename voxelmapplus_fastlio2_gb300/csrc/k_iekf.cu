@@ -260,10 +260,10 @@ __device__ inline int lin_delta_idx(int u) { return u < 3 ? u : u + 6; }
 // parts.  iekf_boxminus: delta = x boxminus x_pred and D = J^-1, the
 // transcendental pieces on separate warps (thread `base`: rot, base + 32:
 // rot_ext, base + 64: the S2 block, base + 96 .. 110: the linear
-// coordinates); it needs nothing of the measurement, so it runs beside the
-// fold of the block partials.  iekf_step_rest: the rest, after a
-// __syncthreads.  H / b of the measurement (nj x nj, nj) are in shared
-// memory.  One CTA.
+// coordinates); it needs nothing of the measurement, so it runs in its own
+// kernel (k_iekf_boxminus) beside the iteration's point kernel.
+// iekf_step_rest: the rest, in the fold kernel after its fold.  H / b of the
+// measurement (nj x nj, nj) are in shared memory.  One CTA.
 __device__ void iekf_boxminus(const DFilter* f, IekfSm& s, int base) {
     const int t = threadIdx.x;
     const DState& x = f->x;
@@ -359,6 +359,22 @@ __device__ void iekf_step_rest(DFilter* f, IekfSm& s, const double* Hm, const do
 }
 
 // ---------------------------------------------------------------- kernels
+// The boxminus part of an iteration's step (x boxminus x_pred and D = J^-1),
+// one CTA of 128 threads.  It reads only x and x_pred, so it runs beside the
+// iteration's point kernel (on a side stream) and the fold kernel reads its
+// result: its transcendentals leave the fold's critical path.
+__global__ void __launch_bounds__(128) k_iekf_boxminus(DFilter* f) {
+    __shared__ IekfSm sm;
+    if (f->converged) return;  // uniform
+    iekf_boxminus(f, sm, 0);
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t < 23) f->bmx_d[t] = sm.d[t];
+    else if (t < 32) f->bmx_D[t - 23] = sm.D.r[t - 23];
+    else if (t < 41) f->bmx_D[9 + t - 32] = sm.D.e[t - 32];
+    else if (t < 45) f->bmx_D[18 + t - 41] = sm.D.g[t - 41];
+}
+
 // IESKF::update entry (ieskf.cpp:125-130): predict_x = x, delta = 0.
 __global__ void k_update_begin(DFilter* f) {
     const int t = threadIdx.x;
@@ -384,7 +400,7 @@ constexpr size_t residual_smem_bytes() {
     return rows > fold ? rows : fold;
 }
 // ... and of k_residual_fold<NJ>: the filter step's scratch, then the stripes.
-constexpr int kFoldThreads = 384;  // warps 0-7 fold, warps 8-11 boxminus
+constexpr int kFoldThreads = kIekfThreads;
 template <int NJ>
 constexpr size_t fold_smem_bytes() {
     using R = Red<NJ>;
@@ -494,13 +510,17 @@ __global__ void __launch_bounds__(kFoldThreads) k_residual_fold(DFilter* f, DSca
     const int t = threadIdx.x;
     IekfSm& sm = *reinterpret_cast<IekfSm*>(smem_dyn);
     double* s_red = reinterpret_cast<double*>(smem_dyn + (sizeof(IekfSm) + 15) / 16 * 16);
+    if (do_step) {  // k_iekf_boxminus's result
+        if (t < 23) sm.d[t] = f->bmx_d[t];
+        else if (t < 32) sm.D.r[t - 23] = f->bmx_D[t - 23];
+        else if (t < 41) sm.D.e[t - 32] = f->bmx_D[9 + t - 32];
+        else if (t < 45) sm.D.g[t - 41] = f->bmx_D[18 + t - 41];
+    }
     if (t < R::STRIPES * R::NV) {
         const int q = t / R::NV, k = t - q * R::NV;
         double x = 0.0;
         for (int b = q; b < G; b += R::STRIPES) x = x + s.partials[b * kPartStride2 + k];
         s_red[q * R::NV + k] = x;
-    } else if (do_step && t >= kIekfThreads) {
-        iekf_boxminus(f, sm, kIekfThreads);
     }
     __syncthreads();
     double* s_sum = s_red + R::STRIPES * R::NV;
@@ -649,8 +669,13 @@ void launch_residual_step(DFilter* f, DScan& s, int n_max, int estimate_ext, dou
     else
         k_residual_fold<6><<<1, kFoldThreads, fold_smem_bytes<6>(), st>>>(f, s, grid, eps, do_step);
 }
+void launch_iekf_boxminus(DFilter* f, cudaStream_t st) {
+    VMP_NOTE_LAUNCH();
+    k_iekf_boxminus<<<1, 128, 0, st>>>(f);
+}
 void launch_residual_iter(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, double eps,
                           cudaStream_t st, int do_step, int from_down) {
+    if (do_step) launch_iekf_boxminus(f, st);
     launch_residual_points(f, s, m, n_max, estimate_ext, st, from_down);
     launch_residual_step(f, s, n_max, estimate_ext, eps, st, do_step);
 }

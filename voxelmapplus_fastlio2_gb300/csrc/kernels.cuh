@@ -78,10 +78,13 @@ void residual_set_ctas_per_sm(int c);
 int residual_ctas_per_sm();
 // Bumped whenever a launch shape that captured graphs hold changes.
 long long launch_shape_epoch();
-// One IEKF iteration: launch_residual_points (sharedUpdateFunc over the points,
-// block partials of H / b) then launch_residual_step (their fold and, with
-// do_step, the filter step).  from_down: LiDAR points from the downsampled
-// cloud (s.down), else from s.pl.
+// One IEKF iteration: launch_iekf_boxminus (with do_step: x boxminus x_pred
+// and its inverse Jacobian; it may run on another stream beside the points),
+// launch_residual_points (sharedUpdateFunc over the points, block partials of
+// H / b), then launch_residual_step (their fold and, with do_step, the filter
+// step).  from_down: LiDAR points from the downsampled cloud (s.down), else
+// from s.pl.
+void launch_iekf_boxminus(DFilter* f, cudaStream_t st);
 void launch_residual_points(DFilter* f, DScan& s, const DMap& m, int n_max, int estimate_ext, cudaStream_t st,
                             int from_down);
 void launch_residual_step(DFilter* f, DScan& s, int n_max, int estimate_ext, double eps, cudaStream_t st,

@@ -961,12 +961,23 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     launch_update_begin(s->f, st);
     s->pend(VMP_PROF_UPDATE_OTHER, -1);
     for (int it = 0; it < cfg.ieskf_max_iter; ++it) {
-        s->pbeg();
-        launch_residual_points(s->f, s->s, s->m, nb, cfg.estimate_ext, st, 1);
-        s->pend(VMP_PROF_RESIDUAL, 1);
-        s->pbeg();
-        launch_residual_step(s->f, s->s, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
-        s->pend(VMP_PROF_RESIDUAL_STEP, -1);
+        if (s->prof_on) {  // one phase after the other: the boxminus is timed with the step
+            s->pbeg();
+            launch_residual_points(s->f, s->s, s->m, nb, cfg.estimate_ext, st, 1);
+            s->pend(VMP_PROF_RESIDUAL, 1);
+            s->pbeg();
+            launch_iekf_boxminus(s->f, st);
+            launch_residual_step(s->f, s->s, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+            s->pend(VMP_PROF_RESIDUAL_STEP, -1);
+        } else {  // the boxminus beside the point kernel, joined before the fold
+            cudaEventRecord(s->ev_fork, st);
+            cudaStreamWaitEvent(s->st_side, s->ev_fork, 0);
+            launch_iekf_boxminus(s->f, s->st_side);
+            cudaEventRecord(s->ev_join, s->st_side);
+            launch_residual_points(s->f, s->s, s->m, nb, cfg.estimate_ext, st, 1);
+            cudaStreamWaitEvent(st, s->ev_join, 0);
+            launch_residual_step(s->f, s->s, nb, cfg.estimate_ext, cfg.ieskf_eps, st, 1);
+        }
     }
     s->pbeg();
     launch_update_end(s->f, cfg.estimate_ext, st);
