@@ -16,6 +16,11 @@
 //     structural non-zero terms in k order -- the same value as the dense
 //     product -- one warp per row with the lanes over the other index;
 //     the G Q G^T blocks (Q diagonal) are precomputed per step.
+// Two kernels: k_predict_chain2 (the state chain, the per-step F / G data and
+// the pose cache the undistortion needs) and k_predict_cov (the covariance
+// chain over that per-step data).  Nothing reads P before the first residual
+// kernel (its gate), so the second runs beside the undistortion,
+// downsampling and body covariances.
 #include "kernels.cuh"
 
 namespace vmp {
@@ -124,9 +129,6 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
                                                                  DStep* st) {
     const int n_imu = hdr->n_imu;
     const double t_begin = hdr->t_start, t_end = hdr->t_end;
-    __shared__ double sP[2][529];
-    __shared__ double sFP[529];
-    __shared__ StepSm sStep[2];
     __shared__ double sNM[4], sMx[6], sQd[12];
     __shared__ double sBg[3], sBa[3], sG[3], sRot0[9], sVel0[3], sPos0[3], sRotF[9], sVelF[3], sPosF[3];
     __shared__ int sPosOf[1024];
@@ -135,7 +137,6 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
     if (n_imu > 1024) return;  // bounded by max_imu_per_scan (<= 1000) on the host
     const double last_end = f->last_cloud_end_time;
     const double gn = f->gravity_norm;
-    for (int e = t; e < 529; e += blockDim.x) sP[0][e] = f->P[e];
     if (t < 12) sQd[t] = f->Q[t * 13];
     if (t < 3) {
         sBg[t] = f->x.bg[t]; sBa[t] = f->x.ba[t]; sG[t] = f->x.g[t];
@@ -293,7 +294,45 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
         }
         for (int q = 0; q < 9; ++q) p0.rot[q] = sRot0[q];
     }
-    // ---- phase 4: covariance chain P = F P F^T + G Q G^T
+    // ---- write back (the covariance chain is k_predict_cov)
+    __syncthreads();
+    if (t == 0) {
+        DState& x = f->x;
+        for (int q = 0; q < 9; ++q) x.rot[q] = sRotF[q];
+        for (int a = 0; a < 3; ++a) { x.vel[a] = sVelF[a]; x.pos[a] = sPosF[a]; }
+        f->npose = S + 1;
+        if (S > 0) {
+            for (int a = 0; a < 3; ++a) {
+                f->last_acc[a] = poses[S].acc[a];
+                f->last_gyro[a] = poses[S].gyro[a];
+                f->inp_acc[a] = st[S - 1].acc[a];
+                f->inp_gyro[a] = st[S - 1].gyro[a];
+            }
+        }
+        const vmp_imu& last = imus[n_imu - 1];
+        f->last_imu_t = last.t;
+        for (int a = 0; a < 3; ++a) { f->last_imu_acc[a] = last.acc[a]; f->last_imu_gyro[a] = last.gyro[a]; }
+        f->last_cloud_end_time = t_end;
+    }
+}
+
+// The covariance chain P = F P F^T + G Q G^T over the steps k_predict_chain2
+// wrote (f->npose of them), with the F / G data of each step staged in shared
+// memory while the previous step runs.
+__global__ void __launch_bounds__(kPredThreads) k_predict_cov(DFilter* f, const DStep* __restrict__ st) {
+    __shared__ double sP[2][529];
+    __shared__ double sFP[529];
+    __shared__ StepSm sStep[2];
+    __shared__ double sNM[4];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int NS = f->npose;
+    for (int e = t; e < 529; e += blockDim.x) sP[0][e] = f->P[e];
+    if (t == 0) {  // the S2 block of F: N(g) M(g) (g does not change while predicting)
+        double Nx[6], Mx[6];
+        s2_Mx(f->x.g, Mx);
+        s2_Nx(f->x.g, Nx);
+        mm<2, 3, 2>(Nx, Mx, sNM);
+    }
     if (t < 67) stage_step(sStep[0], st[0], t);
     __syncthreads();
     int cur = 0;
@@ -328,30 +367,18 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
         __syncthreads();
         cur ^= 1;
     }
-    // ---- write back
     for (int e = t; e < 529; e += blockDim.x) f->P[e] = sP[cur][e];
-    if (t == 0) {
-        DState& x = f->x;
-        for (int q = 0; q < 9; ++q) x.rot[q] = sRotF[q];
-        for (int a = 0; a < 3; ++a) { x.vel[a] = sVelF[a]; x.pos[a] = sPosF[a]; }
-        f->npose = S + 1;
-        if (S > 0) {
-            for (int a = 0; a < 3; ++a) {
-                f->last_acc[a] = poses[S].acc[a];
-                f->last_gyro[a] = poses[S].gyro[a];
-                f->inp_acc[a] = st[S - 1].acc[a];
-                f->inp_gyro[a] = st[S - 1].gyro[a];
-            }
-        }
-        const vmp_imu& last = imus[n_imu - 1];
-        f->last_imu_t = last.t;
-        for (int a = 0; a < 3; ++a) { f->last_imu_acc[a] = last.acc[a]; f->last_imu_gyro[a] = last.gyro[a]; }
-        f->last_cloud_end_time = t_end;
-    }
 }
 
-void launch_predict_chain2(DFilter* f, DScan& s, cudaStream_t st) {
+void launch_predict_state(DFilter* f, DScan& s, cudaStream_t st) {
     VMP_NOTE_LAUNCH(); k_predict_chain2<<<1, kPredThreads, 0, st>>>(f, s.imus, s.hdr, s.poses, s.steps);
+}
+void launch_predict_cov(DFilter* f, DScan& s, cudaStream_t st) {
+    VMP_NOTE_LAUNCH(); k_predict_cov<<<1, kPredThreads, 0, st>>>(f, s.steps);
+}
+void launch_predict_chain2(DFilter* f, DScan& s, cudaStream_t st) {
+    launch_predict_state(f, s, st);
+    launch_predict_cov(f, s, st);
 }
 
 }  // namespace vmp

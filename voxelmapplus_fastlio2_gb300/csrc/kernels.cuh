@@ -68,6 +68,12 @@ void launch_imu_init(DFilter* f, const vmp_imu* imus, int n, const vmp_config& c
                      cudaStream_t st);
 void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st);
 // ---- k_predict.cu
+// The predict chain: launch_predict_state (the state chain, per-step F / G
+// data and the pose cache), then launch_predict_cov (the covariance chain;
+// only the residual kernel's gate and the map batch read P);
+// launch_predict_chain2 launches both on one stream.
+void launch_predict_state(DFilter* f, DScan& s, cudaStream_t st);
+void launch_predict_cov(DFilter* f, DScan& s, cudaStream_t st);
 void launch_predict_chain2(DFilter* f, DScan& s, cudaStream_t st);
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st);
 void launch_update_begin(DFilter* f, cudaStream_t st);

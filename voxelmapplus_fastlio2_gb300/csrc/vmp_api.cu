@@ -367,7 +367,7 @@ struct vmp_stream_s {
     // the IMU predict chain runs beside the time sort (they share no data):
     // forked onto st_side and joined before the undistortion
     cudaStream_t st_side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_cov = nullptr;
     // CUDA-event profiler (vmp_profile_enable): per pipeline phase, events on
     // the stream's own CUDA stream, resolved after the call's final sync
     struct ProfRec { int slot; int items_kind; cudaEvent_t a, b; };
@@ -537,6 +537,7 @@ vmp_status vmp_destroy(vmp_stream_t s) {
     if (s->done_ev) cudaEventDestroy(s->done_ev);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->ev_cov) cudaEventDestroy(s->ev_cov);
     if (s->st_side) cudaStreamDestroy(s->st_side);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
@@ -580,6 +581,7 @@ vmp_status vmp_create(const vmp_config* cfg_in, vmp_stream_t* out) {
     CREATE_TRY(cudaStreamCreateWithFlags(&s->st_side, cudaStreamNonBlocking));
     CREATE_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     CREATE_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    CREATE_TRY(cudaEventCreateWithFlags(&s->ev_cov, cudaEventDisableTiming));
     const int max_pts = cfg.max_scan_points;
     const int max_imu = cfg.max_imu_per_scan;
     s->sin_deg = std::sin(cfg.angle_cov * 0.017453293);  // pcl_macros.h DEG2RAD
@@ -933,11 +935,14 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
         s->pbeg();
         launch_predict_chain2(s->f, s->s, st);
         s->pend(VMP_PROF_PREDICT, -1);
-    } else {  // the predict chain beside the time sort
+    } else {  // the predict chain beside the time sort; its covariance chain
+              // beside everything up to the first reader of P (ev_cov)
         cudaEventRecord(s->ev_fork, st);
         cudaStreamWaitEvent(s->st_side, s->ev_fork, 0);
-        launch_predict_chain2(s->f, s->s, s->st_side);
+        launch_predict_state(s->f, s->s, s->st_side);
         cudaEventRecord(s->ev_join, s->st_side);
+        launch_predict_cov(s->f, s->s, s->st_side);
+        cudaEventRecord(s->ev_cov, s->st_side);
         launch_time_sort(s->s, nb, s->ss, st);
         cudaStreamWaitEvent(st, s->ev_join, 0);
     }
@@ -945,6 +950,7 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     launch_undistort(s->f, s->s, nb, st);
     s->pend(VMP_PROF_UNDISTORT, 0);
     if (map_init) {
+        if (!s->prof_on) cudaStreamWaitEvent(st, s->ev_cov, 0);
         s->pbeg();
         launch_map_batch(s->f, s->s, nb, true, cfg.ranging_cov, s->sin_deg, st);
         s->pend(VMP_PROF_MAP_BATCH, 0);
@@ -957,6 +963,7 @@ static void enqueue_scan_front(vmp_stream_t s, int nb, bool map_init) {
     s->pbeg();
     launch_body_cov(s->s, nb, cfg.ranging_cov, s->sin_deg, st);
     s->pend(VMP_PROF_BODY_COV, 1);
+    if (!s->prof_on) cudaStreamWaitEvent(st, s->ev_cov, 0);
     s->pbeg();
     launch_update_begin(s->f, st);
     s->pend(VMP_PROF_UPDATE_OTHER, -1);
