@@ -368,6 +368,40 @@ def test_graph_and_direct_launches_agree(lio_mod, evicting):
     assert out[0][1] == out[1][1]
 
 
+@pytest.mark.parametrize("graphs", [1, 0])
+def test_shuffled_scans_give_the_same_results(lio_mod, graphs):
+    """The points of every scan in a random order instead of time order.  The
+    time sort's passes then run in full (on time-ordered scans they return at
+    once: the stable sort is the identity), and since the point times are
+    distinct they give back the time order: every result and the final map
+    equal those of the time-ordered scans, bit for bit."""
+    from voxelmapplus_fastlio2_gb300 import abi as A
+    seq = synth.Sequence(synth.KIND_URBAN, points_per_scan=30000)
+    cfg = A.default_config(scan_resolution=0.1, map_capacity=300000, max_scan_points=40000, ieskf_max_iter=4)
+    pkgs = [seq.next() for _ in range(10)]
+    rng = np.random.default_rng(0x5EED)
+    shuffled = []
+    for p in pkgs:
+        pts = p.points_np()
+        assert np.all(np.diff(pts[:, 3]) > 0)  # generated in time order, distinct times
+        perm = rng.permutation(p.n)
+        arr = (A.vmp_point * p.n).from_buffer_copy(np.ascontiguousarray(pts[perm], dtype=np.float32).tobytes())
+        shuffled.append(synth.Package(arr, p.n, p.t_start, p.t_end, p.imus, p.n_imu))
+    out = []
+    for run in (pkgs, shuffled):
+        g = lio_mod.LIOBuilder(cfg)
+        g.lib.vmp_set_graphs(g.h, graphs)
+        res = []
+        for q in run:
+            r = g.process(q)
+            res.append((r.lio_status, r.iters, r.effect_num, r.n_down, r.map_size, bytes(r.x), bytes(r.P)))
+        v, n = g.map.export()
+        out.append((res, C.string_at(v, n * C.sizeof(A.vmp_voxel))))
+        g.close()
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
+
+
 def test_undistort_and_predict_chain_match_oracle(lio_mod, oracle_lib):
     """undistortCloud after IMU init + map init: the time-sorted compensated
     cloud and the filter state / covariance at the scan end."""

@@ -24,12 +24,20 @@ __device__ inline uint32_t float_order_key(float f) {
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
-__global__ void k_time_keys(const float4* __restrict__ raw, const int* d_n, uint32_t* k, uint32_t* v) {
+// Also records whether the keys are out of order anywhere: point clouds of
+// spinning and Livox sensors come in time order, and then the stable time
+// sort is the identity and its passes return at once.
+__global__ void k_time_keys(const float4* __restrict__ raw, const int* d_n, uint32_t* k, uint32_t* v,
+                            int* unsorted) {
     const int n = *d_n;
+    bool down = false;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        k[i] = float_order_key(raw[i].w);
+        const uint32_t ki = float_order_key(raw[i].w);
+        k[i] = ki;
         v[i] = (uint32_t)i;
+        if (i > 0 && ki < float_order_key(raw[i - 1].w)) down = true;
     }
+    if (__any_sync(0xffffffffu, down) && (threadIdx.x & 31) == 0) *unsorted = 1;
 }
 // Applies the time-sort permutation to the points and their intensities.
 __global__ void k_gather4(const float4* __restrict__ src, const float* __restrict__ src_int,
@@ -51,8 +59,9 @@ static int grid_for(int n_max) {
 
 void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st) {
     int g = grid_for(n_max);
-    VMP_NOTE_LAUNCH(); k_time_keys<<<g, kPtThreads, 0, st>>>(s.raw, s.d_n_raw, s.sort_k, s.sort_v);
-    radix_sort_pairs(s.sort_k, s.sort_v, s.d_n_raw, 32, ss, st);
+    VMP_NOTE_LAUNCH();
+    k_time_keys<<<g, kPtThreads, 0, st>>>(s.raw, s.d_n_raw, s.sort_k, s.sort_v, &s.hdr->time_unsorted);
+    radix_sort_pairs(s.sort_k, s.sort_v, s.d_n_raw, 32, ss, st, &s.hdr->time_unsorted);
     VMP_NOTE_LAUNCH(); k_gather4<<<g, kPtThreads, 0, st>>>(s.raw, s.raw_int, s.sort_v, s.d_n_raw, s.cloud, s.cloud_int);
 }
 

@@ -25,8 +25,9 @@ long long& dev_bytes_counter() {
 }
 
 __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __restrict__ d_n, int shift,
-                             uint32_t* __restrict__ hist, int blocks) {
+                             uint32_t* __restrict__ hist, int blocks, const int* need) {
     __shared__ uint32_t cnt[256];
+    if (need && *need == 0) return;  // uniform
     const int n = *d_n;
     cnt[threadIdx.x] = 0;
     __syncthreads();
@@ -41,7 +42,8 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __res
 
 // Exclusive scan of each digit's tile counts, one warp per digit, in place;
 // the digit totals go to row_total.
-__global__ void k_radix_scan_rows(uint32_t* hist, int blocks, uint32_t* row_total) {
+__global__ void k_radix_scan_rows(uint32_t* hist, int blocks, uint32_t* row_total, const int* need) {
+    if (need && *need == 0) return;  // uniform
     const int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (d >= 256) return;
     uint32_t* row = hist + (size_t)d * blocks;
@@ -65,8 +67,9 @@ __device__ inline uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot, 
 __global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                 const int* __restrict__ d_n, int shift, const uint32_t* __restrict__ hist,
-                                const uint32_t* __restrict__ row_total, int blocks) {
+                                const uint32_t* __restrict__ row_total, int blocks, const int* need) {
     constexpr int W = kSortThreads / 32;
+    if (need && *need == 0) return;  // uniform
     static_assert(kSortThreads == 256, "one thread per digit");
     __shared__ uint32_t wcnt[W][256];
     __shared__ uint32_t dbase[256];
@@ -137,7 +140,8 @@ void sort_scratch_free(SortScratch& s) {
 }
 
 __global__ void k_copy_pairs(const uint32_t* __restrict__ ks, const uint32_t* __restrict__ vs, uint32_t* kd,
-                             uint32_t* vd, const int* d_n) {
+                             uint32_t* vd, const int* d_n, const int* need) {
+    if (need && *need == 0) return;  // uniform: the pairs never left keys / vals
     const int n = *d_n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         kd[i] = ks[i];
@@ -145,24 +149,26 @@ __global__ void k_copy_pairs(const uint32_t* __restrict__ ks, const uint32_t* __
     }
 }
 
-void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, SortScratch& s, cudaStream_t st) {
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, SortScratch& s, cudaStream_t st,
+                      const int* need) {
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
     if (passes > 4) passes = 4;
     uint32_t *ka = keys, *va = vals, *kb = s.k_alt, *vb = s.v_alt;
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
-        VMP_NOTE_LAUNCH(); k_radix_hist<<<s.blocks, kSortThreads, 0, st>>>(ka, d_n, shift, s.hist, s.blocks);
-        VMP_NOTE_LAUNCH(); k_radix_scan_rows<<<8, 1024, 0, st>>>(s.hist, s.blocks, s.row_total);
+        VMP_NOTE_LAUNCH(); k_radix_hist<<<s.blocks, kSortThreads, 0, st>>>(ka, d_n, shift, s.hist, s.blocks, need);
+        VMP_NOTE_LAUNCH(); k_radix_scan_rows<<<8, 1024, 0, st>>>(s.hist, s.blocks, s.row_total, need);
         VMP_NOTE_LAUNCH();
-        k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.row_total, s.blocks);
+        k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.row_total, s.blocks,
+                                                            need);
         uint32_t* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
     }
     if (ka != keys) {  // odd pass count: the result is in the alternate buffers
         int g = (s.n_max + 255) / 256;
         if (g > 152 * 8) g = 152 * 8;
-        VMP_NOTE_LAUNCH(); k_copy_pairs<<<g, 256, 0, st>>>(ka, va, keys, vals, d_n);
+        VMP_NOTE_LAUNCH(); k_copy_pairs<<<g, 256, 0, st>>>(ka, va, keys, vals, d_n, need);
     }
 }
 

@@ -18,6 +18,8 @@ struct DScanHdr {
     int n_imu;
     double t_start;
     double t_end;
+    int time_unsorted;  // 0 from the host; k_time_keys sets 1 if a point time decreases
+    int pad;
 };
 
 struct DScan {

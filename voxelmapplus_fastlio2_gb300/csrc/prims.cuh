@@ -37,8 +37,11 @@ void scan_scratch_free(ScanScratch& s);
 
 // Sorts keys/vals (length *d_n <= s.n_max) by the low `bits` key bits,
 // stably.  The result is left in keys/vals (in place; s holds the alternate
-// buffers).
-void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, SortScratch& s, cudaStream_t st);
+// buffers).  need (device, may be null): when it holds 0 the keys are known
+// to be in non-decreasing order already, so the stable sort is the identity
+// and every pass returns at once.
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, SortScratch& s, cudaStream_t st,
+                      const int* need = nullptr);
 
 // out[i] = sum_{j<i} in[i] for i < *d_n; *d_total = sum (may alias nothing).
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, const int* d_n, int* d_total, ScanScratch& s,

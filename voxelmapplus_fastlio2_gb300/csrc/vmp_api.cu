@@ -832,6 +832,8 @@ static vmp_status upload_header(vmp_stream_t s, int n, int n_imu, double t_start
     s->h_hdr->n_imu = n_imu;
     s->h_hdr->t_start = t_start;
     s->h_hdr->t_end = t_end;
+    s->h_hdr->time_unsorted = 0;
+    s->h_hdr->pad = 0;
     VMP_TRY(cudaMemcpyAsync(s->s.hdr, s->h_hdr, sizeof(DScanHdr), cudaMemcpyHostToDevice, s->st), "header");
     s->io_h2d += (long long)sizeof(DScanHdr);
     return VMP_OK;
