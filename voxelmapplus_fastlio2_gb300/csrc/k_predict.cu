@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
                                                                  DStep* st) {
     const int n_imu = hdr->n_imu;
     const double t_begin = hdr->t_start, t_end = hdr->t_end;
-    __shared__ double sNM[4], sMx[6], sQd[12];
+    __shared__ double sMx[6], sQd[12];
     __shared__ double sBg[3], sBa[3], sG[3], sRot0[9], sVel0[3], sPos0[3], sRotF[9], sVelF[3], sPosF[3];
     __shared__ int sPosOf[1024];
     __shared__ int sS;
@@ -144,12 +144,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
     }
     if (t < 9) sRot0[t] = f->x.rot[t];
     __syncthreads();
-    if (t == 0) {
-        double Nx[6];
-        s2_Mx(sG, sMx);
-        s2_Nx(sG, Nx);
-        mm<2, 3, 2>(Nx, sMx, sNM);
-    }
+    if (t == 64) s2_Mx(sG, sMx);  // beside warp 0's compaction below
     // ---- phase 0: active IMU pairs (tail at or after the last scan end), compacted in order
     if (warp == 0) {
         int running = 0;
@@ -199,24 +194,38 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
         d.pose = 0;
     }
     __syncthreads();
-    // ---- phase 1: per-step terms that do not involve the rotation (one lane per step)
-    for (int s = t; s < NS; s += blockDim.x) {
-        DStep& d = st[s];
-        double w[3], Jr[9], GQ[9];
-        for (int a = 0; a < 3; ++a) w[a] = (d.gyro[a] - sBg[a]) * d.dt;
-        so3_exp(w, d.E);
-        so3_right_jac(w, Jr);
-        for (int q = 0; q < 9; ++q) d.nJr[q] = (-Jr[q]) * d.dt;
-        for (int a = 0; a < 3; ++a) d.ab[a] = d.acc[a] - sBa[a];
-        for (int q = 0; q < 6; ++q) d.Mxdt[q] = sMx[q] * d.dt;
-        for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) GQ[a * 3 + c] = d.nJr[a * 3 + c] * sQd[c];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b)
-                d.B[a * 3 + b] = (GQ[a * 3] * d.nJr[b * 3] + GQ[a * 3 + 1] * d.nJr[b * 3 + 1]) + GQ[a * 3 + 2] * d.nJr[b * 3 + 2];
-        for (int a = 0; a < 3; ++a) {
-            d.B[18 + a] = (d.dt * sQd[6 + a]) * d.dt;
-            d.B[21 + a] = (d.dt * sQd[9 + a]) * d.dt;
+    // ---- phase 1: per-step terms that do not involve the rotation, one lane
+    // per step: Exp(w) on warps 0.., the right Jacobian and its products on
+    // the warps after them (the two are independent)
+    // threads per role: whole warps, at most half the block
+    const int role = min(((NS + 31) / 32) * 32, (int)(blockDim.x / 64) * 32);
+    {
+        if (t < role) {
+            for (int s = t; s < NS; s += role) {
+                DStep& d = st[s];
+                double w[3];
+                for (int a = 0; a < 3; ++a) w[a] = (d.gyro[a] - sBg[a]) * d.dt;
+                so3_exp(w, d.E);
+                for (int a = 0; a < 3; ++a) d.ab[a] = d.acc[a] - sBa[a];
+                for (int q = 0; q < 6; ++q) d.Mxdt[q] = sMx[q] * d.dt;
+            }
+        } else if (t < 2 * role) {
+            for (int s = t - role; s < NS; s += role) {
+                DStep& d = st[s];
+                double w[3], Jr[9], GQ[9];
+                for (int a = 0; a < 3; ++a) w[a] = (d.gyro[a] - sBg[a]) * d.dt;
+                so3_right_jac(w, Jr);
+                for (int q = 0; q < 9; ++q) d.nJr[q] = (-Jr[q]) * d.dt;
+                for (int a = 0; a < 3; ++a)
+                    for (int c = 0; c < 3; ++c) GQ[a * 3 + c] = d.nJr[a * 3 + c] * sQd[c];
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b)
+                        d.B[a * 3 + b] = (GQ[a * 3] * d.nJr[b * 3] + GQ[a * 3 + 1] * d.nJr[b * 3 + 1]) + GQ[a * 3 + 2] * d.nJr[b * 3 + 2];
+                for (int a = 0; a < 3; ++a) {
+                    d.B[18 + a] = (d.dt * sQd[6 + a]) * d.dt;
+                    d.B[21 + a] = (d.dt * sQd[9 + a]) * d.dt;
+                }
+            }
         }
     }
     __syncthreads();
@@ -238,61 +247,72 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_chain2(DFilter* f, con
         if (lane < 9) sRotF[lane] = r;
     }
     __syncthreads();
-    // ---- phase 3: terms that involve the step's rotation (one lane per step)
-    for (int s = t; s < NS; s += blockDim.x) {
-        DStep& d = st[s];
-        double ra[3], nr[9], H[9], T[9], GQ[9];
-        m3v(d.rot, d.ab, ra);
-        for (int a = 0; a < 3; ++a) d.vinc[a] = (ra[a] + sG[a]) * d.dt;
-        for (int q = 0; q < 9; ++q) nr[q] = -d.rot[q];
-        hat3(d.ab, H);
-        mm<3, 3, 3>(nr, H, T);
-        for (int q = 0; q < 9; ++q) { d.FRa[q] = T[q] * d.dt; d.nRdt[q] = nr[q] * d.dt; }
-        for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) GQ[a * 3 + c] = d.nRdt[a * 3 + c] * sQd[3 + c];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b)
-                d.B[9 + a * 3 + b] =
-                    (GQ[a * 3] * d.nRdt[b * 3] + GQ[a * 3 + 1] * d.nRdt[b * 3 + 1]) + GQ[a * 3 + 2] * d.nRdt[b * 3 + 2];
-    }
-    __syncthreads();
-    if (t < 3) {  // velocity / position prefix (pos uses the velocity before the step)
-        double v = sVel0[t], p = sPos0[t];
-        for (int s = 0; s < NS; ++s) {
+    // ---- phase 3: terms that involve the step's rotation, one lane per step.
+    // The warps of the second role form the F / G blocks the covariance chain
+    // needs (only k_predict_cov reads them); those of the first form the
+    // velocity increments and go on, behind a barrier of their own, to the
+    // velocity / position prefix and the pose cache the undistortion needs.
+    if (t >= role && t < 2 * role) {
+        for (int s = t - role; s < NS; s += role) {
             DStep& d = st[s];
-            p = p + v * d.dt;
-            v = v + d.vinc[t];
-            d.velA[t] = v;
-            d.posA[t] = p;
+            double nr[9], H[9], T[9], GQ[9];
+            for (int q = 0; q < 9; ++q) nr[q] = -d.rot[q];
+            hat3(d.ab, H);
+            mm<3, 3, 3>(nr, H, T);
+            for (int q = 0; q < 9; ++q) { d.FRa[q] = T[q] * d.dt; d.nRdt[q] = nr[q] * d.dt; }
+            for (int a = 0; a < 3; ++a)
+                for (int c = 0; c < 3; ++c) GQ[a * 3 + c] = d.nRdt[a * 3 + c] * sQd[3 + c];
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    d.B[9 + a * 3 + b] =
+                        (GQ[a * 3] * d.nRdt[b * 3] + GQ[a * 3 + 1] * d.nRdt[b * 3 + 1]) + GQ[a * 3 + 2] * d.nRdt[b * 3 + 2];
         }
-        sVelF[t] = v;
-        sPosF[t] = p;
-    }
-    __syncthreads();
-    // ---- pose cache (imu_poses_cache): pose 0 = state before the chain, pose s+1 after step s
-    for (int s = t; s < S; s += blockDim.x) {
-        const DStep& d = st[s];
-        const double* rotA = st[s + 1].rot;
-        DPose& p = poses[s + 1];
-        double ra[3];
-        m3v(rotA, d.ab, ra);
-        p.offset = d.offset;
-        for (int a = 0; a < 3; ++a) {
-            p.acc[a] = ra[a] + sG[a];
-            p.gyro[a] = d.gyro[a] - sBg[a];
-            p.vel[a] = d.velA[a];
-            p.pos[a] = d.posA[a];
+    } else if (t < role) {
+        for (int s = t; s < NS; s += role) {
+            DStep& d = st[s];
+            double ra[3];
+            m3v(d.rot, d.ab, ra);
+            for (int a = 0; a < 3; ++a) d.vinc[a] = (ra[a] + sG[a]) * d.dt;
         }
-        for (int q = 0; q < 9; ++q) p.rot[q] = rotA[q];
-    }
-    if (t == 0) {
-        DPose& p0 = poses[0];
-        p0.offset = 0.0;
-        for (int a = 0; a < 3; ++a) {
-            p0.acc[a] = f->last_acc[a]; p0.gyro[a] = f->last_gyro[a];
-            p0.vel[a] = sVel0[a]; p0.pos[a] = sPos0[a];
+        asm volatile("bar.sync 1, %0;" ::"r"(role) : "memory");
+        if (t < 3) {  // velocity / position prefix (pos uses the velocity before the step)
+            double v = sVel0[t], p = sPos0[t];
+            for (int s = 0; s < NS; ++s) {
+                DStep& d = st[s];
+                p = p + v * d.dt;
+                v = v + d.vinc[t];
+                d.velA[t] = v;
+                d.posA[t] = p;
+            }
+            sVelF[t] = v;
+            sPosF[t] = p;
         }
-        for (int q = 0; q < 9; ++q) p0.rot[q] = sRot0[q];
+        asm volatile("bar.sync 1, %0;" ::"r"(role) : "memory");
+        // pose cache (imu_poses_cache): pose 0 = state before the chain, pose s+1 after step s
+        for (int s = t; s < S; s += role) {
+            const DStep& d = st[s];
+            const double* rotA = st[s + 1].rot;
+            DPose& p = poses[s + 1];
+            double ra[3];
+            m3v(rotA, d.ab, ra);
+            p.offset = d.offset;
+            for (int a = 0; a < 3; ++a) {
+                p.acc[a] = ra[a] + sG[a];
+                p.gyro[a] = d.gyro[a] - sBg[a];
+                p.vel[a] = d.velA[a];
+                p.pos[a] = d.posA[a];
+            }
+            for (int q = 0; q < 9; ++q) p.rot[q] = rotA[q];
+        }
+        if (t == 0) {
+            DPose& p0 = poses[0];
+            p0.offset = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                p0.acc[a] = f->last_acc[a]; p0.gyro[a] = f->last_gyro[a];
+                p0.vel[a] = sVel0[a]; p0.pos[a] = sPos0[a];
+            }
+            for (int q = 0; q < 9; ++q) p0.rot[q] = sRot0[q];
+        }
     }
     // ---- write back (the covariance chain is k_predict_cov)
     __syncthreads();
