@@ -417,6 +417,10 @@ __global__ void __launch_bounds__(kIekfThreads, MINB) k_residual(DFilter* f, DSc
     __shared__ double s_rwl[9], s_pwl[3], s_rot[9], s_rext[9], s_pext[3], s_prr[9], s_ppp[9];
     if (f->converged) return;  // written by the previous launch; uniform
     const int n = *s.d_n_down;
+    // the grid is sized for the stream's largest scan: blocks past this
+    // scan's points return (the fold reads the partials of the others; block
+    // 0 always writes one)
+    if (blockIdx.x > 0 && (long long)blockIdx.x * blockDim.x >= n) return;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) {
         const DState& x = f->x;
@@ -516,10 +520,12 @@ __global__ void __launch_bounds__(kFoldThreads) k_residual_fold(DFilter* f, DSca
         else if (t < 41) sm.D.e[t - 32] = f->bmx_D[9 + t - 32];
         else if (t < 45) sm.D.g[t - 41] = f->bmx_D[18 + t - 41];
     }
+    // the blocks of the grid that held points (k_residual's others return)
+    const int Gw = max(1, min(G, (*s.d_n_down + kIekfThreads - 1) / kIekfThreads));
     if (t < R::STRIPES * R::NV) {
         const int q = t / R::NV, k = t - q * R::NV;
         double x = 0.0;
-        for (int b = q; b < G; b += R::STRIPES) x = x + s.partials[b * kPartStride2 + k];
+        for (int b = q; b < Gw; b += R::STRIPES) x = x + s.partials[b * kPartStride2 + k];
         s_red[q * R::NV + k] = x;
     }
     __syncthreads();
