@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(256, 3) k_undistort(const DFilter* __restrict_
     __shared__ double s_off[1024];
     __shared__ DState cur;
     const int n = *d_n;
+    if (blockIdx.x > 0 && (long long)blockIdx.x * blockDim.x >= n) return;  // past the points: no setup either
     const int npose = f->npose;
     if (npose > 1024) return;  // bounded by max_imu (checked on the host)
     for (int i = threadIdx.x; i < npose; i += blockDim.x) s_off[i] = poses[i].offset;

@@ -285,6 +285,7 @@ __global__ void __launch_bounds__(kPtThreads, 3) k_map_batch(const DFilter* __re
     __shared__ float sR[9], sT[3];
     __shared__ double rwl[9], prr[9], ppp[9];
     const int n = *d_n;
+    if (blockIdx.x > 0 && (long long)blockIdx.x * blockDim.x >= n) return;  // past the points: no setup either
     if (threadIdx.x == 0) {
         const DState& x = f->x;
         mm<3, 3, 3>(x.rot, x.rot_ext, rwl);

@@ -29,6 +29,9 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __res
     __shared__ uint32_t cnt[256];
     if (need && *need == 0) return;  // uniform
     const int n = *d_n;
+    // the grid covers the largest n: tiles past this n hold nothing, and
+    // k_radix_scan_rows / k_radix_scatter read only the tiles that do
+    if (blockIdx.x > 0 && (long long)blockIdx.x * kSortTile >= n) return;
     cnt[threadIdx.x] = 0;
     __syncthreads();
     const int base = blockIdx.x * kSortTile;
@@ -42,21 +45,23 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, const int* __res
 
 // Exclusive scan of each digit's tile counts, one warp per digit, in place;
 // the digit totals go to row_total.
-__global__ void k_radix_scan_rows(uint32_t* hist, int blocks, uint32_t* row_total, const int* need) {
+__global__ void k_radix_scan_rows(uint32_t* hist, int blocks, uint32_t* row_total, const int* need,
+                                  const int* d_n) {
     if (need && *need == 0) return;  // uniform
     const int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (d >= 256) return;
+    const int used = max(1, min(blocks, (*d_n + kSortTile - 1) / kSortTile));  // tiles that hold keys
     uint32_t* row = hist + (size_t)d * blocks;
     uint32_t carry = 0;
-    for (int base = 0; base < blocks; base += 32) {
+    for (int base = 0; base < used; base += 32) {
         const int i = base + lane;
-        const uint32_t v = i < blocks ? row[i] : 0u;
+        const uint32_t v = i < used ? row[i] : 0u;
         uint32_t x = v;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
-        if (i < blocks) row[i] = carry + x - v;
+        if (i < used) row[i] = carry + x - v;
         carry += __shfl_sync(0xffffffffu, x, 31);
     }
     if (lane == 0) row_total[d] = carry;
@@ -70,6 +75,7 @@ __global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t
                                 const uint32_t* __restrict__ row_total, int blocks, const int* need) {
     constexpr int W = kSortThreads / 32;
     if (need && *need == 0) return;  // uniform
+    if ((long long)blockIdx.x * kSortTile >= *d_n) return;  // a tile past the keys: nothing to place
     static_assert(kSortThreads == 256, "one thread per digit");
     __shared__ uint32_t wcnt[W][256];
     __shared__ uint32_t dbase[256];
@@ -158,7 +164,7 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, const int* d_n, int bits, 
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
         VMP_NOTE_LAUNCH(); k_radix_hist<<<s.blocks, kSortThreads, 0, st>>>(ka, d_n, shift, s.hist, s.blocks, need);
-        VMP_NOTE_LAUNCH(); k_radix_scan_rows<<<8, 1024, 0, st>>>(s.hist, s.blocks, s.row_total, need);
+        VMP_NOTE_LAUNCH(); k_radix_scan_rows<<<8, 1024, 0, st>>>(s.hist, s.blocks, s.row_total, need, d_n);
         VMP_NOTE_LAUNCH();
         k_radix_scatter<<<s.blocks, kSortThreads, 0, st>>>(ka, va, kb, vb, d_n, shift, s.hist, s.row_total, s.blocks,
                                                             need);
@@ -201,6 +207,8 @@ __global__ void k_scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restri
                              uint32_t* __restrict__ block_sums) {
     __shared__ uint32_t warp_tot[32];
     const int n = *d_n;
+    // tiles past n: k_scan_top and k_scan_add read only the tiles that hold values
+    if (blockIdx.x > 0 && (long long)blockIdx.x * kScanTile >= n) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t s = 0;
@@ -244,6 +252,7 @@ __global__ void k_scan_top(uint32_t* block_sums, int blocks, const int* d_n, int
 
 __global__ void k_scan_add(uint32_t* __restrict__ out, const int* d_n, const uint32_t* __restrict__ block_sums) {
     const int n = *d_n;
+    if ((long long)blockIdx.x * kScanTile >= n) return;
     const uint32_t add = block_sums[blockIdx.x];
     const int base = blockIdx.x * kScanTile;
     for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
