@@ -273,6 +273,19 @@ __device__ inline void tr(const double* A, double* O) {
         for (int j = 0; j < C; ++j) O[j * R + i] = A[i * C + j];
 }
 __device__ inline void m3v(const double* A, const double* v, double* o) { mm<3, 3, 1>(A, v, o); }
+// Entry e = i * 3 + j of mm<3, 3, 3>(A, B, .) and entry i of m3v(A, v, .),
+// the same operations in the same order (one thread per entry).
+__device__ inline double mm3_entry(const double* A, const double* B, int e) {
+    const int i = e / 3, j = e - 3 * (e / 3);
+    double s = __dmul_rn(A[i * 3], B[j]);
+    s = __dadd_rn(s, __dmul_rn(A[i * 3 + 1], B[3 + j]));
+    return __dadd_rn(s, __dmul_rn(A[i * 3 + 2], B[6 + j]));
+}
+__device__ inline double m3v_entry(const double* A, const double* v, int i) {
+    double s = __dmul_rn(A[i * 3], v[0]);
+    s = __dadd_rn(s, __dmul_rn(A[i * 3 + 1], v[1]));
+    return __dadd_rn(s, __dmul_rn(A[i * 3 + 2], v[2]));
+}
 __device__ inline double dot3(const double* a, const double* b) {
     return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
 }

@@ -422,12 +422,11 @@ __global__ void __launch_bounds__(kIekfThreads, MINB) k_residual(DFilter* f, DSc
     // 0 always writes one)
     if (blockIdx.x > 0 && (long long)blockIdx.x * blockDim.x >= n) return;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    if (t == 0) {
-        const DState& x = f->x;
-        mm<3, 3, 3>(x.rot, x.rot_ext, s_rwl);
-        double rp[3];
-        m3v(x.rot, x.pos_ext, rp);
-        for (int a = 0; a < 3; ++a) s_pwl[a] = rp[a] + x.pos[a];
+    // R_wl = rot rot_ext and p_wl = rot pos_ext + pos, one entry per thread
+    if (t < 9) {
+        s_rwl[t] = mm3_entry(f->x.rot, f->x.rot_ext, t);
+    } else if (t < 12) {
+        s_pwl[t - 9] = m3v_entry(f->x.rot, f->x.pos_ext, t - 9) + f->x.pos[t - 9];
     } else if (t >= 32 && t < 41) {
         const int a = t - 32;
         s_rot[a] = f->x.rot[a];

@@ -286,18 +286,18 @@ __global__ void __launch_bounds__(kPtThreads, 3) k_map_batch(const DFilter* __re
     __shared__ double rwl[9], prr[9], ppp[9];
     const int n = *d_n;
     if (blockIdx.x > 0 && (long long)blockIdx.x * blockDim.x >= n) return;  // past the points: no setup either
-    if (threadIdx.x == 0) {
-        const DState& x = f->x;
-        mm<3, 3, 3>(x.rot, x.rot_ext, rwl);
-        double rp[3];
-        m3v(x.rot, x.pos_ext, rp);
-        for (int a = 0; a < 9; ++a) sR[a] = (float)rwl[a];
-        for (int a = 0; a < 3; ++a) sT[a] = (float)(rp[a] + x.pos[a]);
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                prr[i * 3 + j] = f->P[(3 + i) * 23 + 3 + j];
-                ppp[i * 3 + j] = f->P[i * 23 + j];
-            }
+    // R_wl = rot rot_ext and p_wl = rot pos_ext + pos (one entry per
+    // thread), their float casts, and the P blocks
+    const int t = threadIdx.x;
+    if (t < 9) {
+        rwl[t] = mm3_entry(f->x.rot, f->x.rot_ext, t);
+        sR[t] = (float)rwl[t];
+    } else if (t < 12) {
+        sT[t - 9] = (float)(m3v_entry(f->x.rot, f->x.pos_ext, t - 9) + f->x.pos[t - 9]);
+    } else if (t >= 32 && t < 41) {
+        const int i = (t - 32) / 3, j = (t - 32) % 3;
+        prr[i * 3 + j] = f->P[(3 + i) * 23 + 3 + j];
+        ppp[i * 3 + j] = f->P[i * 23 + j];
     }
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
