@@ -514,7 +514,7 @@ typedef struct vmp_server_config {
     int queue_depth;            /* queued packages per stream before vmp_submit answers VMP_ERR_CAPACITY (default 64) */
     int autotune;               /* 1 (default): tune the launch shape of the served merge resolution online */
     int merge_grid_divisor;     /* served merge launches use SMs / divisor CTAs (0: 16); autotune's start */
-    int seg_grid_blocks;        /* working blocks of the voxel-chain kernels while the server runs (0: 304); autotune's start */
+    int seg_grid_blocks;        /* working blocks of the voxel-chain kernels while the server runs (0: 304, at most 304); autotune's start */
     int reserved[4];
 } vmp_server_config;
 
@@ -535,9 +535,9 @@ void vmp_server_config_default(vmp_server_config* c);
  * starting shapes, the best measured ones) -- merge_grid_divisor (served
  * merge launches use SMs / d CTAs, d in 4..64; process-wide), max_inflight
  * (packages on the GPU at once: 8, 16, 24 or 32 of the workers) and
- * seg_grid_blocks (blocks of the voxel-chain kernels that take work: 152,
- * 304, 608, 1216 or 2432; process-wide, device-side, back to all blocks when
- * the last server is destroyed).  None changes results, and none needs the
+ * seg_grid_blocks (blocks of the voxel-chain kernels that take work: 76, 152
+ * or 304, the launches' size under a server; process-wide, device-side, back
+ * to all blocks when the last server is destroyed).  None changes results, and none needs the
  * streams' scan graphs captured again.  vmp_server_tuning: the merge divisor
  * in use, the windows measured so far and the best rate seen (packages/s);
  * vmp_server_knob: "merge_grid_divisor", "max_inflight", "seg_grid_blocks"
@@ -552,10 +552,10 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value);
  * this one alone. */
 vmp_status vmp_set_residual_ctas_per_sm(int ctas);
 /* Test hook: the autotuner's climb on a model instead of a GPU (no CUDA
- * call).  rates[(i * 4 + j) * 5 + k]: packages/s with merge divisor
+ * call).  rates[(i * 4 + j) * 3 + k]: packages/s with merge divisor
  * candidate i (4, 8, 16, 32, 64), max_inflight candidate j (8, 16, 24, 32)
- * and seg_grid_blocks candidate k (152, 304, 608, 1216, 2432); trace
- * (3 x windows ints): the three knobs after each window. */
+ * and seg_grid_blocks candidate k (76, 152, 304); trace (3 x windows ints):
+ * the three knobs after each window. */
 vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, int seg_blocks, const double* rates, int windows,
                              int* trace);
 vmp_status vmp_server_create(const vmp_server_config* c, vmp_server_t* out);

@@ -1117,6 +1117,7 @@ void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double*
     // blocks work)
     int sg = (n_max + (kSegThreads / 32) - 1) / (kSegThreads / 32);
     if (sg > 152 * 16) sg = 152 * 16;
+    if (seg_grid_blocks() > 0 && sg > kSegServedBlocks) sg = kSegServedBlocks;  // blocks past it would return
     if (sg < 1) sg = 1;
     const int cg = sg;
     SegScratch ss{static_cast<RefitSnap*>(ms.seg_snaps), ms.refit_list, static_cast<CovSeg*>(ms.covsegs),

@@ -197,6 +197,9 @@ bool merge_throughput_mode();
 // working blocks of the voxel-chain kernels (0: all); process-wide, device-side
 cudaError_t seg_set_grid_blocks(int blocks);
 int seg_grid_blocks();
+// While that is set (a server runs) the voxel-chain launches have at most this
+// many blocks: the largest working-block count the serving tuner picks.
+constexpr int kSegServedBlocks = 304;
 // Served merge launches use SMs / d CTAs (process-wide; 16 by default).
 void merge_set_grid_divisor(int d);
 // Writes the reciprocal table of the voxel state machine on the current

@@ -130,7 +130,8 @@ struct KnobClimb {
 //                       fewer contend less for the hardware work queues,
 //                       more overlap more;
 //   seg_grid_blocks     blocks of the voxel-chain kernels that take work
-//                       (a device-side value the captured launches read):
+//                       (a device-side value the captured launches read;
+//                       they have 304 blocks while a server runs):
 //                       fewer leave more SM slots to other streams' kernels,
 //                       more run more of one scan's chains at once.
 struct Autotuner {
@@ -192,14 +193,14 @@ static void model_set_d(int d) { g_model_d = d; }
 static void model_set_c(int c) { g_model_c = c; }
 static void model_set_s(int b) { g_model_s = b; }
 
-constexpr int kDefaultSegBlocks = 304;  // 2 per SM: the best of 152 .. 2432 on the 64-stream mix
+constexpr int kDefaultSegBlocks = 304;  // 2 per SM: of 152 .. 2432 on the 64-stream mix, 152-304 were best
 
 static Autotuner make_tuner(int merge_divisor, int inflight, int seg_blocks, std::function<void(int)> set_d,
                             std::function<void(int)> set_c, std::function<void(int)> set_s) {
     Autotuner t;
     t.knobs.push_back(KnobClimb{"merge_grid_divisor", {4, 8, 16, 32, 64}, set_d});
     t.knobs.push_back(KnobClimb{"max_inflight", {8, 16, 24, 32}, set_c});
-    t.knobs.push_back(KnobClimb{"seg_grid_blocks", {152, 304, 608, 1216, 2432}, set_s});
+    t.knobs.push_back(KnobClimb{"seg_grid_blocks", {76, 152, 304}, set_s});
     t.knobs[0].set_nearest(merge_divisor);
     t.knobs[1].set_nearest(inflight);
     t.knobs[2].set_nearest(seg_blocks);
@@ -644,10 +645,10 @@ vmp_status vmp_server_knob(vmp_server_t sv, const char* name, int* value) {
 }
 
 // Test hook: the autotuner's climb on a model throughput instead of a GPU.
-// rates[(i * 4 + j) * 5 + k]: packages/s with merge divisor candidate i (4,
+// rates[(i * 4 + j) * 3 + k]: packages/s with merge divisor candidate i (4,
 // 8, 16, 32, 64), max_inflight candidate j (8, 16, 24, 32) and
-// seg_grid_blocks candidate k (152, 304, 608, 1216, 2432); completions are
-// spaced by 1 / rate.  trace[3 * w .. 3 * w + 2]: the three knobs after
+// seg_grid_blocks candidate k (76, 152, 304); completions are spaced by
+// 1 / rate.  trace[3 * w .. 3 * w + 2]: the three knobs after
 // window w.
 vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, int seg_blocks, const double* rates, int windows,
                              int* trace) {
@@ -665,7 +666,7 @@ vmp_status vmp_test_autotune(int merge_divisor, int max_inflight, int seg_blocks
         int si = 0;
         for (int i = 0; i < (int)t.knobs[2].cand.size(); ++i)
             if (t.knobs[2].cand[i] == g_model_s) si = i;
-        const double r = rates[(di * 4 + ci) * 5 + si];
+        const double r = rates[(di * 4 + ci) * 3 + si];
         if (!(r > 0.0)) return VMP_ERR_INVALID_ARG;
         now += 1000.0 / r;
         const long long before = t.windows;
