@@ -300,6 +300,7 @@ void launch_undistort(DFilter* f, DScan& s, int n_max, cudaStream_t st) {
     int blocks = (n_max + 255) / 256;
     if (blocks > 1216) blocks = 1216;
     if (blocks < 1) blocks = 1;
+    blocks = served_grid(blocks);
     VMP_NOTE_LAUNCH(); k_undistort<<<blocks, 256, 0, st>>>(f, s.poses, s.cloud, s.d_n_raw);
 }
 void launch_ieskf_predict_once(DFilter* f, const double* acc, const double* gyro, double dt, cudaStream_t st) {

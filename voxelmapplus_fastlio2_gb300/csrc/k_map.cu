@@ -33,7 +33,7 @@ constexpr int kSegThreads = 128;  // 4 warps: 4 x 32 x 36 doubles of refit stagi
 static int grid_for_map(int n) {
     int b = (n + kMapThreads - 1) / kMapThreads;
     if (b > 152 * 8) b = 152 * 8;
-    return b < 1 ? 1 : b;
+    return b < 1 ? 1 : served_grid(b);
 }
 
 // Blocks of k_seg_chain and k_seg_cov that take work.  The launches keep
@@ -1132,11 +1132,13 @@ void launch_map_state(DMap& m, MapScratch& ms, const double* bpts, const double*
     int eg = (n_max + 255) / 256;
     if (eg > 152 * 8) eg = 152 * 8;
     if (eg < 1) eg = 1;
+    eg = served_grid(eg);
     VMP_NOTE_LAUNCH();
     k_refit_eig<<<eg, 32, 0, st>>>(m, ss);
     int tg = (2 * n_max + kTermThreads - 1) / kTermThreads;
     if (tg > 152 * 8) tg = 152 * 8;
     if (tg < 1) tg = 1;
+    tg = served_grid(tg);
     VMP_NOTE_LAUNCH();
     k_cov_terms<<<tg, kTermThreads, 0, st>>>(m, ms.seg_start, ms.sv, bpts, bcov, ss);
     VMP_NOTE_LAUNCH();

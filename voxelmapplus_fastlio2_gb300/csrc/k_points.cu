@@ -54,7 +54,7 @@ __global__ void k_gather4(const float4* __restrict__ src, const float* __restric
 static int grid_for(int n_max) {
     int b = (n_max + kPtThreads - 1) / kPtThreads;
     if (b > 152 * 8) b = 152 * 8;
-    return b < 1 ? 1 : b;
+    return b < 1 ? 1 : served_grid(b);
 }
 
 void launch_time_sort(DScan& s, int n_max, SortScratch& ss, cudaStream_t st) {
