@@ -200,11 +200,12 @@ int seg_grid_blocks();
 // While that is set (a server runs) the voxel-chain launches have at most this
 // many blocks: the largest working-block count the serving tuner picks.
 constexpr int kSegServedBlocks = 304;
-// Grid of an element-wise (grid-stride) kernel while a server runs: at most 2
-// blocks per SM.  A stream's grids are sized for its largest scan, and most
+// Grid of an element-wise (grid-stride) kernel while a server runs: at most
+// one block per SM.  A stream's grids are sized for its largest scan, and most
 // of those blocks would find no element of a served scan; the results do not
-// depend on the grid.
-inline int served_grid(int g) { return (g > 304 && seg_grid_blocks() > 0) ? 304 : g; }
+// depend on the grid.  (On the 64-stream mix: 6455 / 6545 / 6597 scans/s with
+// at most 608 / 304 / 152 blocks.)
+inline int served_grid(int g) { return (g > 152 && seg_grid_blocks() > 0) ? 152 : g; }
 // Served merge launches use SMs / d CTAs (process-wide; 16 by default).
 void merge_set_grid_divisor(int d);
 // Writes the reciprocal table of the voxel state machine on the current
