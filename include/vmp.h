@@ -514,7 +514,7 @@ typedef struct vmp_server_config {
     int queue_depth;            /* queued packages per stream before vmp_submit answers VMP_ERR_CAPACITY (default 64) */
     int autotune;               /* 1 (default): tune the launch shape of the served merge resolution online */
     int merge_grid_divisor;     /* served merge launches use SMs / divisor CTAs (0: 16); autotune's start */
-    int seg_grid_blocks;        /* working blocks of the voxel-chain kernels while the server runs (0: 304, at most 304); autotune's start */
+    int seg_grid_blocks;        /* working blocks of the voxel-chain kernels while the server runs (0: 152, at most 304); autotune's start */
     int reserved[4];
 } vmp_server_config;
 

@@ -262,7 +262,7 @@ def test_autotuner_reports_state():
         t = srv.tuning()
         assert t["merge_grid_divisor"] in (4, 8, 16, 32, 64) and t["windows"] == 0
         assert t["max_inflight"] == 2  # starts at the workers
-        assert t["seg_grid_blocks"] == 304
+        assert t["seg_grid_blocks"] == 152
     finally:
         srv.close()
 

@@ -193,7 +193,7 @@ static void model_set_d(int d) { g_model_d = d; }
 static void model_set_c(int c) { g_model_c = c; }
 static void model_set_s(int b) { g_model_s = b; }
 
-constexpr int kDefaultSegBlocks = 304;  // 2 per SM: of 152 .. 2432 on the 64-stream mix, 152-304 were best
+constexpr int kDefaultSegBlocks = 152;  // 1 per SM: on the 64-stream mix 152 and 304 were the best of 152 .. 2432
 
 static Autotuner make_tuner(int merge_divisor, int inflight, int seg_blocks, std::function<void(int)> set_d,
                             std::function<void(int)> set_c, std::function<void(int)> set_s) {

@@ -16,7 +16,7 @@ from .lio import LIOBuilder
 
 class Server:
     def __init__(self, hbm_budget_bytes=150e9, max_streams=64, workers=32, queue_depth=64, autotune=True,
-                 merge_grid_divisor=16, seg_grid_blocks=304):
+                 merge_grid_divisor=16, seg_grid_blocks=152):
         self.lib = load()
         cfg = abi.vmp_server_config()
         self.lib.vmp_server_config_default(C.byref(cfg))
